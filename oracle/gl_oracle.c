@@ -1,0 +1,67 @@
+/*
+ * gl_oracle.c -- CPU restatement of the mepgl hot path (TEST INFRASTRUCTURE).
+ *
+ * Builds libgl_oracle.so (oracle/Makefile), loaded through ctypes by
+ * oracle/cref.py.  Never linked into the product library.  Compiled with
+ * -ffp-contract=off so results are identical on x86-64 and AArch64.
+ *
+ * Exported symbols (X = d for double, f for float):
+ *   glo_nn_map                      neighbour codes (nlcg.cu:48-103)
+ *   glo_energy_X                    per-image free energy (nlcg.cu:105-240)
+ *   glo_gradient_X                  dF/dA, dF/dpsi (nlcg.cu:504-888)
+ *   glo_polynomial_X                F(x + a d) coefficients (nlcg.cu:997-1370)
+ *   glo_line_search_X               step length (nlcg.cu:1398-1445)
+ *   glo_jb_X                        B, J observables (nlcg.cu:243-364)
+ *   glo_arc_length_X                arc length (interpolation.cu:39-140)
+ *   glo_redistribute_linear_X       linear resample (interpolation.cu:190-250)
+ *   glo_redistribute_cubic_X        cubic resample (interpolation.cu:252-481)
+ *   glo_solver_*_X                  nlcgSteps / loop() state machine
+ *                                   (nlcg.cu:1462-1586, mepgl.cu:38-391)
+ */
+#include <math.h>
+#include <stdint.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include "gl_oracle.h"
+#include "tridiag.h"
+
+#ifndef M_PI
+#define M_PI 3.14159265358979323846
+#endif
+
+MEPGL_DEFINE_GTTRF(glo_gttrf_d, double)
+MEPGL_DEFINE_GTTRS(glo_gttrs_d, double)
+
+/* Neighbour code of every site (bit order 0:+x 1:+x+y 2:+y 3:-x+y 4:-x
+ * 5:-x-y 6:-y 7:+x-y), restating buildNearestNeighbourMap
+ * (mepgl/src/nlcg.cu:48-103): a bit is set when both the site and that
+ * neighbour lie in the domain. */
+void glo_nn_map(int nx, int ny, const int32_t *domain, uint8_t *out)
+{
+    static const int di[8] = {1, 1, 0, -1, -1, -1, 0, 1};
+    static const int dj[8] = {0, 1, 1, 1, 0, -1, -1, -1};
+    for (int j = 0; j < ny; ++j)
+        for (int i = 0; i < nx; ++i) {
+            unsigned code = 0;
+            if (domain[i + nx * j] != 0)
+                for (int b = 0; b < 8; ++b) {
+                    const int ii = i + di[b], jj = j + dj[b];
+                    if (ii < 0 || ii >= nx || jj < 0 || jj >= ny) continue;
+                    if (domain[ii + nx * jj] != 0) code |= 1u << b;
+                }
+            out[i + nx * j] = (uint8_t)code;
+        }
+}
+
+#define REAL double
+#define SFX _d
+#include "gl_oracle_impl.h"
+#undef REAL
+#undef SFX
+
+#define REAL float
+#define SFX _f
+#include "gl_oracle_impl.h"
+#undef REAL
+#undef SFX
