@@ -1,0 +1,182 @@
+/*
+ * mepgl.h -- C ABI of the GB300 implementation of mepgl's string-method hot
+ * path (libmepgl_gb300.so).
+ *
+ * The reference (maiani/mepgl) has no library boundary: its host operators
+ * are C++ functions taking ~40 raw device pointers each, with the lattice
+ * size, spacing, component count and precision fixed at compile time
+ * (mepgl/src/nlcg.cuh:18-54, mepgl/src/interpolation.cuh:6-24,
+ * mepgl/src/config.cuh).  This header is the boundary that replaces them: an
+ * opaque context owns every device buffer, the compile-time constants are
+ * runtime fields of mepgl_problem, and every call returns a status instead
+ * of exiting the process (mepgl/src/cuda_errors.cuh:561-571).  Each entry
+ * point names the reference function it stands in for.
+ *
+ * Data layout (identical to the reference's device layout,
+ * mepgl/src/io.cu:69-123): site (i, j) of image n at index
+ * i + nx*j + nx*ny*n, x fastest; A, psi_1 and psi_2 are arrays of (x, y) /
+ * (Re, Im) pairs of the context's precision (float or double).  Lattice
+ * parameter arrays are nx*ny doubles in the same site order.  Per-image
+ * scalars (energies, norms, steps, arc lengths) are always double.
+ *
+ * Threading: a context is bound to the CUDA stream given at creation and is
+ * not re-entrant; use one context per stream.  Calls that return host data
+ * synchronise that stream; the others are asynchronous.
+ */
+#ifndef MEPGL_H
+#define MEPGL_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum mepgl_status {
+    MEPGL_OK = 0,
+    MEPGL_ERR_INVALID_ARG = 1,   /* bad size, pointer or option                    */
+    MEPGL_ERR_CUDA = 2,          /* a CUDA runtime call or kernel launch failed    */
+    MEPGL_ERR_NAN = 3,           /* a per-image scalar became NaN or infinite      */
+    MEPGL_ERR_IO = 4,            /* file reading / writing (npy helpers)           */
+    MEPGL_ERR_UNSUPPORTED = 5,   /* option not available for this problem         */
+    MEPGL_ERR_STATE = 6          /* call not valid in the context's current state  */
+} mepgl_status;
+
+enum { MEPGL_FP32 = 0, MEPGL_FP64 = 1 };          /* working precision of the fields  */
+enum { MEPGL_HOST = 0, MEPGL_DEVICE = 1 };        /* where a caller buffer lives      */
+enum { MEPGL_LS_COMPAT = 0, MEPGL_LS_EXACT = 1 }; /* step: geometric scan | minimiser */
+enum { MEPGL_POLY_COMPAT = 0, MEPGL_POLY_EXACT = 1 };       /* line polynomial        */
+enum { MEPGL_SPLINE_COMPAT = 0, MEPGL_SPLINE_FMM = 1 };     /* cubic evaluation       */
+enum { MEPGL_METRIC_FIELDS = 0, MEPGL_METRIC_JB = 1 };      /* arc-length metric      */
+enum { MEPGL_REDIST_LINEAR = 0, MEPGL_REDIST_CUBIC = 1 };
+
+/* The physical problem.  Replaces the generated headers config.cuh/real.cuh
+ * (N, dx, MULTICOMPONENT, NO_SELF_FIELD, DOUBLE_PRECISION) and the lattice
+ * inputs read by loadInput (mepgl/src/io.cu:10-126).  All pointers are host
+ * pointers, read during mepgl_create only.  The *_2 arrays may be NULL when
+ * multicomponent == 0.  Domains are int32, nonzero = inside. */
+typedef struct mepgl_problem {
+    int32_t nx, ny;            /* lattice (the reference has nx == ny == N)    */
+    int32_t n_images;          /* F                                            */
+    int32_t multicomponent;    /* 0: psi_1 only, 1: psi_1 and psi_2            */
+    int32_t thin_film;         /* 1: no magnetic self-field, A is frozen       */
+    int32_t precision;         /* MEPGL_FP32 or MEPGL_FP64                     */
+    double dx;
+    double q_1, q_2, eta, gamma, delta;
+    const double *a_1, *b_1, *m_xx_1, *m_yy_1;
+    const double *a_2, *b_2, *m_xx_2, *m_yy_2;
+    const double *h;
+    const int32_t *comp_domain, *sc_domain;
+} mepgl_problem;
+
+/* Method options.  The defaults (mepgl_default_options) reproduce the
+ * reference: compat line search and polynomial, compat spline, (B, J)
+ * metric (mepgl/src/mepgl.cu:32). */
+typedef struct mepgl_options {
+    int32_t line_search;       /* MEPGL_LS_*                                    */
+    int32_t line_polynomial;   /* MEPGL_POLY_*                                  */
+    int32_t spline;            /* MEPGL_SPLINE_*                                */
+    int32_t metric;            /* MEPGL_METRIC_*                                */
+    int32_t use_graphs;        /* capture NLCG steps as CUDA graphs (default 1) */
+    int32_t tile_rows;         /* rows per stencil tile: 0 = auto, 4, 8 or 16   */
+} mepgl_options;
+
+typedef struct mepgl_ctx mepgl_ctx;
+
+/* Defaults described above. */
+void mepgl_default_options(mepgl_options *opt);
+
+/* Version string of the library. */
+const char *mepgl_version(void);
+
+/* Create a context: uploads parameters and masks, allocates all device
+ * buffers (fields, gradients, directions, scratch) once.  `stream` is a
+ * cudaStream_t (NULL = default stream).  Replaces the allocation and setup
+ * part of main() (mepgl/src/mepgl.cu:453-616). */
+mepgl_status mepgl_create(const mepgl_problem *prob, const mepgl_options *opt, void *stream, mepgl_ctx **out);
+
+/* Free every device buffer of the context. */
+mepgl_status mepgl_destroy(mepgl_ctx *ctx);
+
+/* Message of the last failed call on this context (or of the last failed
+ * mepgl_create on this thread when ctx is NULL). */
+const char *mepgl_last_error(const mepgl_ctx *ctx);
+
+/* Copy the string in / out.  a, psi_1, psi_2: F*nx*ny pairs of the context's
+ * precision, in host or device memory.  psi_2 is ignored for one component.
+ * mepgl_set_state resets the NLCG history (the reference starts every run
+ * from zero gradients and infinite norms, mepgl/src/mepgl.cu:127-146). */
+mepgl_status mepgl_set_state(mepgl_ctx *ctx, const void *a, const void *psi_1, const void *psi_2, int memory);
+mepgl_status mepgl_get_state(mepgl_ctx *ctx, void *a, void *psi_1, void *psi_2, int memory);
+
+/* Per-image free energy of the current state (host array of F doubles).
+ * Replaces computeFreeEnergy (mepgl/src/nlcg.cu:217-240). */
+mepgl_status mepgl_free_energy(mepgl_ctx *ctx, double *fenergy);
+
+/* Free energy and gradient dF/d(A, psi) of the current state.  Gradients
+ * have the layout of the fields; NULL outputs are skipped.  Replaces the
+ * gradientPsi / gradientA launches (mepgl/src/nlcg.cu:1521-1537). */
+mepgl_status mepgl_energy_grad(mepgl_ctx *ctx, double *fenergy, void *g_a, void *g_psi_1, void *g_psi_2,
+                               int memory);
+
+/* `iterations` nonlinear-conjugate-gradient steps on every image.
+ * use_cg = 0 gives steepest descent; maxwell_only = 1 freezes psi (mode M).
+ * Replaces nlcgSteps (mepgl/src/nlcg.cu:1462-1586), with its gradient
+ * buffer convention: each call starts from the same "previous" slot. */
+mepgl_status mepgl_nlcg_steps(mepgl_ctx *ctx, int iterations, int use_cg, int maxwell_only);
+
+/* Restart conjugate gradients (norm history = infinity) for images
+ * [first, last).  The reference does this for the interior images after
+ * every reparametrization (mepgl/src/mepgl.cu:231-234). */
+mepgl_status mepgl_reset_cg(mepgl_ctx *ctx, int first_image, int last_image);
+
+/* Per-image scalars after the last NLCG step (host arrays of F doubles;
+ * NULL skips): energy before the step's update, |g|^2 of the slot the
+ * reference's loop() reads, and the step length alpha. */
+mepgl_status mepgl_image_scalars(mepgl_ctx *ctx, double *fenergy, double *g_norm2, double *alpha);
+
+/* B (F*nx*ny reals) and J_1, J_2 (pairs) of the current state; NULL skips.
+ * Replaces computeJB (mepgl/src/nlcg.cu:366-380). */
+mepgl_status mepgl_compute_jb(mepgl_ctx *ctx, void *b, void *j_1, void *j_2, int memory);
+
+/* Normalised arc length (host array of F doubles) in the field metric or
+ * the (B, J) metric.  Replaces arcLength / arcLengthJB
+ * (mepgl/src/interpolation.cu:143-169). */
+mepgl_status mepgl_arc_length(mepgl_ctx *ctx, int metric, double *s);
+
+/* Reparametrize the string to F_new equidistant images in the context's
+ * metric, linear or cubic.  F_new == F keeps the buffers; otherwise the
+ * context is resized (the reference's final F_out resample,
+ * mepgl/src/mepgl.cu:699-766).  Does NOT restart CG (see mepgl_reset_cg).
+ * Replaces redistributeLinear / redistributeCubic
+ * (mepgl/src/interpolation.cu:229-481). */
+mepgl_status mepgl_redistribute(mepgl_ctx *ctx, int kind, int F_new);
+
+/* One outer iteration of the reference's loop() in mode 'S', 'M', 'L' or
+ * 'C' (mepgl/src/mepgl.cu:148-303): optional reparametrization + CG restart
+ * of the interior images, then relaxation_steps NLCG steps. */
+mepgl_status mepgl_iteration(mepgl_ctx *ctx, char mode, int relaxation_steps, int use_cg);
+
+/* Change the working precision in place (FP32 <-> FP64): the fields are
+ * converted, the NLCG history is reset.  Used for FP32 bulk relaxation
+ * followed by FP64 polish. */
+mepgl_status mepgl_set_precision(mepgl_ctx *ctx, int precision);
+
+/* Number of images, working precision, and the number of kernel launches
+ * issued by this context so far (graph replays count their kernels). */
+mepgl_status mepgl_info(const mepgl_ctx *ctx, int *n_images, int *precision, int64_t *kernel_launches);
+
+/* Run `steps` NLCG steps launched one pass at a time with CUDA events
+ * between the passes on the context's stream, and return the mean duration
+ * (milliseconds) of the gradient pass and of the direction/line pass.  The
+ * steps are real steps: the state advances.  No reference counterpart (the
+ * reference has no timing facility); used by the benchmark's roofline. */
+mepgl_status mepgl_profile_passes(mepgl_ctx *ctx, int steps, int use_cg, double *ms_grad, double *ms_dir_poly);
+
+/* Wait for the context's stream. */
+mepgl_status mepgl_synchronize(mepgl_ctx *ctx);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,917 @@
+// api.cu -- the C ABI of libmepgl_gb300 (include/mepgl.h): context,
+// buffers, NLCG orchestration with CUDA-graph replay, reparametrization.
+//
+// A context owns one or more strings (all of one precision and component
+// count) and every device buffer they need, allocated at creation: fields
+// x (ping-pong), gradients g (two slots), directions d (ping-pong),
+// packed neighbour masks, per-site parameters when not uniform, per-image
+// scalars and per-tile partials.  The reference instead allocated and freed
+// scratch inside every call (mepgl/src/nlcg.cu:225-239,
+// mepgl/src/parallel_sum.cu:49-67, mepgl/src/interpolation.cu:410-480).
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <string>
+#include <tuple>
+#include <vector>
+
+#include "../../include/mepgl.h"
+#include "kernels.cuh"
+
+using namespace mepgl;
+
+namespace {
+
+thread_local std::string g_create_error;
+
+struct StringHost {
+    int nx, ny, F;
+    long M() const { return (long)nx * ny; }
+    std::vector<double> params[9];     // a1 b1 mxx1 myy1 a2 b2 mxx2 myy2 h (host copy)
+    std::vector<int32_t> comp, sc;
+    bool uniform;
+    void *dparams[9] = {};             // per-site arrays (type T) when not uniform
+    uint16_t *dmask = nullptr;
+    void *x[2][3] = {}, *g[2][3] = {}, *d[2][3] = {};
+    double q[2], eta, gamma, delta, dx;
+};
+
+}  // namespace
+
+struct mepgl_ctx {
+    int ncomp = 1, thin_film = 0, precision = 1;
+    mepgl_options opt{};
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    std::vector<StringHost> strings;
+    std::vector<StringDesc> hdesc;
+    StringDesc *ddesc = nullptr;
+    TileRef *dtiles = nullptr;
+    int n_tiles = 0, total_images = 0;
+    std::vector<int> string_tile0, string_ntiles;
+    Scalars sc{};
+    double *dscratch = nullptr;   // per-image temporaries (energies)
+    double *ds = nullptr, *ds_jb = nullptr;   // arc lengths of string 0
+    RedistPlan plan{};
+    int plan_cap = 0;
+    void *cubic_scratch = nullptr;   // 2 * F * sites doubles, allocated on first cubic use
+    size_t cubic_cap = 0;
+    int xi = 0, di = 0;           // current x / d buffers
+    bool pending = false;         // an NLCG update not yet applied to x
+    int64_t launches = 0;
+    std::string err;
+    std::map<std::tuple<int, int, int, int>, cudaGraphExec_t> graphs;
+    std::vector<double> host_s, host_sjb;
+    int sm_count = 152;
+};
+
+namespace {
+
+const double INF = INFINITY;
+
+mepgl_status fail(mepgl_ctx *c, mepgl_status st, const std::string &msg)
+{
+    if (c) c->err = msg;
+    else g_create_error = msg;
+    return st;
+}
+
+#define CK(ctx, call)                                                                               \
+    do {                                                                                            \
+        cudaError_t e_ = (call);                                                                    \
+        if (e_ != cudaSuccess)                                                                      \
+            return fail(ctx, MEPGL_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_));  \
+    } while (0)
+
+size_t real_size(int prec) { return prec == 1 ? 8 : 4; }
+
+template <class T>
+void *upload_as(mepgl_ctx *c, const std::vector<double> &v, cudaError_t *e)
+{
+    std::vector<T> tmp(v.begin(), v.end());
+    void *p = nullptr;
+    *e = cudaMalloc(&p, tmp.size() * sizeof(T));
+    if (*e == cudaSuccess) *e = cudaMemcpy(p, tmp.data(), tmp.size() * sizeof(T), cudaMemcpyHostToDevice);
+    (void)c;
+    return p;
+}
+
+std::vector<uint16_t> masks_of(const StringHost &s)
+{
+    static const int di[8] = {1, 1, 0, -1, -1, -1, 0, 1};
+    static const int dj[8] = {0, 1, 1, 1, 0, -1, -1, -1};
+    std::vector<uint16_t> m(s.M());
+    for (int j = 0; j < s.ny; ++j)
+        for (int i = 0; i < s.nx; ++i) {
+            unsigned code[2] = {0, 0};
+            const std::vector<int32_t> *dom[2] = {&s.comp, &s.sc};
+            for (int w = 0; w < 2; ++w) {
+                if ((*dom[w])[i + (long)s.nx * j] == 0) continue;
+                for (int b = 0; b < 8; ++b) {
+                    const int ii = i + di[b], jj = j + dj[b];
+                    if (ii < 0 || ii >= s.nx || jj < 0 || jj >= s.ny) continue;
+                    if ((*dom[w])[ii + (long)s.nx * jj] != 0) code[w] |= 1u << b;
+                }
+            }
+            m[i + (long)s.nx * j] = (uint16_t)(code[0] | (code[1] << 8));
+        }
+    return m;
+}
+
+void free_string_buffers(StringHost &s)
+{
+    for (int b = 0; b < 2; ++b)
+        for (int f = 0; f < 3; ++f) {
+            cudaFree(s.x[b][f]);
+            cudaFree(s.g[b][f]);
+            cudaFree(s.d[b][f]);
+            s.x[b][f] = s.g[b][f] = s.d[b][f] = nullptr;
+        }
+}
+
+void free_string_params(StringHost &s)
+{
+    for (auto &p : s.dparams) { cudaFree(p); p = nullptr; }
+    cudaFree(s.dmask);
+    s.dmask = nullptr;
+}
+
+mepgl_status alloc_string_buffers(mepgl_ctx *c, StringHost &s)
+{
+    const size_t bytes = (size_t)s.F * s.M() * 2 * real_size(c->precision);
+    for (int b = 0; b < 2; ++b)
+        for (int f = 0; f < 1 + c->ncomp; ++f) {
+            CK(c, cudaMalloc(&s.x[b][f], bytes));
+            CK(c, cudaMalloc(&s.g[b][f], bytes));
+            CK(c, cudaMalloc(&s.d[b][f], bytes));
+            CK(c, cudaMemsetAsync(s.x[b][f], 0, bytes, c->stream));
+            CK(c, cudaMemsetAsync(s.g[b][f], 0, bytes, c->stream));
+            CK(c, cudaMemsetAsync(s.d[b][f], 0, bytes, c->stream));
+        }
+    return MEPGL_OK;
+}
+
+mepgl_status upload_string_params(mepgl_ctx *c, StringHost &s)
+{
+    free_string_params(s);
+    const std::vector<uint16_t> m = masks_of(s);
+    CK(c, cudaMalloc(&s.dmask, m.size() * sizeof(uint16_t)));
+    CK(c, cudaMemcpy(s.dmask, m.data(), m.size() * sizeof(uint16_t), cudaMemcpyHostToDevice));
+    if (!s.uniform) {
+        for (int k = 0; k < 9; ++k) {
+            if (k >= 4 && k < 8 && c->ncomp == 1) continue;
+            cudaError_t e;
+            s.dparams[k] = c->precision == 1 ? upload_as<double>(c, s.params[k], &e) : upload_as<float>(c, s.params[k], &e);
+            CK(c, e);
+        }
+    }
+    return MEPGL_OK;
+}
+
+void fill_desc(mepgl_ctx *c, int si, int img_base, int tile_base)
+{
+    StringHost &s = c->strings[si];
+    StringDesc &D = c->hdesc[si];
+    memset(&D, 0, sizeof(D));
+    D.nx = s.nx;
+    D.ny = s.ny;
+    D.F = s.F;
+    D.ncomp = c->ncomp;
+    D.tiles_x = (s.nx + TX - 1) / TX;
+    D.tiles_y = (s.ny + TY - 1) / TY;
+    D.img_base = img_base;
+    D.tile_base = tile_base;
+    D.thin_film = c->thin_film;
+    D.per_site = s.uniform ? 0 : 1;
+    D.dx = s.dx;
+    D.inv_dx = 1.0 / s.dx;
+    D.q[0] = s.q[0];
+    D.q[1] = s.q[1];
+    D.eta = s.eta;
+    D.gamma = s.gamma;
+    D.delta = s.delta;
+    for (int k = 0; k < 2; ++k) {
+        const int o = 4 * k;
+        D.a[k] = s.params[o][0];
+        D.b[k] = s.params[o + 1][0];
+        D.mxx[k] = s.params[o + 2][0];
+        D.myy[k] = s.params[o + 3][0];
+        D.hmx[k] = 0.5 / D.mxx[k];
+        D.hmy[k] = 0.5 / D.myy[k];
+        D.aob[k] = D.a[k] / D.b[k];
+        D.pa[k] = s.dparams[o];
+        D.pb[k] = s.dparams[o + 1];
+        D.pmxx[k] = s.dparams[o + 2];
+        D.pmyy[k] = s.dparams[o + 3];
+    }
+    D.h = s.params[8][0];
+    D.ph = s.dparams[8];
+    D.mask = s.dmask;
+    for (int b = 0; b < 2; ++b)
+        for (int f = 0; f < 3; ++f) {
+            D.x[b][f] = s.x[b][f];
+            D.g[b][f] = s.g[b][f];
+            D.d[b][f] = s.d[b][f];
+        }
+}
+
+void free_scalars(mepgl_ctx *c)
+{
+    Scalars &S = c->sc;
+    cudaFree(S.gn[0]); cudaFree(S.gn[1]); cudaFree(S.gdg); cudaFree(S.beta); cudaFree(S.alpha);
+    cudaFree(S.alpha_pend); cudaFree(S.fenergy); cudaFree(S.poly); cudaFree(S.part); cudaFree(S.ticket);
+    cudaFree(S.xtab_f); cudaFree(S.xtab_d); cudaFree(S.status);
+    memset(&S, 0, sizeof(S));
+    cudaFree(c->dscratch); c->dscratch = nullptr;
+    cudaFree(c->ds); cudaFree(c->ds_jb); c->ds = c->ds_jb = nullptr;
+    cudaFree(c->ddesc); c->ddesc = nullptr;
+    cudaFree(c->dtiles); c->dtiles = nullptr;
+}
+
+void drop_graphs(mepgl_ctx *c)
+{
+    for (auto &kv : c->graphs) cudaGraphExecDestroy(kv.second);
+    c->graphs.clear();
+}
+
+// (Re)build tile table, descriptors and per-image arrays for the current strings.
+mepgl_status build_layout(mepgl_ctx *c)
+{
+    drop_graphs(c);
+    free_scalars(c);
+    c->hdesc.assign(c->strings.size(), StringDesc{});
+    std::vector<TileRef> tiles;
+    int img = 0;
+    c->string_tile0.clear();
+    c->string_ntiles.clear();
+    for (size_t si = 0; si < c->strings.size(); ++si) {
+        fill_desc(c, (int)si, img, (int)tiles.size());
+        const StringDesc &D = c->hdesc[si];
+        c->string_tile0.push_back((int)tiles.size());
+        for (int n = 0; n < D.F; ++n)
+            for (int ty = 0; ty < D.tiles_y; ++ty)
+                for (int tx = 0; tx < D.tiles_x; ++tx)
+                    tiles.push_back(TileRef{(int16_t)si, (int16_t)ty, (int16_t)tx, 0, n});
+        c->string_ntiles.push_back((int)tiles.size() - c->string_tile0.back());
+        img += D.F;
+    }
+    c->n_tiles = (int)tiles.size();
+    c->total_images = img;
+    CK(c, cudaMalloc(&c->ddesc, sizeof(StringDesc) * c->hdesc.size()));
+    CK(c, cudaMemcpy(c->ddesc, c->hdesc.data(), sizeof(StringDesc) * c->hdesc.size(), cudaMemcpyHostToDevice));
+    CK(c, cudaMalloc(&c->dtiles, sizeof(TileRef) * tiles.size()));
+    CK(c, cudaMemcpy(c->dtiles, tiles.data(), sizeof(TileRef) * tiles.size(), cudaMemcpyHostToDevice));
+    Scalars &S = c->sc;
+    const size_t I = (size_t)img;
+    for (double **p : {&S.gn[0], &S.gn[1], &S.gdg, &S.beta, &S.alpha, &S.alpha_pend, &S.fenergy})
+        CK(c, cudaMalloc(p, I * sizeof(double)));
+    CK(c, cudaMalloc(&S.poly, 4 * I * sizeof(double)));
+    CK(c, cudaMalloc(&S.part, (size_t)c->n_tiles * 8 * sizeof(double) + 4096 * sizeof(double)));
+    CK(c, cudaMalloc(&S.ticket, I * sizeof(unsigned)));
+    CK(c, cudaMemset(S.ticket, 0, I * sizeof(unsigned)));
+    CK(c, cudaMalloc(&S.status, 16 * sizeof(int)));
+    CK(c, cudaMemset(S.status, 0, 16 * sizeof(int)));
+    // line-search grid x_p = x_0 * m^p rounded to float / double at every step
+    std::vector<double> xf(LS_GRID), xd(LS_GRID);
+    float fx = 1e-10f;
+    const float fm = 1.025f;
+    double dxx = 1e-10;
+    const double dm = (double)1.025f;
+    for (int p = 0; p < LS_GRID; ++p) {
+        xf[p] = fx;
+        xd[p] = dxx;
+        fx = fx * fm;
+        dxx = dxx * dm;
+    }
+    CK(c, cudaMalloc(&S.xtab_f, LS_GRID * sizeof(double)));
+    CK(c, cudaMalloc(&S.xtab_d, LS_GRID * sizeof(double)));
+    CK(c, cudaMemcpy(S.xtab_f, xf.data(), LS_GRID * sizeof(double), cudaMemcpyHostToDevice));
+    CK(c, cudaMemcpy(S.xtab_d, xd.data(), LS_GRID * sizeof(double), cudaMemcpyHostToDevice));
+    CK(c, cudaMalloc(&c->dscratch, (I + 64) * sizeof(double)));
+    int fmax = 0;
+    for (auto &s : c->strings) fmax = fmax > s.F ? fmax : s.F;
+    CK(c, cudaMalloc(&c->ds, (fmax + 1) * sizeof(double)));
+    CK(c, cudaMalloc(&c->ds_jb, (fmax + 1) * sizeof(double)));
+    CK(c, cudaMemset(c->ds, 0, (fmax + 1) * sizeof(double)));
+    CK(c, cudaMemset(c->ds_jb, 0, (fmax + 1) * sizeof(double)));
+    c->host_s.assign(fmax, 0.0);
+    c->host_sjb.assign(fmax, 0.0);
+    return MEPGL_OK;
+}
+
+// Restart NLCG history: zero g and d, |g|^2 = inf, nothing pending.
+mepgl_status reset_history(mepgl_ctx *c)
+{
+    for (auto &s : c->strings) {
+        const size_t bytes = (size_t)s.F * s.M() * 2 * real_size(c->precision);
+        for (int b = 0; b < 2; ++b)
+            for (int f = 0; f < 1 + c->ncomp; ++f) {
+                CK(c, cudaMemsetAsync(s.g[b][f], 0, bytes, c->stream));
+                CK(c, cudaMemsetAsync(s.d[b][f], 0, bytes, c->stream));
+            }
+    }
+    std::vector<double> inf(c->total_images, INF);
+    CK(c, cudaMemcpyAsync(c->sc.gn[0], inf.data(), inf.size() * 8, cudaMemcpyHostToDevice, c->stream));
+    CK(c, cudaMemcpyAsync(c->sc.gn[1], inf.data(), inf.size() * 8, cudaMemcpyHostToDevice, c->stream));
+    for (double *p : {c->sc.alpha, c->sc.alpha_pend, c->sc.fenergy, c->sc.beta, c->sc.gdg})
+        CK(c, cudaMemsetAsync(p, 0, c->total_images * 8, c->stream));
+    CK(c, cudaMemsetAsync(c->sc.poly, 0, c->total_images * 32, c->stream));
+    CK(c, cudaStreamSynchronize(c->stream));
+    c->pending = false;
+    return MEPGL_OK;
+}
+
+Launch make_launch(mepgl_ctx *c, int first_tile = 0, int ntiles = -1)
+{
+    Launch L;
+    L.strings = c->ddesc;
+    L.tiles = c->dtiles + first_tile;
+    L.n_tiles = ntiles < 0 ? c->n_tiles : ntiles;
+    L.grid = L.n_tiles;
+    L.precision = c->precision;
+    L.ncomp = c->ncomp;
+    L.stream = c->stream;
+    return L;
+}
+
+mepgl_status flush(mepgl_ctx *c)
+{
+    if (!c->pending) return MEPGL_OK;
+    CK(c, launch_apply_update(make_launch(c), c->sc, c->hdesc.data(), (int)c->hdesc.size(), c->xi, c->di));
+    c->launches += (int64_t)c->strings.size() * (1 + c->ncomp);
+    c->pending = false;
+    return MEPGL_OK;
+}
+
+StepFlags step_flags(mepgl_ctx *c, int it, int use_cg, int maxwell)
+{
+    StepFlags f;
+    f.gcur = it & 1;
+    f.gprev = f.gcur ^ 1;
+    f.xin = c->xi;
+    f.xout = c->xi ^ 1;
+    f.din = c->di;
+    f.dout = c->di ^ 1;
+    f.use_cg = use_cg;
+    f.maxwell = maxwell;
+    f.thin_film_any = c->thin_film;
+    f.poly_compat = c->opt.line_polynomial == MEPGL_POLY_COMPAT;
+    f.ls_exact = c->opt.line_search == MEPGL_LS_EXACT;
+    return f;
+}
+
+mepgl_status one_step(mepgl_ctx *c, int it, int use_cg, int maxwell)
+{
+    const StepFlags f = step_flags(c, it, use_cg, maxwell);
+    const Launch L = make_launch(c);
+    CK(c, launch_grad(L, c->sc, f));
+    CK(c, launch_dir_poly(L, c->sc, f));
+    c->xi ^= 1;
+    c->di ^= 1;
+    c->launches += 2;
+    c->pending = true;
+    return MEPGL_OK;
+}
+
+mepgl_status two_step_graph(mepgl_ctx *c, int use_cg, int maxwell, cudaGraphExec_t *out)
+{
+    auto key = std::make_tuple(c->xi, c->di, use_cg, maxwell);
+    auto it = c->graphs.find(key);
+    if (it != c->graphs.end()) {
+        *out = it->second;
+        return MEPGL_OK;
+    }
+    const int xi0 = c->xi, di0 = c->di;
+    const int64_t l0 = c->launches;
+    CK(c, cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+    mepgl_status st = one_step(c, 1, use_cg, maxwell);
+    if (st == MEPGL_OK) st = one_step(c, 2, use_cg, maxwell);
+    cudaGraph_t g = nullptr;
+    cudaError_t e = cudaStreamEndCapture(c->stream, &g);
+    c->xi = xi0;
+    c->di = di0;
+    c->launches = l0;
+    if (st != MEPGL_OK) return st;
+    CK(c, e);
+    cudaGraphExec_t ex = nullptr;
+    CK(c, cudaGraphInstantiate(&ex, g, 0));
+    cudaGraphDestroy(g);
+    c->graphs[key] = ex;
+    *out = ex;
+    return MEPGL_OK;
+}
+
+mepgl_status nlcg_steps(mepgl_ctx *c, int iters, int use_cg, int maxwell)
+{
+    int it = 1;
+    if (c->opt.use_graphs && iters >= 2) {
+        cudaGraphExec_t ex;
+        mepgl_status st = two_step_graph(c, use_cg, maxwell, &ex);
+        if (st != MEPGL_OK) return st;
+        for (; it + 1 <= iters; it += 2) {
+            CK(c, cudaGraphLaunch(ex, c->stream));
+            c->launches += 4;
+        }
+        c->pending = true;
+    }
+    for (; it <= iters; ++it) {
+        mepgl_status st = one_step(c, it, use_cg, maxwell);
+        if (st != MEPGL_OK) return st;
+    }
+    return MEPGL_OK;
+}
+
+mepgl_status copy_fields(mepgl_ctx *c, StringHost &s, void *const *dst, const void *const *src, int memory, bool in)
+{
+    const size_t bytes = (size_t)s.F * s.M() * 2 * real_size(c->precision);
+    const cudaMemcpyKind k = memory == MEPGL_DEVICE ? cudaMemcpyDeviceToDevice
+                             : in                    ? cudaMemcpyHostToDevice
+                                                     : cudaMemcpyDeviceToHost;
+    for (int f = 0; f < 1 + c->ncomp; ++f) {
+        if (!(in ? src[f] : dst[f])) continue;
+        CK(c, cudaMemcpyAsync(dst[f], src[f], bytes, k, c->stream));
+    }
+    CK(c, cudaStreamSynchronize(c->stream));
+    return MEPGL_OK;
+}
+
+// Arc length of string 0 into c->ds (fields) or c->ds_jb (B, J).
+mepgl_status arc_length(mepgl_ctx *c, int metric, double **where)
+{
+    StringHost &s = c->strings[0];
+    mepgl_status st = flush(c);
+    if (st != MEPGL_OK) return st;
+    const void *fl[3];
+    int w[3];
+    int nf = 1 + c->ncomp;
+    if (metric == MEPGL_METRIC_FIELDS) {
+        for (int f = 0; f < nf; ++f) { fl[f] = s.x[c->xi][f]; w[f] = 2; }
+        *where = c->ds;
+    } else {
+        // B, J into the spare direction buffer (its contents are not needed)
+        void *b[1] = {s.d[c->di ^ 1][0]};
+        void *j[1][2] = {{s.d[c->di ^ 1][1], c->ncomp == 2 ? s.d[c->di ^ 1][2] : s.d[c->di ^ 1][1]}};
+        CK(c, launch_jb(make_launch(c, c->string_tile0[0], c->string_ntiles[0]), c->sc, c->xi, b, j));
+        c->launches += 1;
+        fl[0] = b[0]; w[0] = 1;
+        fl[1] = j[0][0]; w[1] = 2;
+        fl[2] = j[0][1]; w[2] = 2;
+        *where = c->ds_jb;
+    }
+    CK(c, launch_arc_length(c->precision, fl, w, nf, s.M(), s.F, c->sc.part, *where, c->stream));
+    c->launches += 2;
+    return MEPGL_OK;
+}
+
+mepgl_status ensure_plan(mepgl_ctx *c, int F, int F_new)
+{
+    const int need = (F > F_new ? F : F_new) + 2;
+    if (need <= c->plan_cap) return MEPGL_OK;
+    RedistPlan &p = c->plan;
+    cudaFree(p.k); cudaFree(p.w); cudaFree(p.h); cudaFree(p.dl); cudaFree(p.d); cudaFree(p.du); cudaFree(p.du2);
+    cudaFree(p.ipiv); cudaFree(p.status);
+    CK(c, cudaMalloc(&p.k, need * sizeof(int)));
+    CK(c, cudaMalloc(&p.ipiv, need * sizeof(int)));
+    CK(c, cudaMalloc(&p.status, 4 * sizeof(int)));
+    CK(c, cudaMemset(p.status, 0, 4 * sizeof(int)));
+    for (double **q : {&p.w, &p.h, &p.dl, &p.d, &p.du, &p.du2}) CK(c, cudaMalloc(q, need * sizeof(double)));
+    c->plan_cap = need;
+    return MEPGL_OK;
+}
+
+mepgl_status redistribute(mepgl_ctx *c, int kind, int F_new)
+{
+    if (c->strings.size() != 1) return fail(c, MEPGL_ERR_UNSUPPORTED, "redistribute: single-string contexts only");
+    StringHost &s = c->strings[0];
+    const int F = s.F;
+    if (F < 2 || F_new < 2) return fail(c, MEPGL_ERR_INVALID_ARG, "redistribute: need at least 2 images");
+    if (kind == MEPGL_REDIST_CUBIC && F < 4)
+        return fail(c, MEPGL_ERR_INVALID_ARG, "cubic reparametrization needs at least 4 images");
+    double *sp = nullptr;
+    mepgl_status st = arc_length(c, MEPGL_METRIC_FIELDS, &sp);
+    if (st != MEPGL_OK) return st;
+    st = arc_length(c, MEPGL_METRIC_JB, &sp);
+    if (st != MEPGL_OK) return st;
+    double *s_use = c->opt.metric == MEPGL_METRIC_FIELDS ? c->ds : c->ds_jb;
+    st = ensure_plan(c, F, F_new);
+    if (st != MEPGL_OK) return st;
+    const int cubic = kind == MEPGL_REDIST_CUBIC;
+    CK(c, launch_redist_plan(s_use, F, F_new, cubic, c->opt.spline, c->plan, c->stream));
+    c->launches += 1;
+    void *target[3] = {};
+    std::vector<void *> fresh;
+    const size_t rs = real_size(c->precision);
+    if (F_new == F) {
+        for (int f = 0; f < 1 + c->ncomp; ++f) target[f] = s.x[c->xi ^ 1][f];
+    } else {
+        for (int f = 0; f < 1 + c->ncomp; ++f) {
+            CK(c, cudaMalloc(&target[f], (size_t)F_new * s.M() * 2 * rs));
+            fresh.push_back(target[f]);
+        }
+    }
+    if (cubic) {
+        const size_t need = (size_t)2 * F * s.M() * sizeof(double);
+        if (need > c->cubic_cap) {
+            cudaFree(c->cubic_scratch);
+            c->cubic_scratch = nullptr;
+            c->cubic_cap = 0;
+            CK(c, cudaMalloc(&c->cubic_scratch, need));
+            c->cubic_cap = need;
+        }
+    }
+    for (int f = 0; f < 1 + c->ncomp; ++f) {
+        if (cubic)
+            CK(c, launch_redist_cubic(c->precision, s.x[c->xi][f], target[f], c->cubic_scratch, s.M(), F, F_new,
+                                      c->opt.spline, c->plan, c->stream));
+        else
+            CK(c, launch_redist_linear(c->precision, s.x[c->xi][f], target[f], s.M(), F_new, c->plan, c->stream));
+        c->launches += 1;
+    }
+    if (F_new == F) {
+        c->xi ^= 1;
+        return MEPGL_OK;
+    }
+    // resize: new buffers for F_new images, state moved in, history reset
+    CK(c, cudaStreamSynchronize(c->stream));
+    free_string_buffers(s);
+    s.F = F_new;
+    st = alloc_string_buffers(c, s);
+    if (st != MEPGL_OK) return st;
+    for (int f = 0; f < 1 + c->ncomp; ++f) {
+        CK(c, cudaMemcpyAsync(s.x[0][f], target[f], (size_t)F_new * s.M() * 2 * rs, cudaMemcpyDeviceToDevice, c->stream));
+        cudaFree(target[f]);
+    }
+    c->xi = 0;
+    c->di = 0;
+    st = build_layout(c);
+    if (st != MEPGL_OK) return st;
+    return reset_history(c);
+}
+
+mepgl_status reset_cg(mepgl_ctx *c, int first, int last)
+{
+    if (first < 0 || last > c->total_images || first > last)
+        return fail(c, MEPGL_ERR_INVALID_ARG, "reset_cg: image range out of bounds");
+    if (first == last) return MEPGL_OK;
+    std::vector<double> inf(last - first, INF);
+    CK(c, cudaMemcpyAsync(c->sc.gn[0] + first, inf.data(), inf.size() * 8, cudaMemcpyHostToDevice, c->stream));
+    CK(c, cudaMemcpyAsync(c->sc.gn[1] + first, inf.data(), inf.size() * 8, cudaMemcpyHostToDevice, c->stream));
+    CK(c, cudaStreamSynchronize(c->stream));
+    return MEPGL_OK;
+}
+
+}  // namespace
+
+// ======================================================================= ABI
+extern "C" {
+
+void mepgl_default_options(mepgl_options *o)
+{
+    if (!o) return;
+    o->line_search = MEPGL_LS_COMPAT;
+    o->line_polynomial = MEPGL_POLY_COMPAT;
+    o->spline = MEPGL_SPLINE_COMPAT;
+    o->metric = MEPGL_METRIC_JB;
+    o->use_graphs = 1;
+    o->tile_rows = 0;
+}
+
+const char *mepgl_version(void) { return "mepgl_gb300 0.1 (sm_103a)"; }
+
+const char *mepgl_last_error(const mepgl_ctx *c) { return c ? c->err.c_str() : g_create_error.c_str(); }
+
+mepgl_status mepgl_create(const mepgl_problem *p, const mepgl_options *opt, void *stream, mepgl_ctx **out)
+{
+    if (!p || !out) return fail(nullptr, MEPGL_ERR_INVALID_ARG, "mepgl_create: null argument");
+    *out = nullptr;
+    if (p->nx < 2 || p->ny < 2 || p->n_images < 1 || !(p->dx > 0))
+        return fail(nullptr, MEPGL_ERR_INVALID_ARG, "mepgl_create: need nx, ny >= 2, n_images >= 1, dx > 0");
+    if (p->nx > 32767 * TX || p->ny > 32767 * TY)
+        return fail(nullptr, MEPGL_ERR_INVALID_ARG, "mepgl_create: lattice too large");
+    if (p->precision != MEPGL_FP32 && p->precision != MEPGL_FP64)
+        return fail(nullptr, MEPGL_ERR_INVALID_ARG, "mepgl_create: precision must be MEPGL_FP32 or MEPGL_FP64");
+    const double *arr[9] = {p->a_1, p->b_1, p->m_xx_1, p->m_yy_1, p->a_2, p->b_2, p->m_xx_2, p->m_yy_2, p->h};
+    for (int k = 0; k < 9; ++k)
+        if (!arr[k] && !(k >= 4 && k < 8 && !p->multicomponent))
+            return fail(nullptr, MEPGL_ERR_INVALID_ARG, "mepgl_create: missing parameter array");
+    if (!p->comp_domain || !p->sc_domain) return fail(nullptr, MEPGL_ERR_INVALID_ARG, "mepgl_create: missing domain");
+
+    mepgl_ctx *c = new mepgl_ctx();
+    if (opt) c->opt = *opt;
+    else mepgl_default_options(&c->opt);
+    c->ncomp = p->multicomponent ? 2 : 1;
+    c->thin_film = p->thin_film ? 1 : 0;
+    c->precision = p->precision;
+    c->stream = (cudaStream_t)stream;
+    if (!c->stream) {
+        // graph capture is not allowed on the legacy default stream
+        if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) {
+            delete c;
+            return fail(nullptr, MEPGL_ERR_CUDA, "mepgl_create: cannot create a stream");
+        }
+        c->own_stream = true;
+    }
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&c->sm_count, cudaDevAttrMultiProcessorCount, dev);
+    StringHost s;
+    s.nx = p->nx;
+    s.ny = p->ny;
+    s.F = p->n_images;
+    s.dx = p->dx;
+    s.q[0] = p->q_1;
+    s.q[1] = p->q_2;
+    s.eta = p->eta;
+    s.gamma = p->gamma;
+    s.delta = p->delta;
+    const long M = s.M();
+    s.uniform = true;
+    for (int k = 0; k < 9; ++k) {
+        if (arr[k]) s.params[k].assign(arr[k], arr[k] + M);
+        else s.params[k].assign(M, 1.0);
+        for (long i = 1; i < M && s.uniform; ++i)
+            if (s.params[k][i] != s.params[k][0]) s.uniform = false;
+    }
+    s.comp.assign(p->comp_domain, p->comp_domain + M);
+    s.sc.assign(p->sc_domain, p->sc_domain + M);
+    c->strings.push_back(std::move(s));
+    mepgl_status st = upload_string_params(c, c->strings[0]);
+    if (st == MEPGL_OK) st = alloc_string_buffers(c, c->strings[0]);
+    if (st == MEPGL_OK) st = build_layout(c);
+    if (st == MEPGL_OK) st = reset_history(c);
+    if (st != MEPGL_OK) {
+        g_create_error = c->err;
+        mepgl_destroy(c);
+        return st;
+    }
+    *out = c;
+    return MEPGL_OK;
+}
+
+mepgl_status mepgl_destroy(mepgl_ctx *c)
+{
+    if (!c) return MEPGL_OK;
+    cudaStreamSynchronize(c->stream);
+    drop_graphs(c);
+    for (auto &s : c->strings) {
+        free_string_buffers(s);
+        free_string_params(s);
+    }
+    free_scalars(c);
+    RedistPlan &p = c->plan;
+    cudaFree(p.k); cudaFree(p.w); cudaFree(p.h); cudaFree(p.dl); cudaFree(p.d); cudaFree(p.du); cudaFree(p.du2);
+    cudaFree(p.ipiv); cudaFree(p.status);
+    cudaFree(c->cubic_scratch);
+    if (c->own_stream) cudaStreamDestroy(c->stream);
+    delete c;
+    return MEPGL_OK;
+}
+
+mepgl_status mepgl_set_state(mepgl_ctx *c, const void *a, const void *psi_1, const void *psi_2, int memory)
+{
+    if (!c || !a || !psi_1 || (c->ncomp == 2 && !psi_2))
+        return fail(c, MEPGL_ERR_INVALID_ARG, "mepgl_set_state: null field");
+    StringHost &s = c->strings[0];
+    c->xi = 0;
+    c->di = 0;
+    void *dst[3] = {s.x[0][0], s.x[0][1], s.x[0][2]};
+    const void *src[3] = {a, psi_1, psi_2};
+    mepgl_status st = copy_fields(c, s, dst, src, memory, true);
+    if (st != MEPGL_OK) return st;
+    return reset_history(c);
+}
+
+mepgl_status mepgl_get_state(mepgl_ctx *c, void *a, void *psi_1, void *psi_2, int memory)
+{
+    if (!c) return MEPGL_ERR_INVALID_ARG;
+    mepgl_status st = flush(c);
+    if (st != MEPGL_OK) return st;
+    StringHost &s = c->strings[0];
+    void *dst[3] = {a, psi_1, psi_2};
+    const void *src[3] = {s.x[c->xi][0], s.x[c->xi][1], s.x[c->xi][2]};
+    return copy_fields(c, s, dst, src, memory, false);
+}
+
+mepgl_status mepgl_free_energy(mepgl_ctx *c, double *fenergy)
+{
+    if (!c || !fenergy) return fail(c, MEPGL_ERR_INVALID_ARG, "mepgl_free_energy: null argument");
+    mepgl_status st = flush(c);
+    if (st != MEPGL_OK) return st;
+    CK(c, launch_energy(make_launch(c), c->sc, c->xi, c->dscratch));
+    c->launches += 1;
+    CK(c, cudaMemcpyAsync(fenergy, c->dscratch, c->strings[0].F * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    CK(c, cudaStreamSynchronize(c->stream));
+    return MEPGL_OK;
+}
+
+mepgl_status mepgl_energy_grad(mepgl_ctx *c, double *fenergy, void *g_a, void *g_psi_1, void *g_psi_2, int memory)
+{
+    if (!c) return MEPGL_ERR_INVALID_ARG;
+    mepgl_status st = flush(c);
+    if (st != MEPGL_OK) return st;
+    StringHost &s = c->strings[0];
+    if (fenergy) {
+        st = mepgl_free_energy(c, fenergy);
+        if (st != MEPGL_OK) return st;
+    }
+    if (!g_a && !g_psi_1 && !g_psi_2) return MEPGL_OK;
+    const bool direct = memory == MEPGL_DEVICE && g_a && g_psi_1 && (c->ncomp == 1 || g_psi_2);
+    FieldPtrs out;
+    for (int f = 0; f < 3; ++f) out.p[f] = s.d[c->di ^ 1][f];   // spare direction buffer
+    if (direct) {
+        out.p[0] = g_a;
+        out.p[1] = g_psi_1;
+        out.p[2] = c->ncomp == 2 ? g_psi_2 : nullptr;
+    }
+    CK(c, launch_gradient_only(make_launch(c), c->xi, out, 0));
+    c->launches += 1;
+    if (direct) {
+        CK(c, cudaStreamSynchronize(c->stream));
+        return MEPGL_OK;
+    }
+    void *dst[3] = {g_a, g_psi_1, g_psi_2};
+    const void *src[3] = {out.p[0], out.p[1], out.p[2]};
+    return copy_fields(c, s, dst, src, memory, false);
+}
+
+mepgl_status mepgl_nlcg_steps(mepgl_ctx *c, int iterations, int use_cg, int maxwell_only)
+{
+    if (!c || iterations < 0) return fail(c, MEPGL_ERR_INVALID_ARG, "mepgl_nlcg_steps: bad argument");
+    return nlcg_steps(c, iterations, use_cg ? 1 : 0, maxwell_only ? 1 : 0);
+}
+
+mepgl_status mepgl_reset_cg(mepgl_ctx *c, int first_image, int last_image)
+{
+    if (!c) return MEPGL_ERR_INVALID_ARG;
+    return reset_cg(c, first_image, last_image);
+}
+
+mepgl_status mepgl_image_scalars(mepgl_ctx *c, double *fenergy, double *g_norm2, double *alpha)
+{
+    if (!c) return MEPGL_ERR_INVALID_ARG;
+    const int F = c->strings[0].F;
+    if (fenergy) CK(c, cudaMemcpyAsync(fenergy, c->sc.fenergy, F * 8, cudaMemcpyDeviceToHost, c->stream));
+    // loop()'s g_norm2 is the slot nlcgSteps writes on even substeps
+    if (g_norm2) CK(c, cudaMemcpyAsync(g_norm2, c->sc.gn[0], F * 8, cudaMemcpyDeviceToHost, c->stream));
+    if (alpha) CK(c, cudaMemcpyAsync(alpha, c->sc.alpha, F * 8, cudaMemcpyDeviceToHost, c->stream));
+    CK(c, cudaStreamSynchronize(c->stream));
+    return MEPGL_OK;
+}
+
+mepgl_status mepgl_compute_jb(mepgl_ctx *c, void *b, void *j_1, void *j_2, int memory)
+{
+    if (!c) return MEPGL_ERR_INVALID_ARG;
+    mepgl_status st = flush(c);
+    if (st != MEPGL_OK) return st;
+    StringHost &s = c->strings[0];
+    void *bb[1] = {s.d[c->di ^ 1][0]};
+    void *jj[1][2] = {{s.d[c->di ^ 1][1], c->ncomp == 2 ? s.d[c->di ^ 1][2] : s.d[c->di ^ 1][1]}};
+    CK(c, launch_jb(make_launch(c), c->sc, c->xi, bb, jj));
+    c->launches += 1;
+    const size_t rs = real_size(c->precision), n = (size_t)s.F * s.M();
+    const cudaMemcpyKind k = memory == MEPGL_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
+    if (b) CK(c, cudaMemcpyAsync(b, bb[0], n * rs, k, c->stream));
+    if (j_1) CK(c, cudaMemcpyAsync(j_1, jj[0][0], 2 * n * rs, k, c->stream));
+    if (j_2 && c->ncomp == 2) CK(c, cudaMemcpyAsync(j_2, jj[0][1], 2 * n * rs, k, c->stream));
+    CK(c, cudaStreamSynchronize(c->stream));
+    return MEPGL_OK;
+}
+
+mepgl_status mepgl_arc_length(mepgl_ctx *c, int metric, double *s)
+{
+    if (!c || !s) return fail(c, MEPGL_ERR_INVALID_ARG, "mepgl_arc_length: null argument");
+    double *where = nullptr;
+    mepgl_status st = arc_length(c, metric, &where);
+    if (st != MEPGL_OK) return st;
+    CK(c, cudaMemcpyAsync(s, where, c->strings[0].F * 8, cudaMemcpyDeviceToHost, c->stream));
+    CK(c, cudaStreamSynchronize(c->stream));
+    return MEPGL_OK;
+}
+
+mepgl_status mepgl_redistribute(mepgl_ctx *c, int kind, int F_new)
+{
+    if (!c) return MEPGL_ERR_INVALID_ARG;
+    if (kind != MEPGL_REDIST_LINEAR && kind != MEPGL_REDIST_CUBIC)
+        return fail(c, MEPGL_ERR_INVALID_ARG, "mepgl_redistribute: unknown kind");
+    mepgl_status st = redistribute(c, kind, F_new);
+    if (st != MEPGL_OK) return st;
+    CK(c, cudaStreamSynchronize(c->stream));
+    int bad = 0;
+    CK(c, cudaMemcpy(&bad, c->plan.status, sizeof(int), cudaMemcpyDeviceToHost));
+    if (bad) {
+        CK(c, cudaMemset(c->plan.status, 0, sizeof(int)));
+        return fail(c, MEPGL_ERR_NAN, "spline matrix is singular (coincident images)");
+    }
+    return MEPGL_OK;
+}
+
+mepgl_status mepgl_iteration(mepgl_ctx *c, char mode, int relaxation_steps, int use_cg)
+{
+    if (!c || relaxation_steps < 0) return fail(c, MEPGL_ERR_INVALID_ARG, "mepgl_iteration: bad argument");
+    mepgl_status st = MEPGL_OK;
+    switch (mode) {
+    case 'S': return mepgl_nlcg_steps(c, relaxation_steps, use_cg, 0);
+    case 'M': return mepgl_nlcg_steps(c, relaxation_steps, use_cg, 1);
+    case 'L':
+    case 'C': {
+        const int F = c->strings[0].F;
+        st = mepgl_redistribute(c, mode == 'L' ? MEPGL_REDIST_LINEAR : MEPGL_REDIST_CUBIC, F);
+        if (st != MEPGL_OK) return st;
+        st = reset_cg(c, 1, F - 1 > 1 ? F - 1 : 1);
+        if (st != MEPGL_OK) return st;
+        return mepgl_nlcg_steps(c, relaxation_steps, use_cg, 0);
+    }
+    default: return fail(c, MEPGL_ERR_INVALID_ARG, "mepgl_iteration: mode must be S, M, L or C");
+    }
+}
+
+mepgl_status mepgl_set_precision(mepgl_ctx *c, int precision)
+{
+    if (!c || (precision != MEPGL_FP32 && precision != MEPGL_FP64))
+        return fail(c, MEPGL_ERR_INVALID_ARG, "mepgl_set_precision: bad precision");
+    if (precision == c->precision) return MEPGL_OK;
+    mepgl_status st = flush(c);
+    if (st != MEPGL_OK) return st;
+    const int old = c->precision;
+    for (auto &s : c->strings) {
+        const long n = (long)s.F * s.M() * 2;
+        void *tmp[3] = {};
+        for (int f = 0; f < 1 + c->ncomp; ++f) {
+            CK(c, cudaMalloc(&tmp[f], n * real_size(precision)));
+            CK(c, launch_convert(s.x[c->xi][f], old, tmp[f], precision, n, c->stream));
+        }
+        CK(c, cudaStreamSynchronize(c->stream));
+        free_string_buffers(s);
+        c->precision = precision;
+        st = alloc_string_buffers(c, s);
+        c->precision = old;
+        if (st != MEPGL_OK) return st;
+        for (int f = 0; f < 1 + c->ncomp; ++f) {
+            CK(c, cudaMemcpyAsync(s.x[0][f], tmp[f], n * real_size(precision), cudaMemcpyDeviceToDevice, c->stream));
+        }
+        CK(c, cudaStreamSynchronize(c->stream));
+        for (int f = 0; f < 1 + c->ncomp; ++f) cudaFree(tmp[f]);
+    }
+    c->precision = precision;
+    for (auto &s : c->strings) {
+        st = upload_string_params(c, s);
+        if (st != MEPGL_OK) return st;
+    }
+    c->xi = 0;
+    c->di = 0;
+    st = build_layout(c);
+    if (st != MEPGL_OK) return st;
+    return reset_history(c);
+}
+
+mepgl_status mepgl_info(const mepgl_ctx *c, int *n_images, int *precision, int64_t *kernel_launches)
+{
+    if (!c) return MEPGL_ERR_INVALID_ARG;
+    if (n_images) *n_images = c->strings[0].F;
+    if (precision) *precision = c->precision;
+    if (kernel_launches) *kernel_launches = c->launches;
+    return MEPGL_OK;
+}
+
+mepgl_status mepgl_profile_passes(mepgl_ctx *c, int steps, int use_cg, double *ms_grad, double *ms_dir_poly)
+{
+    if (!c || steps < 1) return fail(c, MEPGL_ERR_INVALID_ARG, "mepgl_profile_passes: steps must be >= 1");
+    std::vector<cudaEvent_t> ev(2 * steps + 1);
+    for (auto &e : ev) CK(c, cudaEventCreate(&e));
+    const Launch L = make_launch(c);
+    CK(c, cudaEventRecord(ev[0], c->stream));
+    for (int it = 1; it <= steps; ++it) {
+        const StepFlags f = step_flags(c, it, use_cg ? 1 : 0, 0);
+        CK(c, launch_grad(L, c->sc, f));
+        CK(c, cudaEventRecord(ev[2 * it - 1], c->stream));
+        CK(c, launch_dir_poly(L, c->sc, f));
+        CK(c, cudaEventRecord(ev[2 * it], c->stream));
+        c->xi ^= 1;
+        c->di ^= 1;
+        c->launches += 2;
+        c->pending = true;
+    }
+    CK(c, cudaEventSynchronize(ev[2 * steps]));
+    double tg = 0, td = 0;
+    for (int it = 1; it <= steps; ++it) {
+        float a = 0, b = 0;
+        CK(c, cudaEventElapsedTime(&a, ev[2 * it - 2], ev[2 * it - 1]));
+        CK(c, cudaEventElapsedTime(&b, ev[2 * it - 1], ev[2 * it]));
+        tg += a;
+        td += b;
+    }
+    for (auto &e : ev) cudaEventDestroy(e);
+    if (ms_grad) *ms_grad = tg / steps;
+    if (ms_dir_poly) *ms_dir_poly = td / steps;
+    return MEPGL_OK;
+}
+
+mepgl_status mepgl_synchronize(mepgl_ctx *c)
+{
+    if (!c) return MEPGL_ERR_INVALID_ARG;
+    CK(c, cudaStreamSynchronize(c->stream));
+    return MEPGL_OK;
+}
+
+}  // extern "C"

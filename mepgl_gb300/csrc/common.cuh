@@ -1,0 +1,126 @@
+// common.cuh -- shared device-side definitions of libmepgl_gb300.
+//
+// Work decomposition.  Every pass over the string is a list of tiles; a
+// tile is TX x TY sites of one image of one string.  Kernels walk the tile
+// list with a grid-stride loop, so one launch covers every image of every
+// string in the context (strings may differ in size and image count).
+// Per-image reductions are deterministic: each tile writes one partial per
+// quantity, and the last tile of an image to finish (atomic ticket per
+// image) sums that image's partials in a fixed order.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace mepgl {
+
+constexpr int TX = 32;        // tile width: one warp per tile row
+constexpr int NT = 256;       // threads per block for the lattice kernels
+
+template <class T> struct Vec2;
+template <> struct Vec2<float> { using type = float2; };
+template <> struct Vec2<double> { using type = double2; };
+template <class T> using vec2_t = typename Vec2<T>::type;
+
+// One string (one lattice, F images) as seen by the kernels.  Field buffers
+// hold three arrays each (A, psi_1, psi_2) of F*nx*ny pairs; psi_2 is null
+// for one component.  Buffers: x (state, ping-pong), g (gradient, two
+// slots), d (direction, ping-pong).
+struct StringDesc {
+    int nx, ny, F, ncomp;
+    int tiles_x, tiles_y;     // tiles per image
+    int img_base;             // first global image index of this string
+    int tile_base;            // first global tile index of this string
+    int thin_film;
+    int per_site;             // 1: parameters read from the arrays below
+    double dx, inv_dx;
+    double q[2], eta, gamma, delta;
+    double a[2], b[2], mxx[2], myy[2], h;          // uniform values
+    double hmx[2], hmy[2], aob[2];                 // 0.5/m_xx, 0.5/m_yy, a/b (uniform)
+    const void *pa[2], *pb[2], *pmxx[2], *pmyy[2], *ph;  // per-site (type T)
+    const uint16_t *mask;     // per site: comp code | sc code << 8
+    void *x[2][3], *g[2][3], *d[2][3];
+};
+
+struct TileRef {
+    int16_t s;        // string
+    int16_t ty;       // tile row
+    int16_t tx;       // tile column
+    int16_t pad;
+    int32_t n;        // image
+};
+
+// Per-image scalars of the whole context (index = img_base + n).
+struct Scalars {
+    double *gn[2];        // |g|^2, two slots (nlcgSteps' g_norm2 / g_norm2_old)
+    double *gdg;          // g . (g - g_prev)
+    double *beta;         // Polak-Ribiere coefficient of the last step
+    double *alpha;        // step of the last line search (reported)
+    double *alpha_pend;   // step not yet applied to x (0 = nothing pending)
+    double *fenergy;      // energy (polynomial constant term)
+    double *poly;         // [img][4] = B, C, D, E
+    double *part;         // per-tile partials, [tile][8]
+    unsigned *ticket;     // per-image arrival counters
+    double *xtab_f, *xtab_d;   // line-search grid x_p, p = 0..2000, rounded to float / double
+    int *status;          // device-side error flags
+};
+
+__device__ __forceinline__ unsigned bit(unsigned c, int n) { return (c >> n) & 1u; }
+
+// Block-wide sum of NV doubles in a fixed order; result valid in thread 0.
+template <int NV>
+__device__ __forceinline__ void block_sum(double (&v)[NV], double *smem /* NT/32*NV */)
+{
+#pragma unroll
+    for (int k = 0; k < NV; ++k)
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v[k] += __shfl_down_sync(0xffffffffu, v[k], o);
+    const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+    if (l == 0)
+#pragma unroll
+        for (int k = 0; k < NV; ++k) smem[w * NV + k] = v[k];
+    __syncthreads();
+    if (threadIdx.x < 32) {
+#pragma unroll
+        for (int k = 0; k < NV; ++k) {
+            double t = (l < NT / 32) ? smem[l * NV + k] : 0.0;
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) t += __shfl_down_sync(0xffffffffu, t, o);
+            v[k] = t;
+        }
+    }
+    __syncthreads();
+}
+
+// Write this tile's NV partials; return true (in every thread) if this
+// block is the last of its image, in which case `tot` holds the image sums
+// (in thread 0) computed over the image's partials in index order.
+template <int NV>
+__device__ __forceinline__ bool finish_image(double (&v)[NV], double *smem, const Scalars &sc, int tile, int first_tile,
+                             int tiles_per_image, int img, double (&tot)[NV])
+{
+    __shared__ bool last;
+    block_sum<NV>(v, smem);
+    if (threadIdx.x == 0) {
+#pragma unroll
+        for (int k = 0; k < NV; ++k) sc.part[(size_t)tile * 8 + k] = v[k];
+        __threadfence();
+        const unsigned prev = atomicAdd(&sc.ticket[img], 1u);
+        last = (prev == (unsigned)tiles_per_image - 1);
+    }
+    __syncthreads();
+    if (!last) return false;
+    __threadfence();
+#pragma unroll
+    for (int k = 0; k < NV; ++k) tot[k] = 0;
+    for (int t = threadIdx.x; t < tiles_per_image; t += NT) {
+        const double *p = sc.part + (size_t)(first_tile + t) * 8;
+#pragma unroll
+        for (int k = 0; k < NV; ++k) tot[k] += __ldcg(p + k);
+    }
+    block_sum<NV>(tot, smem);
+    if (threadIdx.x == 0) sc.ticket[img] = 0;
+    return true;
+}
+
+}  // namespace mepgl

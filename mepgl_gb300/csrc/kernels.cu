@@ -1,0 +1,726 @@
+// kernels.cu -- CUDA kernels of libmepgl_gb300 (sm_103a).
+//
+// The NLCG iteration of the reference (nlcgSteps, mepgl/src/nlcg.cu:1462-1586:
+// ~12 kernels, 4 two-level reductions, ~10 device-wide syncs per step) is two
+// passes over the string here:
+//
+//   k_grad      x <- x + alpha_pend d   (the previous step's update, fused)
+//               g  = dF/dx              (gradientPsi + gradientA)
+//               |g|^2, g.(g - g_prev)   (gradientDensity + 2 sums)
+//               last tile of an image:  beta (computeStepDirection's scalar)
+//   k_dir_poly  d <- -g + beta d        (computeStepDirection)
+//               quartic F(x + a d)      (polynomialExpansion + 2 sums)
+//               last tile of an image:  line search -> alpha (lineSearch)
+//
+// so one step reads x, d, g_prev, g (twice with halo, served mostly by L2)
+// and writes x, g, d: 9 state-sized streams instead of the reference's ~20.
+// x and d are ping-ponged because neighbouring tiles read them as halo while
+// they are being rewritten.
+#include "kernels.cuh"
+#include "site_ops.cuh"
+
+namespace mepgl {
+
+namespace {
+
+// ------------------------------------------------------------------ staging
+template <class T, int NC>
+__device__ __forceinline__ void stage_state(Tile<T, NC, TY> &t, const StringDesc &S, int n, int i0, int j0,
+                                            int xin, int xout, int dbuf, T alpha, bool write_x)
+{
+    using V = vec2_t<T>;
+    const long M = (long)S.nx * S.ny, off = (long)n * M;
+    for (int q = threadIdx.x; q < (TX + 2) * (TY + 2); q += NT) {
+        const int hx = q % (TX + 2), hy = q / (TX + 2);
+        const int gi = i0 + hx - 1, gj = j0 + hy - 1;
+        V f[1 + NC];
+        uint16_t m = 0;
+        if (gi >= 0 && gi < S.nx && gj >= 0 && gj < S.ny) {
+            const long s = gi + (long)S.nx * gj, k = off + s;
+            m = S.mask[s];
+#pragma unroll
+            for (int c = 0; c < 1 + NC; ++c) f[c] = static_cast<const V *>(S.x[xin][c])[k];
+            if (alpha != (T)0) {
+#pragma unroll
+                for (int c = 0; c < 1 + NC; ++c) {
+                    const V dd = static_cast<const V *>(S.d[dbuf][c])[k];
+                    f[c].x = f[c].x + alpha * dd.x;
+                    f[c].y = f[c].y + alpha * dd.y;
+                }
+            }
+            if (write_x && hx >= 1 && hx <= TX && hy >= 1 && hy <= TY)
+#pragma unroll
+                for (int c = 0; c < 1 + NC; ++c) static_cast<V *>(S.x[xout][c])[k] = f[c];
+        } else {
+#pragma unroll
+            for (int c = 0; c < 1 + NC; ++c) f[c].x = f[c].y = (T)0;
+        }
+        t.A[hy][hx] = f[0];
+#pragma unroll
+        for (int c = 0; c < NC; ++c) t.P[c][hy][hx] = f[1 + c];
+        t.m[hy][hx] = m;
+    }
+}
+
+template <class T, int NC>
+__device__ __forceinline__ void stage_direction(Tile<T, NC, TY> &t, const StringDesc &S, int n, int i0, int j0,
+                                                int gcur, int din, int dout, T beta)
+{
+    using V = vec2_t<T>;
+    const long M = (long)S.nx * S.ny, off = (long)n * M;
+    for (int q = threadIdx.x; q < (TX + 2) * (TY + 2); q += NT) {
+        const int hx = q % (TX + 2), hy = q / (TX + 2);
+        const int gi = i0 + hx - 1, gj = j0 + hy - 1;
+        V f[1 + NC];
+        if (gi >= 0 && gi < S.nx && gj >= 0 && gj < S.ny) {
+            const long k = off + gi + (long)S.nx * gj;
+#pragma unroll
+            for (int c = 0; c < 1 + NC; ++c) {
+                const V gg = static_cast<const V *>(S.g[gcur][c])[k];
+                const V dd = static_cast<const V *>(S.d[din][c])[k];
+                f[c].x = -gg.x + beta * dd.x;
+                f[c].y = -gg.y + beta * dd.y;
+            }
+            if (hx >= 1 && hx <= TX && hy >= 1 && hy <= TY)
+#pragma unroll
+                for (int c = 0; c < 1 + NC; ++c) static_cast<V *>(S.d[dout][c])[k] = f[c];
+        } else {
+#pragma unroll
+            for (int c = 0; c < 1 + NC; ++c) f[c].x = f[c].y = (T)0;
+        }
+        t.A[hy][hx] = f[0];
+#pragma unroll
+        for (int c = 0; c < NC; ++c) t.P[c][hy][hx] = f[1 + c];
+    }
+}
+
+// --------------------------------------------------------------- line search
+// Quartic A + B x + C x^2 + D x^3 + E x^4 evaluated in round-to-nearest
+// double without contraction, in the oracle's order.
+__device__ __forceinline__ double quartic_rn(const double *c, double x)
+{
+    const double x2 = __dmul_rn(x, x);
+    double f = __dmul_rn(c[4], __dmul_rn(x2, x2));
+    f = __dadd_rn(f, __dmul_rn(__dmul_rn(__dmul_rn(c[3], x), x), x));
+    f = __dadd_rn(f, __dmul_rn(__dmul_rn(c[2], x), x));
+    f = __dadd_rn(f, __dmul_rn(c[1], x));
+    return __dadd_rn(f, c[0]);
+}
+
+// lineSearch (nlcg.cu:1398-1445) by one warp: first p in 1..2000 with
+// f(x_p) > f(x_{p-1}) (else 2000); alpha = x_p / m in the working precision.
+template <class T>
+__device__ double line_search_scan(const double *c, const double *xt)
+{
+    const int lane = threadIdx.x & 31;
+    double f_prev = quartic_rn(c, xt[0]);
+    int found = 0;
+    for (int base = 1; base <= 2000; base += 32) {
+        const int p = base + lane;
+        const double fp = p <= 2000 ? quartic_rn(c, xt[p]) : 0.0;
+        double fl = __shfl_up_sync(0xffffffffu, fp, 1);
+        if (lane == 0) fl = f_prev;
+        const unsigned bal = __ballot_sync(0xffffffffu, p <= 2000 && fp > fl);
+        if (bal) { found = base + __ffs(bal) - 1; break; }
+        f_prev = __shfl_sync(0xffffffffu, fp, 31);
+    }
+    const int j = found ? found : 2000;
+    const T m = (T)1.025f;
+    return (double)((T)xt[j] / m);
+}
+
+__device__ double line_search_exact(const double *c, double fallback)
+{
+    const double a3 = 4 * c[4], a2 = 3 * c[3], a1 = 2 * c[2], a0 = c[1];
+    double roots[3];
+    int nr = 0;
+    if (fabs(a0) + fabs(a1) + fabs(a2) + fabs(a3) == 0) return fallback;
+    if (fabs(a3) > 1e-300) {
+        const double A2 = a2 / a3, A1 = a1 / a3, A0 = a0 / a3;
+        const double Q = (3 * A1 - A2 * A2) / 9, R = (9 * A2 * A1 - 27 * A0 - 2 * A2 * A2 * A2) / 54;
+        const double disc = Q * Q * Q + R * R;
+        if (disc >= 0) {
+            const double sd = sqrt(disc);
+            roots[nr++] = -A2 / 3 + cbrt(R + sd) + cbrt(R - sd);
+        } else {
+            const double th = acos(R / sqrt(-Q * Q * Q)), r = 2 * sqrt(-Q);
+            roots[nr++] = r * cos(th / 3) - A2 / 3;
+            roots[nr++] = r * cos((th + 2 * M_PI) / 3) - A2 / 3;
+            roots[nr++] = r * cos((th + 4 * M_PI) / 3) - A2 / 3;
+        }
+    } else if (fabs(a2) > 1e-300) {
+        const double disc = a1 * a1 - 4 * a2 * a0;
+        if (disc >= 0) {
+            const double sq = sqrt(disc), qq = -0.5 * (a1 + (a1 >= 0 ? sq : -sq));
+            if (qq != 0) { roots[nr++] = qq / a2; roots[nr++] = a0 / qq; }
+        }
+    } else if (a1 != 0) {
+        roots[nr++] = -a0 / a1;
+    }
+    double best = -1, fbest = 0;
+    for (int t = 0; t < nr; ++t) {
+        double r = roots[t];
+        for (int it = 0; it < 2; ++it) {
+            const double dp = a0 + r * (a1 + r * (a2 + r * a3)), ddp = a1 + r * (2 * a2 + r * 3 * a3);
+            if (ddp != 0) r -= dp / ddp;
+        }
+        const double ddp = a1 + r * (2 * a2 + r * 3 * a3);
+        if (!(r > 0) || !(ddp > 0)) continue;
+        const double fr = quartic_rn(c, r);
+        if (best < 0 || fr < fbest) { best = r; fbest = fr; }
+    }
+    return best < 0 ? fallback : best;
+}
+
+// ------------------------------------------------------------------ kernels
+template <class T, int NC>
+__global__ void __launch_bounds__(NT) k_grad(const StringDesc *__restrict__ strings, const TileRef *__restrict__ tiles,
+                                             int n_tiles, Scalars sc, StepFlags f)
+{
+    using V = vec2_t<T>;
+    __shared__ Tile<T, NC, TY> t;
+    __shared__ double red[NT / 32 * 2];
+    for (int tt = blockIdx.x; tt < n_tiles; tt += gridDim.x) {
+        const TileRef tr = tiles[tt];
+        const StringDesc &S = strings[tr.s];
+        const int img = S.img_base + tr.n;
+        const int i0 = tr.tx * TX, j0 = tr.ty * TY;
+        stage_state<T, NC>(t, S, tr.n, i0, j0, f.xin, f.xout, f.din, (T)sc.alpha_pend[img], true);
+        __syncthreads();
+        const int lx = threadIdx.x % TX, ly = threadIdx.x / TX, gi = i0 + lx, gj = j0 + ly;
+        double v[2] = {0.0, 0.0};
+        if (gi < S.nx && gj < S.ny) {
+            const long s = gi + (long)S.nx * gj, k = (long)tr.n * S.nx * S.ny + s;
+            SiteParams<T> p;
+            p.load(S, s, NC);
+            T g[2 + 2 * NC];
+            site_gradient<T, NC, TY>(t, lx + 1, ly + 1, p, S, s, f.maxwell, S.thin_film, g);
+#pragma unroll
+            for (int c = 0; c < 1 + NC; ++c) {
+                V gv;
+                gv.x = g[2 * c];
+                gv.y = g[2 * c + 1];
+                static_cast<V *>(S.g[f.gcur][c])[k] = gv;
+                const V go = static_cast<const V *>(S.g[f.gprev][c])[k];
+                v[0] += (double)(gv.x * gv.x) + (double)(gv.y * gv.y);
+                v[1] += (double)(gv.x * (gv.x - go.x)) + (double)(gv.y * (gv.y - go.y));
+            }
+        }
+        const int tpi = S.tiles_x * S.tiles_y;
+        double tot[2];
+        if (finish_image<2>(v, red, sc, tt, S.tile_base + tr.n * tpi, tpi, img, tot) && threadIdx.x == 0) {
+            (f.gcur ? sc.gn[1] : sc.gn[0])[img] = tot[0];
+            sc.gdg[img] = tot[1];
+            double beta = 0.0;
+            if (f.use_cg) {
+                beta = tot[1] / (f.gprev ? sc.gn[1] : sc.gn[0])[img];
+                beta = beta > 0.0 ? beta : 0.0;   // Polak-Ribiere clipped at 0; NaN -> 0
+            }
+            sc.beta[img] = beta;
+        }
+        __syncthreads();
+    }
+}
+
+template <class T, int NC>
+__global__ void __launch_bounds__(NT) k_dir_poly(const StringDesc *__restrict__ strings,
+                                                 const TileRef *__restrict__ tiles, int n_tiles, Scalars sc,
+                                                 StepFlags f)
+{
+    __shared__ Tile<T, NC, TY> tx;
+    __shared__ Tile<T, NC, TY> td;
+    __shared__ double red[NT / 32 * 5];
+    __shared__ double coef[5];
+    for (int tt = blockIdx.x; tt < n_tiles; tt += gridDim.x) {
+        const TileRef tr = tiles[tt];
+        const StringDesc &S = strings[tr.s];
+        const int img = S.img_base + tr.n;
+        const int i0 = tr.tx * TX, j0 = tr.ty * TY;
+        stage_state<T, NC>(tx, S, tr.n, i0, j0, f.xout, f.xout, f.din, (T)0, false);
+        stage_direction<T, NC>(td, S, tr.n, i0, j0, f.gcur, f.din, f.dout, (T)sc.beta[img]);
+        __syncthreads();
+        const int lx = threadIdx.x % TX, ly = threadIdx.x / TX, gi = i0 + lx, gj = j0 + ly;
+        double v[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
+        if (gi < S.nx && gj < S.ny) {
+            const long s = gi + (long)S.nx * gj;
+            SiteParams<T> p;
+            p.load(S, s, NC);
+            T o[5];
+            site_poly<T, NC, TY>(tx, td, lx + 1, ly + 1, p, f.poly_compat, S.thin_film, o);
+#pragma unroll
+            for (int k = 0; k < 5; ++k) v[k] = (double)o[k];
+        }
+        const int tpi = S.tiles_x * S.tiles_y;
+        double tot[5];
+        if (finish_image<5>(v, red, sc, tt, S.tile_base + tr.n * tpi, tpi, img, tot)) {
+            if (threadIdx.x == 0) {
+#pragma unroll
+                for (int k = 0; k < 5; ++k) coef[k] = tot[k];
+                sc.fenergy[img] = tot[0];
+#pragma unroll
+                for (int k = 0; k < 4; ++k) sc.poly[4 * img + k] = tot[1 + k];
+            }
+            __syncthreads();
+            if (threadIdx.x < 32) {
+                const double *xt = sizeof(T) == 8 ? sc.xtab_d : sc.xtab_f;
+                double alpha = line_search_scan<T>(coef, xt);
+                if (f.ls_exact) alpha = line_search_exact(coef, alpha);
+                if (threadIdx.x == 0) {
+                    sc.alpha[img] = alpha;
+                    sc.alpha_pend[img] = alpha;
+                }
+            }
+        }
+        __syncthreads();
+    }
+}
+
+template <class T, int NC>
+__global__ void __launch_bounds__(NT) k_energy(const StringDesc *__restrict__ strings, const TileRef *__restrict__ tiles,
+                                               int n_tiles, Scalars sc, int xbuf, double *out)
+{
+    __shared__ Tile<T, NC, TY> t;
+    __shared__ double red[NT / 32];
+    for (int tt = blockIdx.x; tt < n_tiles; tt += gridDim.x) {
+        const TileRef tr = tiles[tt];
+        const StringDesc &S = strings[tr.s];
+        const int img = S.img_base + tr.n;
+        const int i0 = tr.tx * TX, j0 = tr.ty * TY;
+        stage_state<T, NC>(t, S, tr.n, i0, j0, xbuf, xbuf, 0, (T)0, false);
+        __syncthreads();
+        const int lx = threadIdx.x % TX, ly = threadIdx.x / TX, gi = i0 + lx, gj = j0 + ly;
+        double v[1] = {0.0};
+        if (gi < S.nx && gj < S.ny) {
+            const long s = gi + (long)S.nx * gj;
+            SiteParams<T> p;
+            p.load(S, s, NC);
+            v[0] = (double)site_energy<T, NC, TY>(t, lx + 1, ly + 1, p, S.thin_film);
+        }
+        const int tpi = S.tiles_x * S.tiles_y;
+        double tot[1];
+        if (finish_image<1>(v, red, sc, tt, S.tile_base + tr.n * tpi, tpi, img, tot) && threadIdx.x == 0)
+            out[img] = tot[0];
+        __syncthreads();
+    }
+}
+
+template <class T, int NC>
+__global__ void __launch_bounds__(NT) k_gradient_only(const StringDesc *__restrict__ strings,
+                                                      const TileRef *__restrict__ tiles, int n_tiles, int xbuf,
+                                                      FieldPtrs out, int maxwell)
+{
+    using V = vec2_t<T>;
+    __shared__ Tile<T, NC, TY> t;
+    for (int tt = blockIdx.x; tt < n_tiles; tt += gridDim.x) {
+        const TileRef tr = tiles[tt];
+        const StringDesc &S = strings[tr.s];
+        const int i0 = tr.tx * TX, j0 = tr.ty * TY;
+        stage_state<T, NC>(t, S, tr.n, i0, j0, xbuf, xbuf, 0, (T)0, false);
+        __syncthreads();
+        const int lx = threadIdx.x % TX, ly = threadIdx.x / TX, gi = i0 + lx, gj = j0 + ly;
+        if (gi < S.nx && gj < S.ny) {
+            const long s = gi + (long)S.nx * gj, k = (long)tr.n * S.nx * S.ny + s;
+            SiteParams<T> p;
+            p.load(S, s, NC);
+            T g[2 + 2 * NC];
+            site_gradient<T, NC, TY>(t, lx + 1, ly + 1, p, S, s, maxwell, S.thin_film, g);
+#pragma unroll
+            for (int c = 0; c < 1 + NC; ++c) {
+                V gv;
+                gv.x = g[2 * c];
+                gv.y = g[2 * c + 1];
+                static_cast<V *>(out.p[c])[k] = gv;
+            }
+        }
+        __syncthreads();
+    }
+}
+
+template <class T, int NC>
+__global__ void __launch_bounds__(NT) k_jb(const StringDesc *__restrict__ strings, const TileRef *__restrict__ tiles,
+                                           int n_tiles, int xbuf, T *b, vec2_t<T> *j1, vec2_t<T> *j2)
+{
+    using V = vec2_t<T>;
+    __shared__ Tile<T, NC, TY> t;
+    for (int tt = blockIdx.x; tt < n_tiles; tt += gridDim.x) {
+        const TileRef tr = tiles[tt];
+        const StringDesc &S = strings[tr.s];
+        const int i0 = tr.tx * TX, j0 = tr.ty * TY;
+        stage_state<T, NC>(t, S, tr.n, i0, j0, xbuf, xbuf, 0, (T)0, false);
+        __syncthreads();
+        const int lx = threadIdx.x % TX, ly = threadIdx.x / TX, gi = i0 + lx, gj = j0 + ly;
+        if (gi < S.nx && gj < S.ny) {
+            const long s = gi + (long)S.nx * gj, k = (long)tr.n * S.nx * S.ny + s;
+            SiteParams<T> p;
+            p.load(S, s, NC);
+            T o[1 + 2 * NC];
+            site_jb<T, NC, TY>(t, lx + 1, ly + 1, p, o);
+            b[k] = o[0];
+            V v;
+            v.x = o[1];
+            v.y = o[2];
+            j1[k] = v;
+            if (NC == 2) {
+                v.x = o[3];
+                v.y = o[4];
+                j2[k] = v;
+            }
+        }
+        __syncthreads();
+    }
+}
+
+template <class T>
+__global__ void __launch_bounds__(NT) k_apply_update(vec2_t<T> *x, const vec2_t<T> *d, const double *alpha_pend,
+                                                     long M, long total)
+{
+    for (long p = blockIdx.x * (long)NT + threadIdx.x; p < total; p += (long)gridDim.x * NT) {
+        const T a = (T)alpha_pend[p / M];
+        if (a != (T)0) {
+            vec2_t<T> v = x[p];
+            const vec2_t<T> dd = d[p];
+            v.x = v.x + a * dd.x;
+            v.y = v.y + a * dd.y;
+            x[p] = v;
+        }
+    }
+}
+
+// Arc length: squared image-to-image distance over every site (no mask, no
+// dx^2; interpolation.cu:39-92).  Each thread walks its sites through the
+// images, carrying image n-1 in registers, so every value is read once.
+constexpr int ARC_SPT = 4;
+
+template <class T>
+__global__ void __launch_bounds__(NT) k_arc_partial(const T *f0, const T *f1, const T *f2, int w0, int w1, int w2,
+                                                    long sites, int F, double *part)
+{
+    __shared__ double red[NT / 32];
+    const T *fs[3] = {f0, f1, f2};
+    const int ws[3] = {w0, w1, w2};
+    T prev[3][ARC_SPT][2];
+    const long base = (long)blockIdx.x * NT * ARC_SPT + threadIdx.x;
+    for (int n = 0; n < F; ++n) {
+        double acc = 0.0;
+#pragma unroll
+        for (int q = 0; q < ARC_SPT; ++q) {
+            const long s = base + (long)q * NT;
+            if (s >= sites) continue;
+            T d2 = 0;
+#pragma unroll
+            for (int f = 0; f < 3; ++f) {
+                if (!fs[f]) continue;
+#pragma unroll
+                for (int w = 0; w < 2; ++w) {
+                    if (w >= ws[f]) continue;
+                    const T v = fs[f][((long)n * sites + s) * ws[f] + w];
+                    if (n > 0) d2 += (v - prev[f][q][w]) * (v - prev[f][q][w]);
+                    prev[f][q][w] = v;
+                }
+            }
+            acc += (double)d2;
+        }
+        double vv[1] = {acc};
+        block_sum<1>(vv, red);
+        if (threadIdx.x == 0) part[(size_t)n * gridDim.x + blockIdx.x] = vv[0];
+    }
+}
+
+// computeArcLength (interpolation.cu:126-140): cumulative sqrt, s[F-1] = 1.
+__global__ void k_arc_finish(const double *part, int nblocks, int F, double *s)
+{
+    __shared__ double red[NT / 32];
+    for (int n = 0; n < F; ++n) {
+        double v[1] = {0.0};
+        for (int b = threadIdx.x; b < nblocks; b += NT) v[0] += part[(size_t)n * nblocks + b];
+        block_sum<1>(v, red);
+        if (threadIdx.x == 0) s[n] = v[0];
+    }
+    if (threadIdx.x == 0) {
+        s[0] = 0.0;
+        for (int n = 1; n < F; ++n) s[n] = s[n - 1] + sqrt(s[n]);
+        for (int n = 0; n < F; ++n) s[n] /= s[F - 1];
+    }
+}
+
+// Redistribution plan (one thread): segment and weight per output image,
+// and for the cubic spline the Forsythe-Malcolm-Moler matrix (buildHMatrix,
+// interpolation.cu:252-290) factorised once by Gaussian elimination with
+// partial pivoting (the LAPACK gtsv algorithm) for every site's system.
+__global__ void k_redist_plan(const double *s, int F, int F_new, int cubic, int spline, RedistPlan p)
+{
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    double *h = p.h;
+    h[0] = 0.0;
+    for (int n = 1; n < F; ++n) h[n] = s[n] - s[n - 1];
+    h[F] = INFINITY;
+    const bool walk_sum = cubic && spline == 0;
+    int k = 1;
+    double seg_start = 0.0, seg_end = walk_sum ? h[1] : s[1];
+    for (int n = 0; n < F_new; ++n) {
+        const double s_new = (double)n / (double)(F_new - 1);
+        if (walk_sum) {
+            while (seg_end < s_new) { k++; seg_start += h[k - 1]; seg_end += h[k]; }
+        } else {
+            while (seg_end < s_new && k < F - 1) { k++; seg_start = s[k - 1]; seg_end = s[k]; }
+        }
+        if (k >= F) k = F - 1;
+        p.k[n] = k;
+        p.w[n] = (s_new - seg_start) / (cubic ? h[k] : (s[k] - s[k - 1]));
+    }
+    if (!cubic) return;
+    double *dl = p.dl, *d = p.d, *du = p.du, *du2 = p.du2;
+    int *ipiv = p.ipiv;
+    for (int n = 0; n < F; ++n) { dl[n] = d[n] = du[n] = du2[n] = 0.0; ipiv[n] = 0; }
+    d[0] = -h[1];
+    du[0] = h[1];
+    for (int n = 1; n < F - 1; ++n) { dl[n] = h[n]; d[n] = 2 * (h[n] + h[n + 1]); du[n] = h[n + 1]; }
+    dl[F - 1] = h[F - 1];
+    d[F - 1] = -h[F - 1];
+    for (int q = 0; q < F - 1; ++q) {
+        const double sub = dl[q + 1];
+        if (fabs(d[q]) >= fabs(sub)) {
+            if (d[q] != 0) {
+                const double l = sub / d[q];
+                dl[q + 1] = l;
+                d[q + 1] = d[q + 1] - l * du[q];
+            } else {
+                dl[q + 1] = 0;
+            }
+        } else {
+            const double l = d[q] / sub;
+            d[q] = sub;
+            dl[q + 1] = l;
+            const double tmp = du[q];
+            du[q] = d[q + 1];
+            d[q + 1] = tmp - l * d[q + 1];
+            if (q < F - 2) {
+                du2[q] = du[q + 1];
+                du[q + 1] = -l * du[q + 1];
+            }
+            ipiv[q] = 1;
+        }
+    }
+    for (int q = 0; q < F; ++q)
+        if (d[q] == 0 && p.status) *p.status = 1;
+}
+
+template <class T>
+__global__ void __launch_bounds__(NT) k_redist_linear(const T *f, T *fnew, long reals, int F_new, const int *kk,
+                                                      const double *ww)
+{
+    const long total = reals * F_new;
+    for (long e = blockIdx.x * (long)NT + threadIdx.x; e < total; e += (long)gridDim.x * NT) {
+        const int n = (int)(e / reals);
+        const long r = e - (long)n * reals;
+        const int k = kk[n];
+        const T w = (T)ww[n];
+        fnew[e] = w * f[(long)k * reals + r] + (1 - w) * f[(long)(k - 1) * reals + r];
+    }
+}
+
+// Cubic resample (computeDeltaX/Y + gtsv + generateNewFramesCubic,
+// interpolation.cu:292-402), one thread per real of a site: builds the
+// right-hand side in the strided scratch, solves with the shared factors,
+// evaluates the new images.  Double throughout.
+template <class T>
+__global__ void __launch_bounds__(NT) k_redist_cubic(const T *f, T *fnew, double *sig, long reals, int F, int F_new,
+                                                     int spline, RedistPlan p)
+{
+    for (long e = blockIdx.x * (long)NT + threadIdx.x; e < reals; e += (long)gridDim.x * NT) {
+        const double *h = p.h;
+#define FV(n) ((double)f[(long)(n) * reals + e])
+#define SG(n) sig[(long)(n) * reals + e]
+        // first divided differences D[n] = (f_n - f_{n-1}) / h_n, n >= 1
+        const double D1 = (FV(1) - FV(0)) / h[1], D2 = (FV(2) - FV(1)) / h[2], D3 = (FV(3) - FV(2)) / h[3];
+        const double Dm1 = (FV(F - 1) - FV(F - 2)) / h[F - 1], Dm2 = (FV(F - 2) - FV(F - 3)) / h[F - 2];
+        const double Dm3 = (FV(F - 3) - FV(F - 4)) / h[F - 3];
+        const double d3s = ((D3 - D2) / (h[3] + h[2]) - (D2 - D1) / (h[2] + h[1])) / (h[3] + h[2] + h[1]);
+        const double d3e = ((Dm1 - Dm2) / (h[F - 1] + h[F - 2]) - (Dm2 - Dm3) / (h[F - 2] + h[F - 3])) /
+                           (h[F - 1] + h[F - 2] + h[F - 3]);
+        double Dn = D1;
+        for (int n = 1; n < F - 1; ++n) {
+            const double Dn1 = (FV(n + 1) - FV(n)) / h[n + 1];
+            SG(n) = Dn1 - Dn;
+            Dn = Dn1;
+        }
+        SG(0) = h[1] * h[1] * d3s;
+        SG(F - 1) = -(h[F - 1] * h[F - 1]) * d3e;
+        // forward elimination with the recorded pivots
+        for (int q = 0; q < F - 1; ++q) {
+            const double bk = SG(q), bk1 = SG(q + 1);
+            if (p.ipiv[q]) {
+                SG(q) = bk1;
+                SG(q + 1) = bk - p.dl[q + 1] * bk1;
+            } else {
+                SG(q + 1) = bk1 - p.dl[q + 1] * bk;
+            }
+        }
+        SG(F - 1) = SG(F - 1) / p.d[F - 1];
+        SG(F - 2) = (SG(F - 2) - p.du[F - 2] * SG(F - 1)) / p.d[F - 2];
+        for (int q = F - 3; q >= 0; --q) SG(q) = (SG(q) - p.du[q] * SG(q + 1) - p.du2[q] * SG(q + 2)) / p.d[q];
+        for (int n = 0; n < F_new; ++n) {
+            const int k = p.k[n];
+            const double w = p.w[n], wm = spline == 0 ? (w - 1) : (1 - w), hk2 = h[k] * h[k];
+            fnew[(long)n * reals + e] =
+                (T)(w * FV(k) + (1 - w) * FV(k - 1) + hk2 * ((w * w * w - w) * SG(k) + (wm * wm * wm - wm) * SG(k - 1)));
+        }
+#undef FV
+#undef SG
+    }
+}
+
+template <class S, class D>
+__global__ void k_convert(const S *src, D *dst, long n)
+{
+    for (long e = blockIdx.x * (long)NT + threadIdx.x; e < n; e += (long)gridDim.x * NT) dst[e] = (D)src[e];
+}
+
+inline int grid_for(long n, int cap = 152 * 16)
+{
+    long b = (n + NT - 1) / NT;
+    return (int)(b < 1 ? 1 : (b > cap ? cap : b));
+}
+
+}  // namespace
+
+// ----------------------------------------------------------------- launchers
+#define DISPATCH(L, KERNEL, ...)                                                                    \
+    do {                                                                                            \
+        if ((L).precision == 1) {                                                                   \
+            if ((L).ncomp == 2) KERNEL<double, 2><<<(L).grid, NT, 0, (L).stream>>>(__VA_ARGS__);   \
+            else KERNEL<double, 1><<<(L).grid, NT, 0, (L).stream>>>(__VA_ARGS__);                  \
+        } else {                                                                                    \
+            if ((L).ncomp == 2) KERNEL<float, 2><<<(L).grid, NT, 0, (L).stream>>>(__VA_ARGS__);    \
+            else KERNEL<float, 1><<<(L).grid, NT, 0, (L).stream>>>(__VA_ARGS__);                   \
+        }                                                                                           \
+    } while (0)
+
+cudaError_t launch_grad(const Launch &L, const Scalars &sc, const StepFlags &f)
+{
+    DISPATCH(L, k_grad, L.strings, L.tiles, L.n_tiles, sc, f);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_dir_poly(const Launch &L, const Scalars &sc, const StepFlags &f)
+{
+    DISPATCH(L, k_dir_poly, L.strings, L.tiles, L.n_tiles, sc, f);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_energy(const Launch &L, const Scalars &sc, int xbuf, double *out)
+{
+    DISPATCH(L, k_energy, L.strings, L.tiles, L.n_tiles, sc, xbuf, out);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_gradient_only(const Launch &L, int xbuf, FieldPtrs out, int maxwell)
+{
+    DISPATCH(L, k_gradient_only, L.strings, L.tiles, L.n_tiles, xbuf, out, maxwell);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_jb(const Launch &L, const Scalars &sc, int xbuf, void *const *b, void *const (*j)[2])
+{
+    (void)sc;
+    if (L.precision == 1) {
+        if (L.ncomp == 2)
+            k_jb<double, 2><<<L.grid, NT, 0, L.stream>>>(L.strings, L.tiles, L.n_tiles, xbuf, (double *)b[0],
+                                                         (double2 *)j[0][0], (double2 *)j[0][1]);
+        else
+            k_jb<double, 1><<<L.grid, NT, 0, L.stream>>>(L.strings, L.tiles, L.n_tiles, xbuf, (double *)b[0],
+                                                         (double2 *)j[0][0], (double2 *)j[0][1]);
+    } else {
+        if (L.ncomp == 2)
+            k_jb<float, 2><<<L.grid, NT, 0, L.stream>>>(L.strings, L.tiles, L.n_tiles, xbuf, (float *)b[0],
+                                                        (float2 *)j[0][0], (float2 *)j[0][1]);
+        else
+            k_jb<float, 1><<<L.grid, NT, 0, L.stream>>>(L.strings, L.tiles, L.n_tiles, xbuf, (float *)b[0],
+                                                        (float2 *)j[0][0], (float2 *)j[0][1]);
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_apply_update(const Launch &L, const Scalars &sc, const StringDesc *hs, int n_strings, int xbuf,
+                                int dbuf)
+{
+    for (int si = 0; si < n_strings; ++si) {
+        const StringDesc &S = hs[si];
+        const long M = (long)S.nx * S.ny, total = M * S.F;
+        for (int c = 0; c < 1 + S.ncomp; ++c) {
+            if (L.precision == 1)
+                k_apply_update<double><<<grid_for(total), NT, 0, L.stream>>>(
+                    (double2 *)S.x[xbuf][c], (const double2 *)S.d[dbuf][c], sc.alpha_pend + S.img_base, M, total);
+            else
+                k_apply_update<float><<<grid_for(total), NT, 0, L.stream>>>(
+                    (float2 *)S.x[xbuf][c], (const float2 *)S.d[dbuf][c], sc.alpha_pend + S.img_base, M, total);
+        }
+    }
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    int total_images = 0;
+    for (int si = 0; si < n_strings; ++si) total_images += hs[si].F;
+    return cudaMemsetAsync(sc.alpha_pend, 0, sizeof(double) * total_images, L.stream);
+}
+
+cudaError_t launch_arc_length(int precision, const void *const *fields, const int *width, int nf, long sites, int F,
+                              double *part, double *s, cudaStream_t st)
+{
+    const int nb = (int)((sites + (long)NT * ARC_SPT - 1) / ((long)NT * ARC_SPT));
+    const void *f[3] = {nf > 0 ? fields[0] : nullptr, nf > 1 ? fields[1] : nullptr, nf > 2 ? fields[2] : nullptr};
+    const int w[3] = {nf > 0 ? width[0] : 0, nf > 1 ? width[1] : 0, nf > 2 ? width[2] : 0};
+    if (precision == 1)
+        k_arc_partial<double><<<nb, NT, 0, st>>>((const double *)f[0], (const double *)f[1], (const double *)f[2],
+                                                 w[0], w[1], w[2], sites, F, part);
+    else
+        k_arc_partial<float><<<nb, NT, 0, st>>>((const float *)f[0], (const float *)f[1], (const float *)f[2], w[0],
+                                                w[1], w[2], sites, F, part);
+    k_arc_finish<<<1, NT, 0, st>>>(part, nb, F, s);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_redist_plan(const double *s, int F, int F_new, int cubic, int spline, const RedistPlan &p,
+                               cudaStream_t st)
+{
+    k_redist_plan<<<1, 32, 0, st>>>(s, F, F_new, cubic, spline, p);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_redist_linear(int precision, const void *f, void *fnew, long pairs, int F_new, const RedistPlan &p,
+                                 cudaStream_t st)
+{
+    const long reals = 2 * pairs;
+    if (precision == 1)
+        k_redist_linear<double><<<grid_for(reals * F_new), NT, 0, st>>>((const double *)f, (double *)fnew, reals,
+                                                                        F_new, p.k, p.w);
+    else
+        k_redist_linear<float><<<grid_for(reals * F_new), NT, 0, st>>>((const float *)f, (float *)fnew, reals, F_new,
+                                                                       p.k, p.w);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_redist_cubic(int precision, const void *f, void *fnew, void *sigma, long pairs, int F, int F_new,
+                                int spline, const RedistPlan &p, cudaStream_t st)
+{
+    const long reals = 2 * pairs;
+    if (precision == 1)
+        k_redist_cubic<double><<<grid_for(reals), NT, 0, st>>>((const double *)f, (double *)fnew, (double *)sigma,
+                                                               reals, F, F_new, spline, p);
+    else
+        k_redist_cubic<float><<<grid_for(reals), NT, 0, st>>>((const float *)f, (float *)fnew, (double *)sigma, reals,
+                                                              F, F_new, spline, p);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_convert(const void *src, int src_prec, void *dst, int dst_prec, long n, cudaStream_t st)
+{
+    if (src_prec == 0 && dst_prec == 1)
+        k_convert<float, double><<<grid_for(n), NT, 0, st>>>((const float *)src, (double *)dst, n);
+    else if (src_prec == 1 && dst_prec == 0)
+        k_convert<double, float><<<grid_for(n), NT, 0, st>>>((const double *)src, (float *)dst, n);
+    else
+        return cudaMemcpyAsync(dst, src, n * (src_prec ? 8 : 4), cudaMemcpyDeviceToDevice, st);
+    return cudaGetLastError();
+}
+
+}  // namespace mepgl

@@ -1,0 +1,73 @@
+// kernels.cuh -- host-side launch interface of the lattice kernels.
+#pragma once
+
+#include "common.cuh"
+
+namespace mepgl {
+
+constexpr int TY = 8;                 // tile rows (TX * TY = NT threads, one site each)
+constexpr int LS_GRID = 2001;         // line-search grid points x_0 .. x_2000
+
+struct Launch {
+    const StringDesc *strings;   // device
+    const TileRef *tiles;        // device
+    int n_tiles;
+    int grid;                    // blocks launched (grid-stride over tiles)
+    int precision;               // 0 float, 1 double
+    int ncomp;                   // 1 or 2 (uniform over the strings of a context)
+    cudaStream_t stream;
+};
+
+struct StepFlags {
+    int xin, xout;     // x buffers read / written by the gradient pass
+    int gcur, gprev;   // gradient slots
+    int din, dout;     // direction buffers read / written by the direction pass
+    int use_cg, maxwell, thin_film_any;
+    int poly_compat, ls_exact;
+};
+
+// Pass 1: x <- x + alpha_pend d (into x[xout]); g = dF/dx; |g|^2, g.(g - g_prev);
+// the last tile of each image sets beta.
+cudaError_t launch_grad(const Launch &L, const Scalars &sc, const StepFlags &f);
+// Pass 2: d <- -g + beta d (into d[dout]); quartic of F(x + a d); the last
+// tile of each image runs the line search and sets alpha, alpha_pend.
+cudaError_t launch_dir_poly(const Launch &L, const Scalars &sc, const StepFlags &f);
+// x[xbuf] += alpha_pend d[dbuf]; alpha_pend = 0.
+cudaError_t launch_apply_update(const Launch &L, const Scalars &sc, const StringDesc *host_strings, int n_strings,
+                                int xbuf, int dbuf);
+// Energy of x[xbuf] into sc.fenergy_out (per image).
+cudaError_t launch_energy(const Launch &L, const Scalars &sc, int xbuf, double *out);
+// Gradient of x[xbuf] into the three arrays of `out` (single string).
+struct FieldPtrs { void *p[3]; };
+cudaError_t launch_gradient_only(const Launch &L, int xbuf, FieldPtrs out, int maxwell);
+// B, J of x[xbuf] written to per-string arrays (b: F*M reals, j: F*M pairs).
+cudaError_t launch_jb(const Launch &L, const Scalars &sc, int xbuf, void *const *b, void *const (*j)[2]);
+
+// Arc length of one string over nf per-image arrays of `width` reals per site
+// (reals of the context precision).  Result: s[0..F) (device doubles), using
+// part (>= tiles_per_image * F doubles) as scratch.
+cudaError_t launch_arc_length(int precision, const void *const *fields, const int *width, int nf, long sites, int F,
+                              double *part, double *s, cudaStream_t st);
+// Plan of a redistribution from F to F_new images on the arc length s:
+// segment k and weight w per output image; for cubic also h and the
+// factorised spline matrix (dl, d, du, du2, ipiv) -- all in `plan`.
+struct RedistPlan {
+    int *k;          // [F_new]
+    double *w;       // [F_new]
+    double *h;       // [F + 1]
+    double *dl, *d, *du, *du2;   // [F]
+    int *ipiv;       // [F]
+    int *status;
+};
+cudaError_t launch_redist_plan(const double *s, int F, int F_new, int cubic, int spline, const RedistPlan &p,
+                               cudaStream_t st);
+// Linear resample of `pairs` interleaved pairs per image (precision real).
+cudaError_t launch_redist_linear(int precision, const void *f, void *fnew, long pairs, int F_new, const RedistPlan &p,
+                                 cudaStream_t st);
+// Cubic resample; `sigma` is scratch of 2 * pairs * F reals of the precision.
+cudaError_t launch_redist_cubic(int precision, const void *f, void *fnew, void *sigma, long pairs, int F, int F_new,
+                                int spline, const RedistPlan &p, cudaStream_t st);
+// Precision conversion of n reals.
+cudaError_t launch_convert(const void *src, int src_prec, void *dst, int dst_prec, long n, cudaStream_t st);
+
+}  // namespace mepgl
