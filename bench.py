@@ -1,0 +1,325 @@
+#!/usr/bin/env python3
+"""Benchmark: site-image gradient evaluations per second of the NLCG step.
+
+Workload (the mixed-precision configuration): two-component GL, a1=-1 b1=1,
+a2=-0.6 b2=1, m1=(1,1), m2=(1,2), eta=-0.5, gamma=0.2, H=0.9, 256x256 sites
+at dx=0.4, 64 images, seeded synthetic initial string (Meissner to one
+fractional vortex per component, noise 1e-3).  One step = one nonlinear
+conjugate-gradient iteration of the whole string (every image: update,
+gradient, Polak-Ribiere direction, line quartic, line search), i.e.
+256*256*64 site-image gradient evaluations.  The string (~0.9 GB of state
+streams per step) is larger than L2, so no flush is needed between steps.
+
+``value`` is the FP32 bulk-relaxation throughput (fields in FP32, every
+reduction and the beta / step scalars in FP64); the FP64 polish throughput
+is reported beside it.  ``e2e`` runs the same steps through the C ABI with
+pinned host buffers: each e2e step is one outer iteration of the
+reference's loop() in mode S (state copied in, 10 NLCG steps, per-image
+energies copied out).  ``--impl reference`` times the CPU implementation of
+the same step (the C restatement in oracle/, all host threads) on the same
+workload.
+
+Multi-GPU: the path does not shard within a string; ``--gpus N`` runs N
+independent replicas (one string per GPU) and reports the aggregate.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "site·image grad evals/s; time-to-barrier @1e-6 rel, FP32+FP64 vs FP64"
+UNIT = "site·image/s"
+WORKLOAD = "two-component GL 256x256 dx=0.4, 64 images (mixed-precision config)"
+RELAX = 10
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu: int):
+        self.gpu = gpu
+        self.lines = []
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            time.sleep(0.25)
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def dist_env():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def cpu_oracle_step_rate(prob, st, images: int, steps: int, dtype, budget_s: float = 12.0):
+    """Time the C oracle (OpenMP over images) on a sample of `images` images."""
+    import numpy as np
+    from oracle import cref
+    sub = st.__class__(a=st.a[:images], psi_1=st.psi_1[:images],
+                       psi_2=None if st.psi_2 is None else st.psi_2[:images])
+    orc = cref.Oracle(prob, dtype)
+    sv = orc.solver(sub, ls_mode=cref.LS_COMPAT, poly_compat=False)
+    sv.nlcg_steps(1)                     # warm-up (page-in, thread pool)
+    done, t0 = 0, time.perf_counter()
+    while done < steps or (time.perf_counter() - t0) < 1.0:
+        sv.nlcg_steps(1)
+        done += 1
+        if time.perf_counter() - t0 > budget_s:
+            break
+    dt = time.perf_counter() - t0
+    units = done * images * prob.nx * prob.ny
+    return units / dt, dict(steps=done, images=images, seconds=dt, threads=cref.threads())
+
+
+def run_reference(args):
+    """--impl reference: the CPU implementation (C oracle, all host threads)."""
+    world, rank, _ = dist_env()
+    if rank != 0:
+        return 0
+    import numpy as np
+    from mepgl_gb300 import workloads
+    from oracle import cref
+    prob, st = workloads.config2()
+    sample_images = 16
+    orc = cref.Oracle(prob, np.float32)
+    sub = st.__class__(a=st.a[:sample_images], psi_1=st.psi_1[:sample_images], psi_2=st.psi_2[:sample_images])
+    sv = orc.solver(sub, ls_mode=cref.LS_COMPAT, poly_compat=False)
+    for _ in range(args.warmup):
+        sv.nlcg_steps(1)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        sv.nlcg_steps(1)
+    dt = time.perf_counter() - t0
+    units = args.steps * sample_images * prob.nx * prob.ny
+    value = units / dt
+    sample = (f"{sample_images} of 64 images of the workload per step, {args.steps} steps, "
+              f"C oracle (oracle/gl_oracle.c) in FP32 with FP64 reductions, OpenMP over images")
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * dt / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "sites": prob.nx * prob.ny, "images": 64, "components": 2,
+                   "cache": "inputs larger than L2"},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cref.threads(), "kind": "port", "sample": sample},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_ours(args):
+    import numpy as np
+    import torch
+
+    world, rank, local = dist_env()
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    torch.cuda.set_device(local)
+    from mepgl_gb300 import native, workloads
+
+    prob, st = workloads.config2()
+    F = st.n_images
+    sites = prob.nx * prob.ny
+    units_per_step = sites * F
+    stream = torch.cuda.Stream()          # a real stream: graph capture and events share it
+    torch.cuda.set_stream(stream)
+    ctx = native.StringContext(prob, F, "fp32", stream=stream.cuda_stream, line_polynomial=native.POLY_EXACT)
+    ctx.set_state(st)
+
+    def barrier():
+        torch.cuda.synchronize()
+        if world > 1:
+            torch.distributed.barrier()
+
+    def maxed(x):
+        if world == 1:
+            return x
+        t = torch.tensor([x], dtype=torch.float64, device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        return float(t.item())
+
+    # ---- device-resident timed region (FP32 bulk relaxation) ----------------
+    ctx.nlcg_steps(max(args.warmup, 3))
+    barrier()
+    l0 = ctx.info()["kernel_launches"]
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        barrier()
+        ev0.record(stream)
+        ctx.nlcg_steps(args.steps)
+        ev1.record(stream)
+        barrier()
+    ms = maxed(ev0.elapsed_time(ev1))
+    launches = ctx.info()["kernel_launches"] - l0
+    value = world * units_per_step * args.steps / (ms / 1e3)
+    fe = ctx.image_scalars()["fenergy"]
+    assert np.all(np.isfinite(fe)), "non-finite energies"
+
+    # ---- per-pass timing on the launching stream (roofline) --------------------
+    ms_grad, ms_dir = ctx.profile_passes(10)
+    S = (2 + 2 * 2) * 4                    # bytes of state per site-image (A, psi_1, psi_2 in FP32)
+    bytes_grad = (5 * S + 2) * units_per_step  # read x, d, g_prev; write x, g; masks
+    bytes_dir = (4 * S + 2) * units_per_step   # read x, g, d; write d; masks
+    peak, peak_kind = peaks()
+    kern = {"k_grad": {"ms": ms_grad, "bytes": bytes_grad, "gbs": bytes_grad / ms_grad / 1e6},
+            "k_dir_poly": {"ms": ms_dir, "bytes": bytes_dir, "gbs": bytes_dir / ms_dir / 1e6}}
+    dom = max(kern, key=lambda k: kern[k]["ms"])
+    traffic = None
+    tfile = os.path.join(ROOT, "profiles", "traffic_config2_fp32.json")
+    if os.path.exists(tfile):
+        with open(tfile) as f:
+            traffic = json.load(f).get(dom)
+    roofline = {"bound": "hbm", "achieved": kern[dom]["gbs"], "peak": peak, "unit": "GB/s",
+                "frac": kern[dom]["gbs"] / peak, "traffic": traffic, "kernel": dom,
+                "peak_source": f"{peak_kind} hbm_gbs",
+                "step_gbs": (bytes_grad + bytes_dir) / (ms_grad + ms_dir) / 1e6}
+
+    # ---- FP64 polish throughput (same string) ---------------------------------
+    ctx64 = native.StringContext(prob, F, "fp64", stream=stream.cuda_stream, line_polynomial=native.POLY_EXACT)
+    ctx64.set_state(st)
+    ctx64.nlcg_steps(3)
+    k64 = max(2, args.steps // 4)
+    barrier()
+    ev0.record(stream)
+    ctx64.nlcg_steps(k64)
+    ev1.record(stream)
+    barrier()
+    ms64 = maxed(ev0.elapsed_time(ev1))
+    g64, d64 = ctx64.profile_passes(3)
+    fp64 = {"value": world * units_per_step * k64 / (ms64 / 1e3), "ms_per_step": ms64 / k64, "steps": k64,
+            "ms_grad": g64, "ms_dir_poly": d64}
+    ctx64.close()
+
+    # ---- end to end through the C ABI with pinned host buffers -----------------
+    shape = (F, prob.ny, prob.nx, 2)
+    host = [torch.from_numpy(np.ascontiguousarray(x, np.float32)).pin_memory()
+            for x in (st.a, st.psi_1, st.psi_2)]
+    fe_host = torch.zeros(F, dtype=torch.float64).pin_memory()
+    L = ctx.L
+    import ctypes as C
+
+    def e2e_step():
+        ctx._check(L.mepgl_set_state(ctx.h, C.c_void_p(host[0].data_ptr()), C.c_void_p(host[1].data_ptr()),
+                                     C.c_void_p(host[2].data_ptr()), native.HOST))
+        ctx.nlcg_steps(RELAX)
+        ctx._check(L.mepgl_image_scalars(ctx.h, C.c_void_p(fe_host.data_ptr()), None, None))
+
+    e2e_step()
+    e2e_iters = max(2, args.steps // RELAX)
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(e2e_iters):
+        e2e_step()
+    barrier()
+    e2e_s = maxed(time.perf_counter() - t0)
+    h2d = sum(h.numel() * h.element_size() for h in host)
+    e2e = {"value": world * units_per_step * RELAX * e2e_iters / e2e_s, "unit": UNIT,
+           "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": F * 8,
+           "step": f"set_state from pinned host + {RELAX} NLCG steps + per-image energies to host"}
+
+    # ---- CPU baseline (rank 0, N = 1 only) ------------------------------------
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        rate, info = cpu_oracle_step_rate(prob, st, images=16, steps=2, dtype=np.float32)
+        cpu = {"value": rate, "unit": UNIT, "cores": info["threads"], "kind": "port",
+               "sample": f"{info['steps']} NLCG steps on {info['images']} of 64 images of the workload "
+                         f"({info['seconds']:.1f} s), C oracle in FP32, OpenMP over images"}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "sites": sites, "images": F, "components": 2,
+                       "line_polynomial": "exact", "line_search": "compat scan",
+                       "cache": "inputs larger than L2 (no flush)", "parallelism": f"replicas x{world}"},
+            "e2e": e2e, "gpu_launches": launches, "roofline": roofline, "kernels": kern, "fp64": fp64,
+            "cpu_baseline": cpu, "clocks": clk.summary(),
+        }
+        print(json.dumps(line), flush=True)
+    ctx.close()
+    if world > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser(description=__doc__.splitlines()[0])
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=40)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", choices=("ours", "reference"), default="ours")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    args = ap.parse_args(argv)
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -15,7 +15,8 @@ import sys
 PKG = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(PKG)
 CSRC = os.path.join(PKG, "csrc")
-LIB_DIR = os.path.join(PKG, "_lib")
+# MEPGL_LIB_DIR / MEPGL_NVCC_FLAGS: build a variant elsewhere with extra flags
+LIB_DIR = os.environ.get("MEPGL_LIB_DIR", os.path.join(PKG, "_lib"))
 LIB = os.path.join(LIB_DIR, "libmepgl_gb300.so")
 CLI = os.path.join(LIB_DIR, "mepgl")
 
@@ -56,7 +57,8 @@ def build(force: bool = False, verbose: bool = False, ptxas_info: bool = False) 
         o = os.path.join(LIB_DIR, src.replace(".cu", ".o"))
         objs.append(o)
         if force or ptxas_info or _stale(o, [s] + hdrs):
-            cmd = [nvcc()] + ARCH + NVCC_FLAGS + (["-Xptxas", "-v"] if ptxas_info else []) + ["-c", s, "-o", o]
+            extra = os.environ.get("MEPGL_NVCC_FLAGS", "").split()
+            cmd = [nvcc()] + ARCH + NVCC_FLAGS + extra + (["-Xptxas", "-v"] if ptxas_info else []) + ["-c", s, "-o", o]
             jobs.append(cmd)
     with cf.ThreadPoolExecutor(max_workers=max(1, len(jobs))) as ex:
         for out in ex.map(_run, jobs):

@@ -46,7 +46,7 @@ struct mepgl_ctx {
     bool own_stream = false;
     std::vector<StringHost> strings;
     std::vector<StringDesc> hdesc;
-    StringDesc *ddesc = nullptr;
+    Batch batch{};                // descriptors passed to every lattice kernel
     TileRef *dtiles = nullptr;
     int n_tiles = 0, total_images = 0;
     std::vector<int> string_tile0, string_ntiles;
@@ -179,33 +179,47 @@ void fill_desc(mepgl_ctx *c, int si, int img_base, int tile_base)
     D.F = s.F;
     D.ncomp = c->ncomp;
     D.tiles_x = (s.nx + TX - 1) / TX;
-    D.tiles_y = (s.ny + TY - 1) / TY;
+    D.tiles_y = (s.ny + tile_rows(c->precision) - 1) / tile_rows(c->precision);
     D.img_base = img_base;
     D.tile_base = tile_base;
     D.thin_film = c->thin_film;
     D.per_site = s.uniform ? 0 : 1;
-    D.dx = s.dx;
-    D.inv_dx = 1.0 / s.dx;
-    D.q[0] = s.q[0];
-    D.q[1] = s.q[1];
-    D.eta = s.eta;
-    D.gamma = s.gamma;
-    D.delta = s.delta;
+    // uniform parameters, formed in double and rounded once per precision
+    Uniform<double> &U = D.ud;
     for (int k = 0; k < 2; ++k) {
         const int o = 4 * k;
-        D.a[k] = s.params[o][0];
-        D.b[k] = s.params[o + 1][0];
-        D.mxx[k] = s.params[o + 2][0];
-        D.myy[k] = s.params[o + 3][0];
-        D.hmx[k] = 0.5 / D.mxx[k];
-        D.hmy[k] = 0.5 / D.myy[k];
-        D.aob[k] = D.a[k] / D.b[k];
+        U.a[k] = s.params[o][0];
+        U.b[k] = s.params[o + 1][0];
+        U.hmx[k] = 0.5 / s.params[o + 2][0];
+        U.hmy[k] = 0.5 / s.params[o + 3][0];
+        U.aob[k] = U.a[k] / U.b[k];
+        U.q[k] = s.q[k];
         D.pa[k] = s.dparams[o];
         D.pb[k] = s.dparams[o + 1];
         D.pmxx[k] = s.dparams[o + 2];
         D.pmyy[k] = s.dparams[o + 3];
     }
-    D.h = s.params[8][0];
+    U.eta = s.eta;
+    U.gamma = s.gamma;
+    U.delta = s.delta;
+    U.h = s.params[8][0];
+    U.idx = 1.0 / s.dx;
+    U.dx2 = s.dx * s.dx;
+    Uniform<float> &Uf = D.uf;
+    for (int k = 0; k < 2; ++k) {
+        Uf.a[k] = (float)U.a[k];
+        Uf.b[k] = (float)U.b[k];
+        Uf.hmx[k] = (float)U.hmx[k];
+        Uf.hmy[k] = (float)U.hmy[k];
+        Uf.aob[k] = (float)U.aob[k];
+        Uf.q[k] = (float)U.q[k];
+    }
+    Uf.eta = (float)U.eta;
+    Uf.gamma = (float)U.gamma;
+    Uf.delta = (float)U.delta;
+    Uf.h = (float)U.h;
+    Uf.idx = (float)U.idx;
+    Uf.dx2 = (float)s.dx * (float)s.dx;
     D.ph = s.dparams[8];
     D.mask = s.dmask;
     for (int b = 0; b < 2; ++b)
@@ -219,13 +233,12 @@ void fill_desc(mepgl_ctx *c, int si, int img_base, int tile_base)
 void free_scalars(mepgl_ctx *c)
 {
     Scalars &S = c->sc;
-    cudaFree(S.gn[0]); cudaFree(S.gn[1]); cudaFree(S.gdg); cudaFree(S.beta); cudaFree(S.alpha);
+    cudaFree(S.gn0); cudaFree(S.gn1); cudaFree(S.gdg); cudaFree(S.beta); cudaFree(S.alpha);
     cudaFree(S.alpha_pend); cudaFree(S.fenergy); cudaFree(S.poly); cudaFree(S.part); cudaFree(S.ticket);
     cudaFree(S.xtab_f); cudaFree(S.xtab_d); cudaFree(S.status);
     memset(&S, 0, sizeof(S));
     cudaFree(c->dscratch); c->dscratch = nullptr;
     cudaFree(c->ds); cudaFree(c->ds_jb); c->ds = c->ds_jb = nullptr;
-    cudaFree(c->ddesc); c->ddesc = nullptr;
     cudaFree(c->dtiles); c->dtiles = nullptr;
 }
 
@@ -258,13 +271,16 @@ mepgl_status build_layout(mepgl_ctx *c)
     }
     c->n_tiles = (int)tiles.size();
     c->total_images = img;
-    CK(c, cudaMalloc(&c->ddesc, sizeof(StringDesc) * c->hdesc.size()));
-    CK(c, cudaMemcpy(c->ddesc, c->hdesc.data(), sizeof(StringDesc) * c->hdesc.size(), cudaMemcpyHostToDevice));
+    if (c->hdesc.size() > (size_t)MAX_STRINGS)
+        return fail(c, MEPGL_ERR_UNSUPPORTED, "too many strings in one context");
+    memset(&c->batch, 0, sizeof(c->batch));
+    c->batch.n = (int)c->hdesc.size();
+    for (size_t si = 0; si < c->hdesc.size(); ++si) c->batch.s[si] = c->hdesc[si];
     CK(c, cudaMalloc(&c->dtiles, sizeof(TileRef) * tiles.size()));
     CK(c, cudaMemcpy(c->dtiles, tiles.data(), sizeof(TileRef) * tiles.size(), cudaMemcpyHostToDevice));
     Scalars &S = c->sc;
     const size_t I = (size_t)img;
-    for (double **p : {&S.gn[0], &S.gn[1], &S.gdg, &S.beta, &S.alpha, &S.alpha_pend, &S.fenergy})
+    for (double **p : {&S.gn0, &S.gn1, &S.gdg, &S.beta, &S.alpha, &S.alpha_pend, &S.fenergy})
         CK(c, cudaMalloc(p, I * sizeof(double)));
     CK(c, cudaMalloc(&S.poly, 4 * I * sizeof(double)));
     CK(c, cudaMalloc(&S.part, (size_t)c->n_tiles * 8 * sizeof(double) + 4096 * sizeof(double)));
@@ -312,8 +328,8 @@ mepgl_status reset_history(mepgl_ctx *c)
             }
     }
     std::vector<double> inf(c->total_images, INF);
-    CK(c, cudaMemcpyAsync(c->sc.gn[0], inf.data(), inf.size() * 8, cudaMemcpyHostToDevice, c->stream));
-    CK(c, cudaMemcpyAsync(c->sc.gn[1], inf.data(), inf.size() * 8, cudaMemcpyHostToDevice, c->stream));
+    CK(c, cudaMemcpyAsync(c->sc.gn0, inf.data(), inf.size() * 8, cudaMemcpyHostToDevice, c->stream));
+    CK(c, cudaMemcpyAsync(c->sc.gn1, inf.data(), inf.size() * 8, cudaMemcpyHostToDevice, c->stream));
     for (double *p : {c->sc.alpha, c->sc.alpha_pend, c->sc.fenergy, c->sc.beta, c->sc.gdg})
         CK(c, cudaMemsetAsync(p, 0, c->total_images * 8, c->stream));
     CK(c, cudaMemsetAsync(c->sc.poly, 0, c->total_images * 32, c->stream));
@@ -325,7 +341,7 @@ mepgl_status reset_history(mepgl_ctx *c)
 Launch make_launch(mepgl_ctx *c, int first_tile = 0, int ntiles = -1)
 {
     Launch L;
-    L.strings = c->ddesc;
+    L.batch = &c->batch;
     L.tiles = c->dtiles + first_tile;
     L.n_tiles = ntiles < 0 ? c->n_tiles : ntiles;
     L.grid = L.n_tiles;
@@ -555,8 +571,8 @@ mepgl_status reset_cg(mepgl_ctx *c, int first, int last)
         return fail(c, MEPGL_ERR_INVALID_ARG, "reset_cg: image range out of bounds");
     if (first == last) return MEPGL_OK;
     std::vector<double> inf(last - first, INF);
-    CK(c, cudaMemcpyAsync(c->sc.gn[0] + first, inf.data(), inf.size() * 8, cudaMemcpyHostToDevice, c->stream));
-    CK(c, cudaMemcpyAsync(c->sc.gn[1] + first, inf.data(), inf.size() * 8, cudaMemcpyHostToDevice, c->stream));
+    CK(c, cudaMemcpyAsync(c->sc.gn0 + first, inf.data(), inf.size() * 8, cudaMemcpyHostToDevice, c->stream));
+    CK(c, cudaMemcpyAsync(c->sc.gn1 + first, inf.data(), inf.size() * 8, cudaMemcpyHostToDevice, c->stream));
     CK(c, cudaStreamSynchronize(c->stream));
     return MEPGL_OK;
 }
@@ -587,8 +603,10 @@ mepgl_status mepgl_create(const mepgl_problem *p, const mepgl_options *opt, void
     *out = nullptr;
     if (p->nx < 2 || p->ny < 2 || p->n_images < 1 || !(p->dx > 0))
         return fail(nullptr, MEPGL_ERR_INVALID_ARG, "mepgl_create: need nx, ny >= 2, n_images >= 1, dx > 0");
-    if (p->nx > 32767 * TX || p->ny > 32767 * TY)
+    if (p->nx > 32767 * TX || p->ny > 32767 * 8 || (long)p->nx * p->ny >= (1L << 31))
         return fail(nullptr, MEPGL_ERR_INVALID_ARG, "mepgl_create: lattice too large");
+    if (upload_mask_tables() != cudaSuccess)
+        return fail(nullptr, MEPGL_ERR_CUDA, "mepgl_create: cannot upload the neighbour-code tables");
     if (p->precision != MEPGL_FP32 && p->precision != MEPGL_FP64)
         return fail(nullptr, MEPGL_ERR_INVALID_ARG, "mepgl_create: precision must be MEPGL_FP32 or MEPGL_FP64");
     const double *arr[9] = {p->a_1, p->b_1, p->m_xx_1, p->m_yy_1, p->a_2, p->b_2, p->m_xx_2, p->m_yy_2, p->h};
@@ -753,7 +771,7 @@ mepgl_status mepgl_image_scalars(mepgl_ctx *c, double *fenergy, double *g_norm2,
     const int F = c->strings[0].F;
     if (fenergy) CK(c, cudaMemcpyAsync(fenergy, c->sc.fenergy, F * 8, cudaMemcpyDeviceToHost, c->stream));
     // loop()'s g_norm2 is the slot nlcgSteps writes on even substeps
-    if (g_norm2) CK(c, cudaMemcpyAsync(g_norm2, c->sc.gn[0], F * 8, cudaMemcpyDeviceToHost, c->stream));
+    if (g_norm2) CK(c, cudaMemcpyAsync(g_norm2, c->sc.gn0, F * 8, cudaMemcpyDeviceToHost, c->stream));
     if (alpha) CK(c, cudaMemcpyAsync(alpha, c->sc.alpha, F * 8, cudaMemcpyDeviceToHost, c->stream));
     CK(c, cudaStreamSynchronize(c->stream));
     return MEPGL_OK;

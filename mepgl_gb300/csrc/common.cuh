@@ -2,11 +2,16 @@
 //
 // Work decomposition.  Every pass over the string is a list of tiles; a
 // tile is TX x TY sites of one image of one string.  Kernels walk the tile
-// list with a grid-stride loop, so one launch covers every image of every
-// string in the context (strings may differ in size and image count).
+// list with a grid-stride loop, so one launch covers every image of up to
+// MAX_STRINGS strings (strings may differ in size and image count).
 // Per-image reductions are deterministic: each tile writes one partial per
 // quantity, and the last tile of an image to finish (atomic ticket per
 // image) sums that image's partials in a fixed order.
+//
+// Precision.  Fields are float or double (T).  Sums are formed in T inside
+// a warp (a fixed pairwise shuffle tree), then in double across warps,
+// tiles and images.  GB300's FP64 pipe is a small fraction of its FP32
+// rate, so FP32 kernels avoid any per-site double arithmetic or conversion.
 #pragma once
 
 #include <cstdint>
@@ -16,11 +21,19 @@ namespace mepgl {
 
 constexpr int TX = 32;        // tile width: one warp per tile row
 constexpr int NT = 256;       // threads per block for the lattice kernels
+constexpr int MAX_STRINGS = 16;   // strings per launch (descriptors travel as a kernel parameter)
 
 template <class T> struct Vec2;
 template <> struct Vec2<float> { using type = float2; };
 template <> struct Vec2<double> { using type = double2; };
 template <class T> using vec2_t = typename Vec2<T>::type;
+
+// Uniform GL parameters in one precision (hm* = 0.5 / m, aob = a / b).
+template <class T>
+struct Uniform {
+    T a[2], b[2], hmx[2], hmy[2], aob[2], q[2];
+    T eta, gamma, delta, h, idx, dx2;
+};
 
 // One string (one lattice, F images) as seen by the kernels.  Field buffers
 // hold three arrays each (A, psi_1, psi_2) of F*nx*ny pairs; psi_2 is null
@@ -33,17 +46,26 @@ struct StringDesc {
     int tile_base;            // first global tile index of this string
     int thin_film;
     int per_site;             // 1: parameters read from the arrays below
-    double dx, inv_dx;
-    double q[2], eta, gamma, delta;
-    double a[2], b[2], mxx[2], myy[2], h;          // uniform values
-    double hmx[2], hmy[2], aob[2];                 // 0.5/m_xx, 0.5/m_yy, a/b (uniform)
+    Uniform<float> uf;
+    Uniform<double> ud;
     const void *pa[2], *pb[2], *pmxx[2], *pmyy[2], *ph;  // per-site (type T)
     const uint16_t *mask;     // per site: comp code | sc code << 8
     void *x[2][3], *g[2][3], *d[2][3];
+
+    template <class T> __host__ __device__ const Uniform<T> &u() const;
+};
+template <> __host__ __device__ inline const Uniform<float> &StringDesc::u<float>() const { return uf; }
+template <> __host__ __device__ inline const Uniform<double> &StringDesc::u<double>() const { return ud; }
+
+// Descriptors of the strings covered by one launch; passed by value as a
+// __grid_constant__ kernel parameter, i.e. read through the constant cache.
+struct Batch {
+    int n;
+    StringDesc s[MAX_STRINGS];
 };
 
 struct TileRef {
-    int16_t s;        // string
+    int16_t s;        // string within the batch
     int16_t ty;       // tile row
     int16_t tx;       // tile column
     int16_t pad;
@@ -52,7 +74,7 @@ struct TileRef {
 
 // Per-image scalars of the whole context (index = img_base + n).
 struct Scalars {
-    double *gn[2];        // |g|^2, two slots (nlcgSteps' g_norm2 / g_norm2_old)
+    double *gn0, *gn1;    // |g|^2, two slots (nlcgSteps' g_norm2 / g_norm2_old)
     double *gdg;          // g . (g - g_prev)
     double *beta;         // Polak-Ribiere coefficient of the last step
     double *alpha;        // step of the last line search (reported)
@@ -67,18 +89,22 @@ struct Scalars {
 
 __device__ __forceinline__ unsigned bit(unsigned c, int n) { return (c >> n) & 1u; }
 
-// Block-wide sum of NV doubles in a fixed order; result valid in thread 0.
-template <int NV>
-__device__ __forceinline__ void block_sum(double (&v)[NV], double *smem /* NT/32*NV */)
+// Block-wide sum of NV values; a pairwise tree in T inside each warp, then
+// double across warps.  Result (double) valid in thread 0.
+template <int NV, class T>
+__device__ __forceinline__ void block_sum(const T (&v)[NV], double (&out)[NV], double *smem /* NT/32*NV */)
 {
+    T w[NV];
 #pragma unroll
-    for (int k = 0; k < NV; ++k)
+    for (int k = 0; k < NV; ++k) {
+        w[k] = v[k];
 #pragma unroll
-        for (int o = 16; o > 0; o >>= 1) v[k] += __shfl_down_sync(0xffffffffu, v[k], o);
-    const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+        for (int o = 16; o > 0; o >>= 1) w[k] += __shfl_down_sync(0xffffffffu, w[k], o);
+    }
+    const int wi = threadIdx.x >> 5, l = threadIdx.x & 31;
     if (l == 0)
 #pragma unroll
-        for (int k = 0; k < NV; ++k) smem[w * NV + k] = v[k];
+        for (int k = 0; k < NV; ++k) smem[wi * NV + k] = (double)w[k];
     __syncthreads();
     if (threadIdx.x < 32) {
 #pragma unroll
@@ -86,7 +112,7 @@ __device__ __forceinline__ void block_sum(double (&v)[NV], double *smem /* NT/32
             double t = (l < NT / 32) ? smem[l * NV + k] : 0.0;
 #pragma unroll
             for (int o = 16; o > 0; o >>= 1) t += __shfl_down_sync(0xffffffffu, t, o);
-            v[k] = t;
+            out[k] = t;
         }
     }
     __syncthreads();
@@ -95,15 +121,16 @@ __device__ __forceinline__ void block_sum(double (&v)[NV], double *smem /* NT/32
 // Write this tile's NV partials; return true (in every thread) if this
 // block is the last of its image, in which case `tot` holds the image sums
 // (in thread 0) computed over the image's partials in index order.
-template <int NV>
-__device__ __forceinline__ bool finish_image(double (&v)[NV], double *smem, const Scalars &sc, int tile, int first_tile,
-                             int tiles_per_image, int img, double (&tot)[NV])
+template <int NV, class T>
+__device__ __forceinline__ bool finish_image(const T (&v)[NV], double *smem, const Scalars &sc, int tile,
+                                             int first_tile, int tiles_per_image, int img, double (&tot)[NV])
 {
     __shared__ bool last;
-    block_sum<NV>(v, smem);
+    double mine[NV];
+    block_sum<NV>(v, mine, smem);
     if (threadIdx.x == 0) {
 #pragma unroll
-        for (int k = 0; k < NV; ++k) sc.part[(size_t)tile * 8 + k] = v[k];
+        for (int k = 0; k < NV; ++k) sc.part[(size_t)tile * 8 + k] = mine[k];
         __threadfence();
         const unsigned prev = atomicAdd(&sc.ticket[img], 1u);
         last = (prev == (unsigned)tiles_per_image - 1);
@@ -111,14 +138,15 @@ __device__ __forceinline__ bool finish_image(double (&v)[NV], double *smem, cons
     __syncthreads();
     if (!last) return false;
     __threadfence();
+    double acc[NV];
 #pragma unroll
-    for (int k = 0; k < NV; ++k) tot[k] = 0;
+    for (int k = 0; k < NV; ++k) acc[k] = 0;
     for (int t = threadIdx.x; t < tiles_per_image; t += NT) {
         const double *p = sc.part + (size_t)(first_tile + t) * 8;
 #pragma unroll
-        for (int k = 0; k < NV; ++k) tot[k] += __ldcg(p + k);
+        for (int k = 0; k < NV; ++k) acc[k] += __ldcg(p + k);
     }
-    block_sum<NV>(tot, smem);
+    block_sum<NV>(acc, tot, smem);
     if (threadIdx.x == 0) sc.ticket[img] = 0;
     return true;
 }

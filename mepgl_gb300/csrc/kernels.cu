@@ -16,82 +16,124 @@
 // and writes x, g, d: 9 state-sized streams instead of the reference's ~20.
 // x and d are ping-ponged because neighbouring tiles read them as halo while
 // they are being rewritten.
+//
+// Tiles are 32 x TileRows<T> sites (16 rows in FP32, 8 in FP64) staged with
+// a one-site halo in shared memory; each thread computes TileRows/8 sites of
+// one column.  Addresses inside an image are 32-bit offsets from per-tile
+// base pointers.
 #include "kernels.cuh"
 #include "site_ops.cuh"
 
 namespace mepgl {
 
+// Tuning knobs (compile time): tile rows per precision and the minimum
+// resident blocks per SM requested from ptxas for the two NLCG passes.
+#ifndef MEPGL_ROWS_F32
+#define MEPGL_ROWS_F32 16
+#endif
+#ifndef MEPGL_ROWS_F64
+#define MEPGL_ROWS_F64 8
+#endif
+#ifndef MEPGL_MINB_GRAD
+#define MEPGL_MINB_GRAD 4
+#endif
+#ifndef MEPGL_MINB_DIR
+#define MEPGL_MINB_DIR 3
+#endif
+
+template <class T> struct TileRows { static constexpr int v = sizeof(T) == 4 ? MEPGL_ROWS_F32 : MEPGL_ROWS_F64; };
+
+int tile_rows(int precision) { return precision == 1 ? TileRows<double>::v : TileRows<float>::v; }
+
+cudaError_t upload_mask_tables()
+{
+    static MaskTable<float> f;
+    static MaskTable<double> d;
+    build_mask_table(f);
+    build_mask_table(d);
+    cudaError_t e = cudaMemcpyToSymbol(c_mask_f, &f, sizeof(f));
+    if (e == cudaSuccess) e = cudaMemcpyToSymbol(c_mask_d, &d, sizeof(d));
+    return e;
+}
+
 namespace {
 
-// ------------------------------------------------------------------ staging
+// Base pointers of one image's fields for one tile.
 template <class T, int NC>
-__device__ __forceinline__ void stage_state(Tile<T, NC, TY> &t, const StringDesc &S, int n, int i0, int j0,
-                                            int xin, int xout, int dbuf, T alpha, bool write_x)
+struct ImagePtrs {
+    const vec2_t<T> *in[1 + NC];
+    const vec2_t<T> *aux[1 + NC];
+    vec2_t<T> *out[1 + NC];
+};
+
+// ------------------------------------------------------------------ staging
+// Rows of the (TYT+2) x (TX+2) halo tile are spread over the warps; a warp
+// loads one row (32 columns, lanes 0 and 1 also the last two columns).
+// mode 0: x = in;  mode 1: x = in + alpha * aux (and interior x -> out);
+// mode 2: x = -aux + beta * in, i.e. the new direction (interior -> out).
+template <class T, int NC, int TYT, int MODE>
+__device__ __forceinline__ void stage(Tile<T, NC, TYT> &t, const StringDesc &S, const ImagePtrs<T, NC> &ip, int i0,
+                                      int j0, T coef, bool write_out, bool masks)
 {
     using V = vec2_t<T>;
-    const long M = (long)S.nx * S.ny, off = (long)n * M;
-    for (int q = threadIdx.x; q < (TX + 2) * (TY + 2); q += NT) {
-        const int hx = q % (TX + 2), hy = q / (TX + 2);
-        const int gi = i0 + hx - 1, gj = j0 + hy - 1;
-        V f[1 + NC];
-        uint16_t m = 0;
-        if (gi >= 0 && gi < S.nx && gj >= 0 && gj < S.ny) {
-            const long s = gi + (long)S.nx * gj, k = off + s;
-            m = S.mask[s];
-#pragma unroll
-            for (int c = 0; c < 1 + NC; ++c) f[c] = static_cast<const V *>(S.x[xin][c])[k];
-            if (alpha != (T)0) {
+    const int lane = threadIdx.x & 31, wrp = threadIdx.x >> 5;
+    for (int hy = wrp; hy < TYT + 2; hy += NT / 32) {
+        const int gj = j0 + hy - 1;
+        const bool rowin = gj >= 0 && gj < S.ny;
+        for (int hx = lane; hx < TX + 2; hx += 32) {
+            const int gi = i0 + hx - 1;
+            V f[1 + NC];
+            uint16_t m = 0;
+            if (rowin && gi >= 0 && gi < S.nx) {
+                const int s = gi + S.nx * gj;
+                if (masks) m = S.mask[s];
 #pragma unroll
                 for (int c = 0; c < 1 + NC; ++c) {
-                    const V dd = static_cast<const V *>(S.d[dbuf][c])[k];
-                    f[c].x = f[c].x + alpha * dd.x;
-                    f[c].y = f[c].y + alpha * dd.y;
+                    if (MODE == 2) {
+                        const V gg = ip.aux[c][s], dd = ip.in[c][s];
+                        f[c].x = -gg.x + coef * dd.x;
+                        f[c].y = -gg.y + coef * dd.y;
+                    } else {
+                        f[c] = ip.in[c][s];
+                        if (MODE == 1 && coef != (T)0) {
+                            const V dd = ip.aux[c][s];
+                            f[c].x = f[c].x + coef * dd.x;
+                            f[c].y = f[c].y + coef * dd.y;
+                        }
+                    }
                 }
+                if (write_out && hx >= 1 && hx <= TX && hy >= 1 && hy <= TYT)
+#pragma unroll
+                    for (int c = 0; c < 1 + NC; ++c) ip.out[c][s] = f[c];
+            } else {
+#pragma unroll
+                for (int c = 0; c < 1 + NC; ++c) f[c].x = f[c].y = (T)0;
             }
-            if (write_x && hx >= 1 && hx <= TX && hy >= 1 && hy <= TY)
+            t.A[hy][hx] = f[0];
 #pragma unroll
-                for (int c = 0; c < 1 + NC; ++c) static_cast<V *>(S.x[xout][c])[k] = f[c];
-        } else {
-#pragma unroll
-            for (int c = 0; c < 1 + NC; ++c) f[c].x = f[c].y = (T)0;
+            for (int c = 0; c < NC; ++c) t.P[c][hy][hx] = f[1 + c];
+            if (masks) t.m[hy][hx] = m;
         }
-        t.A[hy][hx] = f[0];
-#pragma unroll
-        for (int c = 0; c < NC; ++c) t.P[c][hy][hx] = f[1 + c];
-        t.m[hy][hx] = m;
     }
 }
 
 template <class T, int NC>
-__device__ __forceinline__ void stage_direction(Tile<T, NC, TY> &t, const StringDesc &S, int n, int i0, int j0,
-                                                int gcur, int din, int dout, T beta)
+__device__ __forceinline__ void image_ptrs(ImagePtrs<T, NC> &ip, void *const *in, void *const *aux, void *const *out,
+                                           size_t off)
 {
-    using V = vec2_t<T>;
-    const long M = (long)S.nx * S.ny, off = (long)n * M;
-    for (int q = threadIdx.x; q < (TX + 2) * (TY + 2); q += NT) {
-        const int hx = q % (TX + 2), hy = q / (TX + 2);
-        const int gi = i0 + hx - 1, gj = j0 + hy - 1;
-        V f[1 + NC];
-        if (gi >= 0 && gi < S.nx && gj >= 0 && gj < S.ny) {
-            const long k = off + gi + (long)S.nx * gj;
 #pragma unroll
-            for (int c = 0; c < 1 + NC; ++c) {
-                const V gg = static_cast<const V *>(S.g[gcur][c])[k];
-                const V dd = static_cast<const V *>(S.d[din][c])[k];
-                f[c].x = -gg.x + beta * dd.x;
-                f[c].y = -gg.y + beta * dd.y;
-            }
-            if (hx >= 1 && hx <= TX && hy >= 1 && hy <= TY)
-#pragma unroll
-                for (int c = 0; c < 1 + NC; ++c) static_cast<V *>(S.d[dout][c])[k] = f[c];
-        } else {
-#pragma unroll
-            for (int c = 0; c < 1 + NC; ++c) f[c].x = f[c].y = (T)0;
-        }
-        t.A[hy][hx] = f[0];
-#pragma unroll
-        for (int c = 0; c < NC; ++c) t.P[c][hy][hx] = f[1 + c];
+    for (int c = 0; c < 1 + NC; ++c) {
+        ip.in[c] = in ? static_cast<const vec2_t<T> *>(in[c]) + off : nullptr;
+        ip.aux[c] = aux ? static_cast<const vec2_t<T> *>(aux[c]) + off : nullptr;
+        ip.out[c] = out ? static_cast<vec2_t<T> *>(out[c]) + off : nullptr;
     }
+}
+
+// Field h at a neighbour (per-site strings only).
+template <class T>
+__device__ __forceinline__ T h_site(const StringDesc &S, const SiteParams<T> &p, int s)
+{
+    return S.per_site ? static_cast<const T *>(S.ph)[s] : p.h;
 }
 
 // --------------------------------------------------------------- line search
@@ -129,6 +171,8 @@ __device__ double line_search_scan(const double *c, const double *xt)
     return (double)((T)xt[j] / m);
 }
 
+// Exact minimiser of the quartic on alpha > 0 (closed-form roots of the
+// cubic derivative, two Newton steps each); `fallback` when none.
 __device__ double line_search_exact(const double *c, double fallback)
 {
     const double a3 = 4 * c[4], a2 = 3 * c[3], a1 = 2 * c[2], a0 = c[1];
@@ -174,46 +218,71 @@ __device__ double line_search_exact(const double *c, double fallback)
 
 // ------------------------------------------------------------------ kernels
 template <class T, int NC>
-__global__ void __launch_bounds__(NT) k_grad(const StringDesc *__restrict__ strings, const TileRef *__restrict__ tiles,
+__global__ void __launch_bounds__(NT, MEPGL_MINB_GRAD) k_grad(const __grid_constant__ Batch bt, const TileRef *__restrict__ tiles,
                                              int n_tiles, Scalars sc, StepFlags f)
 {
+    constexpr int TYT = TileRows<T>::v;
     using V = vec2_t<T>;
-    __shared__ Tile<T, NC, TY> t;
+    __shared__ Tile<T, NC, TYT> t;
     __shared__ double red[NT / 32 * 2];
     for (int tt = blockIdx.x; tt < n_tiles; tt += gridDim.x) {
         const TileRef tr = tiles[tt];
-        const StringDesc &S = strings[tr.s];
+        const StringDesc &S = bt.s[tr.s];
         const int img = S.img_base + tr.n;
-        const int i0 = tr.tx * TX, j0 = tr.ty * TY;
-        stage_state<T, NC>(t, S, tr.n, i0, j0, f.xin, f.xout, f.din, (T)sc.alpha_pend[img], true);
-        __syncthreads();
-        const int lx = threadIdx.x % TX, ly = threadIdx.x / TX, gi = i0 + lx, gj = j0 + ly;
-        double v[2] = {0.0, 0.0};
-        if (gi < S.nx && gj < S.ny) {
-            const long s = gi + (long)S.nx * gj, k = (long)tr.n * S.nx * S.ny + s;
-            SiteParams<T> p;
-            p.load(S, s, NC);
-            T g[2 + 2 * NC];
-            site_gradient<T, NC, TY>(t, lx + 1, ly + 1, p, S, s, f.maxwell, S.thin_film, g);
+        const int i0 = tr.tx * TX, j0 = tr.ty * TYT;
+        const size_t off = (size_t)tr.n * S.nx * S.ny;
+        ImagePtrs<T, NC> ip;
+        image_ptrs<T, NC>(ip, S.x[f.xin], S.d[f.din], S.x[f.xout], off);
+        stage<T, NC, TYT, 1>(t, S, ip, i0, j0, (T)sc.alpha_pend[img], true, true);
+        V *gcur[1 + NC];
+        const V *gprev[1 + NC];
 #pragma unroll
-            for (int c = 0; c < 1 + NC; ++c) {
-                V gv;
-                gv.x = g[2 * c];
-                gv.y = g[2 * c + 1];
-                static_cast<V *>(S.g[f.gcur][c])[k] = gv;
-                const V go = static_cast<const V *>(S.g[f.gprev][c])[k];
-                v[0] += (double)(gv.x * gv.x) + (double)(gv.y * gv.y);
-                v[1] += (double)(gv.x * (gv.x - go.x)) + (double)(gv.y * (gv.y - go.y));
+        for (int c = 0; c < 1 + NC; ++c) {
+            gcur[c] = static_cast<V *>(S.g[f.gcur][c]) + off;
+            gprev[c] = static_cast<const V *>(S.g[f.gprev][c]) + off;
+        }
+        SiteParams<T> p;
+        p.load_uniform(S);
+        __syncthreads();
+        T v[2] = {(T)0, (T)0};
+        const int lx = threadIdx.x & 31, gi = i0 + lx;
+#pragma unroll
+        for (int r = 0; r < TYT / 8; ++r) {
+            const int ly = (threadIdx.x >> 5) + 8 * r, gj = j0 + ly;
+            if (gi < S.nx && gj < S.ny) {
+                const int s = gi + S.nx * gj;
+                Wts<T> w;
+                w.load(t.m[ly + 1][lx + 1]);
+                T hr = p.h, hl = p.h, hu = p.h, hd = p.h;
+                if (S.per_site) {
+                    p.load_site(S, s, NC);
+                    hr = h_site(S, p, s + 1 < S.nx * S.ny ? s + 1 : s);
+                    hl = h_site(S, p, s > 0 ? s - 1 : s);
+                    hu = h_site(S, p, gj + 1 < S.ny ? s + S.nx : s);
+                    hd = h_site(S, p, gj > 0 ? s - S.nx : s);
+                }
+                T g[2 + 2 * NC];
+                site_gradient<T, NC, TYT>(t, lx + 1, ly + 1, p, w, hr, hl, hu, hd, f.maxwell, S.thin_film, g);
+#pragma unroll
+                for (int c = 0; c < 1 + NC; ++c) {
+                    V gv;
+                    gv.x = g[2 * c];
+                    gv.y = g[2 * c + 1];
+                    gcur[c][s] = gv;
+                    const V go = gprev[c][s];
+                    v[0] += gv.x * gv.x + gv.y * gv.y;
+                    v[1] += gv.x * (gv.x - go.x) + gv.y * (gv.y - go.y);
+                }
             }
         }
         const int tpi = S.tiles_x * S.tiles_y;
         double tot[2];
         if (finish_image<2>(v, red, sc, tt, S.tile_base + tr.n * tpi, tpi, img, tot) && threadIdx.x == 0) {
-            (f.gcur ? sc.gn[1] : sc.gn[0])[img] = tot[0];
+            (f.gcur ? sc.gn1 : sc.gn0)[img] = tot[0];
             sc.gdg[img] = tot[1];
             double beta = 0.0;
             if (f.use_cg) {
-                beta = tot[1] / (f.gprev ? sc.gn[1] : sc.gn[0])[img];
+                beta = tot[1] / (f.gprev ? sc.gn1 : sc.gn0)[img];
                 beta = beta > 0.0 ? beta : 0.0;   // Polak-Ribiere clipped at 0; NaN -> 0
             }
             sc.beta[img] = beta;
@@ -223,32 +292,43 @@ __global__ void __launch_bounds__(NT) k_grad(const StringDesc *__restrict__ stri
 }
 
 template <class T, int NC>
-__global__ void __launch_bounds__(NT) k_dir_poly(const StringDesc *__restrict__ strings,
+__global__ void __launch_bounds__(NT, MEPGL_MINB_DIR) k_dir_poly(const __grid_constant__ Batch bt,
                                                  const TileRef *__restrict__ tiles, int n_tiles, Scalars sc,
                                                  StepFlags f)
 {
-    __shared__ Tile<T, NC, TY> tx;
-    __shared__ Tile<T, NC, TY> td;
+    constexpr int TYT = TileRows<T>::v;
+    __shared__ Tile<T, NC, TYT> tx;
+    __shared__ Tile<T, NC, TYT> td;
     __shared__ double red[NT / 32 * 5];
     __shared__ double coef[5];
     for (int tt = blockIdx.x; tt < n_tiles; tt += gridDim.x) {
         const TileRef tr = tiles[tt];
-        const StringDesc &S = strings[tr.s];
+        const StringDesc &S = bt.s[tr.s];
         const int img = S.img_base + tr.n;
-        const int i0 = tr.tx * TX, j0 = tr.ty * TY;
-        stage_state<T, NC>(tx, S, tr.n, i0, j0, f.xout, f.xout, f.din, (T)0, false);
-        stage_direction<T, NC>(td, S, tr.n, i0, j0, f.gcur, f.din, f.dout, (T)sc.beta[img]);
+        const int i0 = tr.tx * TX, j0 = tr.ty * TYT;
+        const size_t off = (size_t)tr.n * S.nx * S.ny;
+        ImagePtrs<T, NC> ipx, ipd;
+        image_ptrs<T, NC>(ipx, S.x[f.xout], nullptr, nullptr, off);
+        image_ptrs<T, NC>(ipd, S.d[f.din], S.g[f.gcur], S.d[f.dout], off);
+        stage<T, NC, TYT, 0>(tx, S, ipx, i0, j0, (T)0, false, true);
+        stage<T, NC, TYT, 2>(td, S, ipd, i0, j0, (T)sc.beta[img], true, false);
+        SiteParams<T> p;
+        p.load_uniform(S);
         __syncthreads();
-        const int lx = threadIdx.x % TX, ly = threadIdx.x / TX, gi = i0 + lx, gj = j0 + ly;
-        double v[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
-        if (gi < S.nx && gj < S.ny) {
-            const long s = gi + (long)S.nx * gj;
-            SiteParams<T> p;
-            p.load(S, s, NC);
-            T o[5];
-            site_poly<T, NC, TY>(tx, td, lx + 1, ly + 1, p, f.poly_compat, S.thin_film, o);
+        T v[5] = {(T)0, (T)0, (T)0, (T)0, (T)0};
+        const int lx = threadIdx.x & 31, gi = i0 + lx;
 #pragma unroll
-            for (int k = 0; k < 5; ++k) v[k] = (double)o[k];
+        for (int r = 0; r < TYT / 8; ++r) {
+            const int ly = (threadIdx.x >> 5) + 8 * r, gj = j0 + ly;
+            if (gi < S.nx && gj < S.ny) {
+                Wts<T> w;
+                w.load(tx.m[ly + 1][lx + 1]);
+                if (S.per_site) p.load_site(S, gi + S.nx * gj, NC);
+                T o[5];
+                site_poly<T, NC, TYT>(tx, td, lx + 1, ly + 1, p, w, f.poly_compat, S.thin_film, o);
+#pragma unroll
+                for (int k = 0; k < 5; ++k) v[k] += o[k];
+            }
         }
         const int tpi = S.tiles_x * S.tiles_y;
         double tot[5];
@@ -276,25 +356,34 @@ __global__ void __launch_bounds__(NT) k_dir_poly(const StringDesc *__restrict__ 
 }
 
 template <class T, int NC>
-__global__ void __launch_bounds__(NT) k_energy(const StringDesc *__restrict__ strings, const TileRef *__restrict__ tiles,
+__global__ void __launch_bounds__(NT) k_energy(const __grid_constant__ Batch bt, const TileRef *__restrict__ tiles,
                                                int n_tiles, Scalars sc, int xbuf, double *out)
 {
-    __shared__ Tile<T, NC, TY> t;
+    constexpr int TYT = TileRows<T>::v;
+    __shared__ Tile<T, NC, TYT> t;
     __shared__ double red[NT / 32];
     for (int tt = blockIdx.x; tt < n_tiles; tt += gridDim.x) {
         const TileRef tr = tiles[tt];
-        const StringDesc &S = strings[tr.s];
+        const StringDesc &S = bt.s[tr.s];
         const int img = S.img_base + tr.n;
-        const int i0 = tr.tx * TX, j0 = tr.ty * TY;
-        stage_state<T, NC>(t, S, tr.n, i0, j0, xbuf, xbuf, 0, (T)0, false);
+        const int i0 = tr.tx * TX, j0 = tr.ty * TYT;
+        ImagePtrs<T, NC> ip;
+        image_ptrs<T, NC>(ip, S.x[xbuf], nullptr, nullptr, (size_t)tr.n * S.nx * S.ny);
+        stage<T, NC, TYT, 0>(t, S, ip, i0, j0, (T)0, false, true);
+        SiteParams<T> p;
+        p.load_uniform(S);
         __syncthreads();
-        const int lx = threadIdx.x % TX, ly = threadIdx.x / TX, gi = i0 + lx, gj = j0 + ly;
-        double v[1] = {0.0};
-        if (gi < S.nx && gj < S.ny) {
-            const long s = gi + (long)S.nx * gj;
-            SiteParams<T> p;
-            p.load(S, s, NC);
-            v[0] = (double)site_energy<T, NC, TY>(t, lx + 1, ly + 1, p, S.thin_film);
+        T v[1] = {(T)0};
+        const int lx = threadIdx.x & 31, gi = i0 + lx;
+#pragma unroll
+        for (int r = 0; r < TYT / 8; ++r) {
+            const int ly = (threadIdx.x >> 5) + 8 * r, gj = j0 + ly;
+            if (gi < S.nx && gj < S.ny) {
+                Wts<T> w;
+                w.load(t.m[ly + 1][lx + 1]);
+                if (S.per_site) p.load_site(S, gi + S.nx * gj, NC);
+                v[0] += site_energy<T, NC, TYT>(t, lx + 1, ly + 1, p, w, S.thin_film);
+            }
         }
         const int tpi = S.tiles_x * S.tiles_y;
         double tot[1];
@@ -305,31 +394,49 @@ __global__ void __launch_bounds__(NT) k_energy(const StringDesc *__restrict__ st
 }
 
 template <class T, int NC>
-__global__ void __launch_bounds__(NT) k_gradient_only(const StringDesc *__restrict__ strings,
+__global__ void __launch_bounds__(NT) k_gradient_only(const __grid_constant__ Batch bt,
                                                       const TileRef *__restrict__ tiles, int n_tiles, int xbuf,
                                                       FieldPtrs out, int maxwell)
 {
+    constexpr int TYT = TileRows<T>::v;
     using V = vec2_t<T>;
-    __shared__ Tile<T, NC, TY> t;
+    __shared__ Tile<T, NC, TYT> t;
     for (int tt = blockIdx.x; tt < n_tiles; tt += gridDim.x) {
         const TileRef tr = tiles[tt];
-        const StringDesc &S = strings[tr.s];
-        const int i0 = tr.tx * TX, j0 = tr.ty * TY;
-        stage_state<T, NC>(t, S, tr.n, i0, j0, xbuf, xbuf, 0, (T)0, false);
+        const StringDesc &S = bt.s[tr.s];
+        const int i0 = tr.tx * TX, j0 = tr.ty * TYT;
+        const size_t off = (size_t)tr.n * S.nx * S.ny;
+        ImagePtrs<T, NC> ip;
+        image_ptrs<T, NC>(ip, S.x[xbuf], nullptr, nullptr, off);
+        stage<T, NC, TYT, 0>(t, S, ip, i0, j0, (T)0, false, true);
+        SiteParams<T> p;
+        p.load_uniform(S);
         __syncthreads();
-        const int lx = threadIdx.x % TX, ly = threadIdx.x / TX, gi = i0 + lx, gj = j0 + ly;
-        if (gi < S.nx && gj < S.ny) {
-            const long s = gi + (long)S.nx * gj, k = (long)tr.n * S.nx * S.ny + s;
-            SiteParams<T> p;
-            p.load(S, s, NC);
-            T g[2 + 2 * NC];
-            site_gradient<T, NC, TY>(t, lx + 1, ly + 1, p, S, s, maxwell, S.thin_film, g);
+        const int lx = threadIdx.x & 31, gi = i0 + lx;
 #pragma unroll
-            for (int c = 0; c < 1 + NC; ++c) {
-                V gv;
-                gv.x = g[2 * c];
-                gv.y = g[2 * c + 1];
-                static_cast<V *>(out.p[c])[k] = gv;
+        for (int r = 0; r < TYT / 8; ++r) {
+            const int ly = (threadIdx.x >> 5) + 8 * r, gj = j0 + ly;
+            if (gi < S.nx && gj < S.ny) {
+                const int s = gi + S.nx * gj;
+                Wts<T> w;
+                w.load(t.m[ly + 1][lx + 1]);
+                T hr = p.h, hl = p.h, hu = p.h, hd = p.h;
+                if (S.per_site) {
+                    p.load_site(S, s, NC);
+                    hr = h_site(S, p, s + 1 < S.nx * S.ny ? s + 1 : s);
+                    hl = h_site(S, p, s > 0 ? s - 1 : s);
+                    hu = h_site(S, p, gj + 1 < S.ny ? s + S.nx : s);
+                    hd = h_site(S, p, gj > 0 ? s - S.nx : s);
+                }
+                T g[2 + 2 * NC];
+                site_gradient<T, NC, TYT>(t, lx + 1, ly + 1, p, w, hr, hl, hu, hd, maxwell, S.thin_film, g);
+#pragma unroll
+                for (int c = 0; c < 1 + NC; ++c) {
+                    V gv;
+                    gv.x = g[2 * c];
+                    gv.y = g[2 * c + 1];
+                    (static_cast<V *>(out.p[c]) + off)[s] = gv;
+                }
             }
         }
         __syncthreads();
@@ -337,52 +444,64 @@ __global__ void __launch_bounds__(NT) k_gradient_only(const StringDesc *__restri
 }
 
 template <class T, int NC>
-__global__ void __launch_bounds__(NT) k_jb(const StringDesc *__restrict__ strings, const TileRef *__restrict__ tiles,
+__global__ void __launch_bounds__(NT) k_jb(const __grid_constant__ Batch bt, const TileRef *__restrict__ tiles,
                                            int n_tiles, int xbuf, T *b, vec2_t<T> *j1, vec2_t<T> *j2)
 {
+    constexpr int TYT = TileRows<T>::v;
     using V = vec2_t<T>;
-    __shared__ Tile<T, NC, TY> t;
+    __shared__ Tile<T, NC, TYT> t;
     for (int tt = blockIdx.x; tt < n_tiles; tt += gridDim.x) {
         const TileRef tr = tiles[tt];
-        const StringDesc &S = strings[tr.s];
-        const int i0 = tr.tx * TX, j0 = tr.ty * TY;
-        stage_state<T, NC>(t, S, tr.n, i0, j0, xbuf, xbuf, 0, (T)0, false);
+        const StringDesc &S = bt.s[tr.s];
+        const int i0 = tr.tx * TX, j0 = tr.ty * TYT;
+        const size_t off = (size_t)tr.n * S.nx * S.ny;
+        ImagePtrs<T, NC> ip;
+        image_ptrs<T, NC>(ip, S.x[xbuf], nullptr, nullptr, off);
+        stage<T, NC, TYT, 0>(t, S, ip, i0, j0, (T)0, false, true);
+        SiteParams<T> p;
+        p.load_uniform(S);
         __syncthreads();
-        const int lx = threadIdx.x % TX, ly = threadIdx.x / TX, gi = i0 + lx, gj = j0 + ly;
-        if (gi < S.nx && gj < S.ny) {
-            const long s = gi + (long)S.nx * gj, k = (long)tr.n * S.nx * S.ny + s;
-            SiteParams<T> p;
-            p.load(S, s, NC);
-            T o[1 + 2 * NC];
-            site_jb<T, NC, TY>(t, lx + 1, ly + 1, p, o);
-            b[k] = o[0];
-            V v;
-            v.x = o[1];
-            v.y = o[2];
-            j1[k] = v;
-            if (NC == 2) {
-                v.x = o[3];
-                v.y = o[4];
-                j2[k] = v;
+        const int lx = threadIdx.x & 31, gi = i0 + lx;
+#pragma unroll
+        for (int r = 0; r < TYT / 8; ++r) {
+            const int ly = (threadIdx.x >> 5) + 8 * r, gj = j0 + ly;
+            if (gi < S.nx && gj < S.ny) {
+                const size_t k = off + gi + (size_t)S.nx * gj;
+                Wts<T> w;
+                w.load(t.m[ly + 1][lx + 1]);
+                if (S.per_site) p.load_site(S, gi + S.nx * gj, NC);
+                T o[1 + 2 * NC];
+                site_jb<T, NC, TYT>(t, lx + 1, ly + 1, p, w, o);
+                b[k] = o[0];
+                V v;
+                v.x = o[1];
+                v.y = o[2];
+                j1[k] = v;
+                if (NC == 2) {
+                    v.x = o[3];
+                    v.y = o[4];
+                    j2[k] = v;
+                }
             }
         }
         __syncthreads();
     }
 }
 
+// x += alpha_pend[image] d over one image per blockIdx.y.
 template <class T>
 __global__ void __launch_bounds__(NT) k_apply_update(vec2_t<T> *x, const vec2_t<T> *d, const double *alpha_pend,
-                                                     long M, long total)
+                                                     long M)
 {
-    for (long p = blockIdx.x * (long)NT + threadIdx.x; p < total; p += (long)gridDim.x * NT) {
-        const T a = (T)alpha_pend[p / M];
-        if (a != (T)0) {
-            vec2_t<T> v = x[p];
-            const vec2_t<T> dd = d[p];
-            v.x = v.x + a * dd.x;
-            v.y = v.y + a * dd.y;
-            x[p] = v;
-        }
+    const T a = (T)alpha_pend[blockIdx.y];
+    if (a == (T)0) return;
+    const long off = (long)blockIdx.y * M;
+    for (long p = blockIdx.x * (long)NT + threadIdx.x; p < M; p += (long)gridDim.x * NT) {
+        vec2_t<T> v = x[off + p];
+        const vec2_t<T> dd = d[off + p];
+        v.x = v.x + a * dd.x;
+        v.y = v.y + a * dd.y;
+        x[off + p] = v;
     }
 }
 
@@ -401,7 +520,7 @@ __global__ void __launch_bounds__(NT) k_arc_partial(const T *f0, const T *f1, co
     T prev[3][ARC_SPT][2];
     const long base = (long)blockIdx.x * NT * ARC_SPT + threadIdx.x;
     for (int n = 0; n < F; ++n) {
-        double acc = 0.0;
+        T acc = 0;
 #pragma unroll
         for (int q = 0; q < ARC_SPT; ++q) {
             const long s = base + (long)q * NT;
@@ -418,11 +537,12 @@ __global__ void __launch_bounds__(NT) k_arc_partial(const T *f0, const T *f1, co
                     prev[f][q][w] = v;
                 }
             }
-            acc += (double)d2;
+            acc += d2;
         }
-        double vv[1] = {acc};
-        block_sum<1>(vv, red);
-        if (threadIdx.x == 0) part[(size_t)n * gridDim.x + blockIdx.x] = vv[0];
+        const T vv[1] = {acc};
+        double tot[1];
+        block_sum<1>(vv, tot, red);
+        if (threadIdx.x == 0) part[(size_t)n * gridDim.x + blockIdx.x] = tot[0];
     }
 }
 
@@ -433,8 +553,9 @@ __global__ void k_arc_finish(const double *part, int nblocks, int F, double *s)
     for (int n = 0; n < F; ++n) {
         double v[1] = {0.0};
         for (int b = threadIdx.x; b < nblocks; b += NT) v[0] += part[(size_t)n * nblocks + b];
-        block_sum<1>(v, red);
-        if (threadIdx.x == 0) s[n] = v[0];
+        double tot[1];
+        block_sum<1>(v, tot, red);
+        if (threadIdx.x == 0) s[n] = tot[0];
     }
     if (threadIdx.x == 0) {
         s[0] = 0.0;
@@ -598,25 +719,25 @@ inline int grid_for(long n, int cap = 152 * 16)
 
 cudaError_t launch_grad(const Launch &L, const Scalars &sc, const StepFlags &f)
 {
-    DISPATCH(L, k_grad, L.strings, L.tiles, L.n_tiles, sc, f);
+    DISPATCH(L, k_grad, *L.batch, L.tiles, L.n_tiles, sc, f);
     return cudaGetLastError();
 }
 
 cudaError_t launch_dir_poly(const Launch &L, const Scalars &sc, const StepFlags &f)
 {
-    DISPATCH(L, k_dir_poly, L.strings, L.tiles, L.n_tiles, sc, f);
+    DISPATCH(L, k_dir_poly, *L.batch, L.tiles, L.n_tiles, sc, f);
     return cudaGetLastError();
 }
 
 cudaError_t launch_energy(const Launch &L, const Scalars &sc, int xbuf, double *out)
 {
-    DISPATCH(L, k_energy, L.strings, L.tiles, L.n_tiles, sc, xbuf, out);
+    DISPATCH(L, k_energy, *L.batch, L.tiles, L.n_tiles, sc, xbuf, out);
     return cudaGetLastError();
 }
 
 cudaError_t launch_gradient_only(const Launch &L, int xbuf, FieldPtrs out, int maxwell)
 {
-    DISPATCH(L, k_gradient_only, L.strings, L.tiles, L.n_tiles, xbuf, out, maxwell);
+    DISPATCH(L, k_gradient_only, *L.batch, L.tiles, L.n_tiles, xbuf, out, maxwell);
     return cudaGetLastError();
 }
 
@@ -625,17 +746,17 @@ cudaError_t launch_jb(const Launch &L, const Scalars &sc, int xbuf, void *const 
     (void)sc;
     if (L.precision == 1) {
         if (L.ncomp == 2)
-            k_jb<double, 2><<<L.grid, NT, 0, L.stream>>>(L.strings, L.tiles, L.n_tiles, xbuf, (double *)b[0],
+            k_jb<double, 2><<<L.grid, NT, 0, L.stream>>>(*L.batch, L.tiles, L.n_tiles, xbuf, (double *)b[0],
                                                          (double2 *)j[0][0], (double2 *)j[0][1]);
         else
-            k_jb<double, 1><<<L.grid, NT, 0, L.stream>>>(L.strings, L.tiles, L.n_tiles, xbuf, (double *)b[0],
+            k_jb<double, 1><<<L.grid, NT, 0, L.stream>>>(*L.batch, L.tiles, L.n_tiles, xbuf, (double *)b[0],
                                                          (double2 *)j[0][0], (double2 *)j[0][1]);
     } else {
         if (L.ncomp == 2)
-            k_jb<float, 2><<<L.grid, NT, 0, L.stream>>>(L.strings, L.tiles, L.n_tiles, xbuf, (float *)b[0],
+            k_jb<float, 2><<<L.grid, NT, 0, L.stream>>>(*L.batch, L.tiles, L.n_tiles, xbuf, (float *)b[0],
                                                         (float2 *)j[0][0], (float2 *)j[0][1]);
         else
-            k_jb<float, 1><<<L.grid, NT, 0, L.stream>>>(L.strings, L.tiles, L.n_tiles, xbuf, (float *)b[0],
+            k_jb<float, 1><<<L.grid, NT, 0, L.stream>>>(*L.batch, L.tiles, L.n_tiles, xbuf, (float *)b[0],
                                                         (float2 *)j[0][0], (float2 *)j[0][1]);
     }
     return cudaGetLastError();
@@ -646,14 +767,15 @@ cudaError_t launch_apply_update(const Launch &L, const Scalars &sc, const String
 {
     for (int si = 0; si < n_strings; ++si) {
         const StringDesc &S = hs[si];
-        const long M = (long)S.nx * S.ny, total = M * S.F;
+        const long M = (long)S.nx * S.ny;
         for (int c = 0; c < 1 + S.ncomp; ++c) {
+            const dim3 grid((unsigned)((M + NT - 1) / NT < 64 ? (M + NT - 1) / NT : 64), (unsigned)S.F);
             if (L.precision == 1)
-                k_apply_update<double><<<grid_for(total), NT, 0, L.stream>>>(
-                    (double2 *)S.x[xbuf][c], (const double2 *)S.d[dbuf][c], sc.alpha_pend + S.img_base, M, total);
+                k_apply_update<double><<<grid, NT, 0, L.stream>>>(
+                    (double2 *)S.x[xbuf][c], (const double2 *)S.d[dbuf][c], sc.alpha_pend + S.img_base, M);
             else
-                k_apply_update<float><<<grid_for(total), NT, 0, L.stream>>>(
-                    (float2 *)S.x[xbuf][c], (const float2 *)S.d[dbuf][c], sc.alpha_pend + S.img_base, M, total);
+                k_apply_update<float><<<grid, NT, 0, L.stream>>>(
+                    (float2 *)S.x[xbuf][c], (const float2 *)S.d[dbuf][c], sc.alpha_pend + S.img_base, M);
         }
     }
     cudaError_t e = cudaGetLastError();

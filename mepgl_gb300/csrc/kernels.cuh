@@ -5,11 +5,15 @@
 
 namespace mepgl {
 
-constexpr int TY = 8;                 // tile rows (TX * TY = NT threads, one site each)
 constexpr int LS_GRID = 2001;         // line-search grid points x_0 .. x_2000
 
+// Rows per lattice tile for a precision (0 float, 1 double); tiles are TX wide.
+int tile_rows(int precision);
+// Copy the neighbour-code weight tables to constant memory (idempotent).
+cudaError_t upload_mask_tables();
+
 struct Launch {
-    const StringDesc *strings;   // device
+    const Batch *batch;          // host copy; passed by value to the kernels
     const TileRef *tiles;        // device
     int n_tiles;
     int grid;                    // blocks launched (grid-stride over tiles)

@@ -11,17 +11,80 @@
 // at every site, four collocated views of curl A - h (forward/backward
 // differences of A_y along x and of A_x along y), each weighted 1/8 when the
 // plaquette is inside the computational domain.
+//
+// Domain handling is branchless: every link / plaquette term is multiplied
+// by a weight that is zero when the reference would skip it.  The weights
+// of a site come from two constant tables indexed by its 8-bit neighbour
+// codes (bit order 0:+x 1:+x+y 2:+y 3:-x+y 4:-x 5:-x-y 6:-y 7:+x-y,
+// nlcg.cu:48-103), so no bit arithmetic or int->float conversion runs per
+// site.  Outside-lattice halo values are zero, so masked terms are finite.
 #pragma once
 
 #include "common.cuh"
 
 namespace mepgl {
 
-template <class T, int NC, int TY>
+// Weights of a superconducting code: area fraction, link weights (forward
+// x, backward x, forward y, backward y; zero when the link is absent), and
+// the bare link bits (used by J).  Of a computational code: the validity
+// (0/1) of the four curl views UR, UL, LL, LR.
+template <class T>
+struct MaskTable {
+    T sc[256][12];    // area, wfx, wbx, wfy, wby, lfx, lbx, lfy, lby, 0, 0, 0
+    T cc[256][4];     // vUR, vUL, vLL, vLR
+};
+// Defined here: kernels.cu is the only translation unit that includes this file.
+__constant__ MaskTable<float> c_mask_f;
+__constant__ MaskTable<double> c_mask_d;
+
+template <class T> __device__ __forceinline__ const MaskTable<T> &mask_table();
+template <> __device__ __forceinline__ const MaskTable<float> &mask_table<float>() { return c_mask_f; }
+template <> __device__ __forceinline__ const MaskTable<double> &mask_table<double>() { return c_mask_d; }
+
+template <class T>
+struct Wts {
+    T area, wfx, wbx, wfy, wby, lfx, lbx, lfy, lby;
+    T vUR, vUL, vLL, vLR;
+    __device__ __forceinline__ void load(unsigned mk)
+    {
+        const MaskTable<T> &M = mask_table<T>();
+        const unsigned s = mk >> 8, c = mk & 0xffu;
+        area = M.sc[s][0]; wfx = M.sc[s][1]; wbx = M.sc[s][2]; wfy = M.sc[s][3]; wby = M.sc[s][4];
+        lfx = M.sc[s][5]; lbx = M.sc[s][6]; lfy = M.sc[s][7]; lby = M.sc[s][8];
+        vUR = M.cc[c][0]; vUL = M.cc[c][1]; vLL = M.cc[c][2]; vLR = M.cc[c][3];
+    }
+};
+
+// Host-side construction of the tables (same arithmetic as nlcg.cu:522-525,
+// 186-187, 533-609 etc.: weights are exact multiples of 1/4).
+template <class T>
+inline void build_mask_table(MaskTable<T> &M)
+{
+    for (unsigned k = 0; k < 256; ++k) {
+        auto b = [&](int n) { return (int)((k >> n) & 1u); };
+        M.sc[k][0] = (T)(b(0) * b(1) * b(2) + b(2) * b(3) * b(4) + b(4) * b(5) * b(6) + b(6) * b(7) * b(0)) / (T)4;
+        M.sc[k][1] = b(0) ? (T)(b(1) * b(2) + b(6) * b(7)) / (T)2 : (T)0;
+        M.sc[k][2] = b(4) ? (T)(b(2) * b(3) + b(5) * b(6)) / (T)2 : (T)0;
+        M.sc[k][3] = b(2) ? (T)(b(0) * b(1) + b(3) * b(4)) / (T)2 : (T)0;
+        M.sc[k][4] = b(6) ? (T)(b(4) * b(5) + b(7) * b(0)) / (T)2 : (T)0;
+        M.sc[k][5] = (T)b(0);
+        M.sc[k][6] = (T)b(4);
+        M.sc[k][7] = (T)b(2);
+        M.sc[k][8] = (T)b(6);
+        M.sc[k][9] = M.sc[k][10] = M.sc[k][11] = (T)0;
+        M.cc[k][0] = (T)(b(0) & b(1) & b(2));
+        M.cc[k][1] = (T)(b(2) & b(3) & b(4));
+        M.cc[k][2] = (T)(b(4) & b(5) & b(6));
+        M.cc[k][3] = (T)(b(6) & b(7) & b(0));
+    }
+}
+
+// Tile of TYT rows (+ halo) of A, psi_1[, psi_2] and the packed codes.
+template <class T, int NC, int TYT>
 struct Tile {
-    vec2_t<T> A[TY + 2][TX + 2];
-    vec2_t<T> P[NC][TY + 2][TX + 2];
-    uint16_t m[TY + 2][TX + 2];
+    vec2_t<T> A[TYT + 2][TX + 2];
+    vec2_t<T> P[NC][TYT + 2][TX + 2];
+    uint16_t m[TYT + 2][TX + 2];
 };
 
 // Parameters of one site (uniform strings read the descriptor).
@@ -29,65 +92,48 @@ template <class T>
 struct SiteParams {
     T a[2], b[2], hmx[2], hmy[2], aob[2];  // hmx = 0.5 / m_xx
     T q[2], eta, gamma, delta, h, idx, dx2;
-    __device__ __forceinline__ void load(const StringDesc &S, long s, int nc)
+    __device__ __forceinline__ void load_uniform(const StringDesc &S)
+    {
+        const Uniform<T> &U = S.template u<T>();
+#pragma unroll
+        for (int c = 0; c < 2; ++c) {
+            a[c] = U.a[c]; b[c] = U.b[c]; hmx[c] = U.hmx[c]; hmy[c] = U.hmy[c]; aob[c] = U.aob[c]; q[c] = U.q[c];
+        }
+        eta = U.eta; gamma = U.gamma; delta = U.delta; h = U.h; idx = U.idx; dx2 = U.dx2;
+    }
+    // per-site overrides (strings whose parameter arrays are not uniform)
+    __device__ __forceinline__ void load_site(const StringDesc &S, int s, int nc)
     {
         for (int c = 0; c < nc; ++c) {
-            if (S.per_site) {
-                a[c] = static_cast<const T *>(S.pa[c])[s];
-                b[c] = static_cast<const T *>(S.pb[c])[s];
-                hmx[c] = (T)0.5 / static_cast<const T *>(S.pmxx[c])[s];
-                hmy[c] = (T)0.5 / static_cast<const T *>(S.pmyy[c])[s];
-                aob[c] = a[c] / b[c];
-            } else {
-                a[c] = (T)S.a[c];
-                b[c] = (T)S.b[c];
-                hmx[c] = (T)S.hmx[c];
-                hmy[c] = (T)S.hmy[c];
-                aob[c] = (T)S.aob[c];
-            }
-            q[c] = (T)S.q[c];
+            a[c] = static_cast<const T *>(S.pa[c])[s];
+            b[c] = static_cast<const T *>(S.pb[c])[s];
+            hmx[c] = (T)0.5 / static_cast<const T *>(S.pmxx[c])[s];
+            hmy[c] = (T)0.5 / static_cast<const T *>(S.pmyy[c])[s];
+            aob[c] = a[c] / b[c];
         }
-        eta = (T)S.eta;
-        gamma = (T)S.gamma;
-        delta = (T)S.delta;
-        h = S.per_site ? static_cast<const T *>(S.ph)[s] : (T)S.h;
-        idx = (T)S.inv_dx;
-        const T dx = (T)S.dx;
-        dx2 = dx * dx;
+        h = static_cast<const T *>(S.ph)[s];
     }
 };
-
-template <class T>
-__device__ __forceinline__ T h_at(const StringDesc &S, const SiteParams<T> &p, long s)
-{
-    return S.per_site ? static_cast<const T *>(S.ph)[s] : p.h;
-}
 
 template <class T>
 __device__ __forceinline__ void link4(T Ai, T Aj, vec2_t<T> pi, vec2_t<T> pj, T q, T idx, T t[4])
 {
     const T dre = (pj.x - pi.x) * idx, dim = (pj.y - pi.y) * idx;
-    t[0] = -dre - q * Ai * pi.y;
-    t[1] = -dre - q * Aj * pj.y;
-    t[2] = dim - q * Ai * pi.x;
-    t[3] = dim - q * Aj * pj.x;
-}
-
-__device__ __forceinline__ int area4(unsigned sc)
-{
-    return bit(sc, 0) * bit(sc, 1) * bit(sc, 2) + bit(sc, 2) * bit(sc, 3) * bit(sc, 4) +
-           bit(sc, 4) * bit(sc, 5) * bit(sc, 6) + bit(sc, 6) * bit(sc, 7) * bit(sc, 0);
+    const T qi = q * Ai, qj = q * Aj;
+    t[0] = -dre - qi * pi.y;
+    t[1] = -dre - qj * pj.y;
+    t[2] = dim - qi * pi.x;
+    t[3] = dim - qj * pj.x;
 }
 
 #define TA(dx_, dy_) (t.A[ly + (dy_)][lx + (dx_)])
 #define TP(c_, dx_, dy_) (t.P[c_][ly + (dy_)][lx + (dx_)])
 
 // Free-energy density x dx^2 (freeEnergyDensity, nlcg.cu:105-214).
-template <class T, int NC, int TY>
-__device__ __forceinline__ T site_energy(const Tile<T, NC, TY> &t, int lx, int ly, const SiteParams<T> &p, int thin_film)
+template <class T, int NC, int TYT>
+__device__ __forceinline__ T site_energy(const Tile<T, NC, TYT> &t, int lx, int ly, const SiteParams<T> &p,
+                                         const Wts<T> &w, int thin_film)
 {
-    const unsigned mk = t.m[ly][lx], cc = mk & 0xffu, sc = mk >> 8;
-    const T area = (T)area4(sc) * (T)0.25;
     const vec2_t<T> A0 = TA(0, 0);
     T nl = 0;
 #pragma unroll
@@ -103,91 +149,71 @@ __device__ __forceinline__ T site_energy(const Tile<T, NC, TY> &t, int lx, int l
         nl += p.gamma * (T)0.5 * (P1.x * P1.x + P1.y * P1.y) * (P2.x * P2.x + P2.y * P2.y);
         nl += p.delta * (T)0.5 * (R * R - I * I);
     }
-    nl *= area;
     T kx = 0, ky = 0;
-    if (bit(sc, 0)) {
 #pragma unroll
-        for (int c = 0; c < NC; ++c) {
-            T q4[4];
-            link4(A0.x, TA(1, 0).x, TP(c, 0, 0), TP(c, 1, 0), p.q[c], p.idx, q4);
-            kx += (T)0.5 * p.hmx[c] * (q4[0] * q4[0] + q4[1] * q4[1] + q4[2] * q4[2] + q4[3] * q4[3]);
-        }
+    for (int c = 0; c < NC; ++c) {
+        T q4[4];
+        link4(A0.x, TA(1, 0).x, TP(c, 0, 0), TP(c, 1, 0), p.q[c], p.idx, q4);
+        kx += (T)0.5 * p.hmx[c] * (q4[0] * q4[0] + q4[1] * q4[1] + q4[2] * q4[2] + q4[3] * q4[3]);
+        link4(A0.y, TA(0, 1).y, TP(c, 0, 0), TP(c, 0, 1), p.q[c], p.idx, q4);
+        ky += (T)0.5 * p.hmy[c] * (q4[0] * q4[0] + q4[1] * q4[1] + q4[2] * q4[2] + q4[3] * q4[3]);
     }
-    if (bit(sc, 2)) {
-#pragma unroll
-        for (int c = 0; c < NC; ++c) {
-            T q4[4];
-            link4(A0.y, TA(0, 1).y, TP(c, 0, 0), TP(c, 0, 1), p.q[c], p.idx, q4);
-            ky += (T)0.5 * p.hmy[c] * (q4[0] * q4[0] + q4[1] * q4[1] + q4[2] * q4[2] + q4[3] * q4[3]);
-        }
-    }
-    kx *= (T)(bit(sc, 1) * bit(sc, 2) + bit(sc, 6) * bit(sc, 7)) * (T)0.5;
-    ky *= (T)(bit(sc, 0) * bit(sc, 1) + bit(sc, 3) * bit(sc, 4)) * (T)0.5;
     T em = 0;
     if (!thin_film) {
-        const T ayp = bit(cc, 0) ? (TA(1, 0).y - A0.y) * p.idx : (T)0;
-        const T aym = bit(cc, 4) ? (A0.y - TA(-1, 0).y) * p.idx : (T)0;
-        const T axp = bit(cc, 2) ? (TA(0, 1).x - A0.x) * p.idx : (T)0;
-        const T axm = bit(cc, 6) ? (A0.x - TA(0, -1).x) * p.idx : (T)0;
-        T r;
-        if (bit(cc, 0) & bit(cc, 1) & bit(cc, 2)) { r = ayp - axp - p.h; em += r * r; }
-        if (bit(cc, 2) & bit(cc, 3) & bit(cc, 4)) { r = aym - axp - p.h; em += r * r; }
-        if (bit(cc, 4) & bit(cc, 5) & bit(cc, 6)) { r = aym - axm - p.h; em += r * r; }
-        if (bit(cc, 6) & bit(cc, 7) & bit(cc, 0)) { r = ayp - axm - p.h; em += r * r; }
-        em *= (T)0.125;
+        const T ayp = (TA(1, 0).y - A0.y) * p.idx, aym = (A0.y - TA(-1, 0).y) * p.idx;
+        const T axp = (TA(0, 1).x - A0.x) * p.idx, axm = (A0.x - TA(0, -1).x) * p.idx;
+        const T r0 = ayp - axp - p.h, r1 = aym - axp - p.h, r2 = aym - axm - p.h, r3 = ayp - axm - p.h;
+        em = (T)0.125 * (w.vUR * r0 * r0 + w.vUL * r1 * r1 + w.vLL * r2 * r2 + w.vLR * r3 * r3);
     }
-    return (kx + ky + nl + em) * p.dx2;
+    return (kx * w.wfx + ky * w.wfy + nl * w.area + em) * p.dx2;
 }
 
 // Gradient dF/dA (out[0..1]) and dF/dpsi_c (out[2+2c..]) at one site,
 // restating gradientPsi (nlcg.cu:504-744) and gradientA (nlcg.cu:746-888).
-// Both link ends use the mass of this site, as the reference does.
-template <class T, int NC, int TY>
-__device__ __forceinline__ void site_gradient(const Tile<T, NC, TY> &t, int lx, int ly, const SiteParams<T> &p,
-                              const StringDesc &S, long s, int maxwell, int thin_film, T *out)
+// Both link ends use the mass of this site, as the reference does.  hr, hl,
+// hu, hd: applied field at the right, left, upper and lower neighbours.
+template <class T, int NC, int TYT>
+__device__ __forceinline__ void site_gradient(const Tile<T, NC, TYT> &t, int lx, int ly, const SiteParams<T> &p,
+                                              const Wts<T> &w, T hr, T hl, T hu, T hd, int maxwell, int thin_film,
+                                              T *out)
 {
-    const unsigned mk = t.m[ly][lx], cc = mk & 0xffu, sc = mk >> 8;
-    const T area = (T)area4(sc) * (T)0.25;
-    const T w0 = (T)(bit(sc, 1) * bit(sc, 2) + bit(sc, 6) * bit(sc, 7)) * (T)0.5;   // forward x
-    const T w1 = (T)(bit(sc, 2) * bit(sc, 3) + bit(sc, 5) * bit(sc, 6)) * (T)0.5;   // backward x
-    const T w2 = (T)(bit(sc, 0) * bit(sc, 1) + bit(sc, 3) * bit(sc, 4)) * (T)0.5;   // forward y
-    const T w3 = (T)(bit(sc, 4) * bit(sc, 5) + bit(sc, 7) * bit(sc, 0)) * (T)0.5;   // backward y
     const vec2_t<T> A0 = TA(0, 0);
+    const vec2_t<T> Ar = TA(1, 0), Al = TA(-1, 0), Au = TA(0, 1), Ad = TA(0, -1);
     T gax = 0, gay = 0;
     const T idx = p.idx;
 #pragma unroll
     for (int c = 0; c < NC; ++c) {
         const vec2_t<T> P0 = TP(c, 0, 0);
         const T x = P0.x, y = P0.y, r2 = x * x + y * y, q = p.q[c];
-        T gx = (2 * p.a[c] * x + p.b[c] * 2 * x * r2) * area;
-        T gy = (2 * p.a[c] * y + p.b[c] * 2 * y * r2) * area;
+        T gx = (2 * p.a[c] * x + p.b[c] * 2 * x * r2) * w.area;
+        T gy = (2 * p.a[c] * y + p.b[c] * 2 * y * r2) * w.area;
         T u[4];
-        if (bit(sc, 0)) {
-            link4(A0.x, TA(1, 0).x, P0, TP(c, 1, 0), q, idx, u);
-            const T f = p.hmx[c] * w0;
-            gx += f * ((u[0] + u[1]) * idx - q * A0.x * u[2]);
-            gy += f * (-(u[2] + u[3]) * idx - q * A0.x * u[0]);
+        {
+            link4(A0.x, Ar.x, P0, TP(c, 1, 0), q, idx, u);
+            const T f = p.hmx[c] * w.wfx, qa = q * A0.x;
+            gx += f * ((u[0] + u[1]) * idx - qa * u[2]);
+            gy += f * (-(u[2] + u[3]) * idx - qa * u[0]);
             gax -= f * q * (y * u[0] + x * u[2]);
         }
-        if (bit(sc, 4)) {
-            link4(TA(-1, 0).x, A0.x, TP(c, -1, 0), P0, q, idx, u);
-            const T f = p.hmx[c] * w1;
-            gx += f * (-(u[1] + u[0]) * idx - q * A0.x * u[3]);
-            gy += f * ((u[3] + u[2]) * idx - q * A0.x * u[1]);
+        {
+            link4(Al.x, A0.x, TP(c, -1, 0), P0, q, idx, u);
+            const T f = p.hmx[c] * w.wbx, qa = q * A0.x;
+            gx += f * (-(u[1] + u[0]) * idx - qa * u[3]);
+            gy += f * ((u[3] + u[2]) * idx - qa * u[1]);
             gax -= f * q * (y * u[1] + x * u[3]);
         }
-        if (bit(sc, 2)) {
-            link4(A0.y, TA(0, 1).y, P0, TP(c, 0, 1), q, idx, u);
-            const T f = p.hmy[c] * w2;
-            gx += f * ((u[0] + u[1]) * idx - q * A0.y * u[2]);
-            gy += f * (-(u[2] + u[3]) * idx - q * A0.y * u[0]);
+        {
+            link4(A0.y, Au.y, P0, TP(c, 0, 1), q, idx, u);
+            const T f = p.hmy[c] * w.wfy, qa = q * A0.y;
+            gx += f * ((u[0] + u[1]) * idx - qa * u[2]);
+            gy += f * (-(u[2] + u[3]) * idx - qa * u[0]);
             gay -= f * q * (y * u[0] + x * u[2]);
         }
-        if (bit(sc, 6)) {
-            link4(TA(0, -1).y, A0.y, TP(c, 0, -1), P0, q, idx, u);
-            const T f = p.hmy[c] * w3;
-            gx += f * (-(u[1] + u[0]) * idx - q * A0.y * u[3]);
-            gy += f * ((u[3] + u[2]) * idx - q * A0.y * u[1]);
+        {
+            link4(Ad.y, A0.y, TP(c, 0, -1), P0, q, idx, u);
+            const T f = p.hmy[c] * w.wby, qa = q * A0.y;
+            gx += f * (-(u[1] + u[0]) * idx - qa * u[3]);
+            gy += f * ((u[3] + u[2]) * idx - qa * u[1]);
             gay -= f * q * (y * u[1] + x * u[3]);
         }
         out[2 + 2 * c] = gx;
@@ -198,49 +224,31 @@ __device__ __forceinline__ void site_gradient(const Tile<T, NC, TY> &t, int lx, 
         const T x1 = P1.x, y1 = P1.y, x2 = P2.x, y2 = P2.y;
         const T r1 = x1 * x1 + y1 * y1, r2 = x2 * x2 + y2 * y2;
         const T R = x1 * x2 + y1 * y2, I = x1 * y2 - y1 * x2;
-        out[2] += (p.eta * x2 + p.gamma * x1 * r2 + p.delta * (x2 * R - y2 * I)) * area;
-        out[3] += (p.eta * y2 + p.gamma * y1 * r2 + p.delta * (y2 * R + x2 * I)) * area;
-        out[2 + 2 * (NC - 1)] += (p.eta * x1 + p.gamma * x2 * r1 + p.delta * (x1 * R + y1 * I)) * area;
-        out[3 + 2 * (NC - 1)] += (p.eta * y1 + p.gamma * y2 * r1 + p.delta * (y1 * R - x1 * I)) * area;
+        out[2] += (p.eta * x2 + p.gamma * x1 * r2 + p.delta * (x2 * R - y2 * I)) * w.area;
+        out[3] += (p.eta * y2 + p.gamma * y1 * r2 + p.delta * (y2 * R + x2 * I)) * w.area;
+        out[2 + 2 * (NC - 1)] += (p.eta * x1 + p.gamma * x2 * r1 + p.delta * (x1 * R + y1 * I)) * w.area;
+        out[3 + 2 * (NC - 1)] += (p.eta * y1 + p.gamma * y2 * r1 + p.delta * (y1 * R - x1 * I)) * w.area;
     }
 #pragma unroll
     for (int k = 2; k < 2 + 2 * NC; ++k) out[k] = maxwell ? (T)0 : out[k] * p.dx2;
 
     if (!thin_film) {
-        const int nx = S.nx;
+        // link differences ex(i,j) = d_x A_y on the x-link i -> i+1, ey(i,j) = d_y A_x
+        const T ex0 = (Ar.y - A0.y) * idx, exm = (A0.y - Al.y) * idx;
+        const T ey0 = (Au.x - A0.x) * idx, eym = (A0.x - Ad.x) * idx;
+        const T exu = (TA(1, 1).y - Au.y) * idx, exmu = (Au.y - TA(-1, 1).y) * idx;
+        const T exd = (TA(1, -1).y - Ad.y) * idx, exmd = (Ad.y - TA(-1, -1).y) * idx;
+        const T eyr = (TA(1, 1).x - Ar.x) * idx, eyrm = (Ar.x - TA(1, -1).x) * idx;
+        const T eyl = (TA(-1, 1).x - Al.x) * idx, eylm = (Al.x - TA(-1, -1).x) * idx;
+        const T h = p.h;
+        // residuals of the collocated views of this site and of the
+        // neighbours' views of the same plaquettes (nlcg.cu:852-883)
+        const T rUR = ex0 - ey0 - h, rUL = exm - ey0 - h, rLL = exm - eym - h, rLR = ex0 - eym - h;
         const T c4 = (T)0.25 * idx;
-#define AX(a_, b_) TA(a_, b_).x
-#define AY(a_, b_) TA(a_, b_).y
-        if (bit(cc, 0) & bit(cc, 1) & bit(cc, 2)) {
-            const T r = (AY(1, 0) - AY(0, 0)) * idx - (AX(0, 1) - AX(0, 0)) * idx - p.h;
-            gax += c4 * r;
-            gay -= c4 * r;
-            gay -= c4 * ((AY(1, 0) - AY(0, 0)) * idx - (AX(1, 1) - AX(1, 0)) * idx - h_at(S, p, s + 1));
-            gax += c4 * ((AY(1, 1) - AY(0, 1)) * idx - (AX(0, 1) - AX(0, 0)) * idx - h_at(S, p, s + nx));
-        }
-        if (bit(cc, 2) & bit(cc, 3) & bit(cc, 4)) {
-            const T r = (AY(0, 0) - AY(-1, 0)) * idx - (AX(0, 1) - AX(0, 0)) * idx - p.h;
-            gax += c4 * r;
-            gay += c4 * r;
-            gax += c4 * ((AY(0, 1) - AY(-1, 1)) * idx - (AX(0, 1) - AX(0, 0)) * idx - h_at(S, p, s + nx));
-            gay += c4 * ((AY(0, 0) - AY(-1, 0)) * idx - (AX(-1, 1) - AX(-1, 0)) * idx - h_at(S, p, s - 1));
-        }
-        if (bit(cc, 4) & bit(cc, 5) & bit(cc, 6)) {
-            const T r = (AY(0, 0) - AY(-1, 0)) * idx - (AX(0, 0) - AX(0, -1)) * idx - p.h;
-            gax -= c4 * r;
-            gay += c4 * r;
-            gay += c4 * ((AY(0, 0) - AY(-1, 0)) * idx - (AX(-1, 0) - AX(-1, -1)) * idx - h_at(S, p, s - 1));
-            gax -= c4 * ((AY(0, -1) - AY(-1, -1)) * idx - (AX(0, 0) - AX(0, -1)) * idx - h_at(S, p, s - nx));
-        }
-        if (bit(cc, 6) & bit(cc, 7) & bit(cc, 0)) {
-            const T r = (AY(1, 0) - AY(0, 0)) * idx - (AX(0, 0) - AX(0, -1)) * idx - p.h;
-            gax -= c4 * r;
-            gay -= c4 * r;
-            gax -= c4 * ((AY(1, -1) - AY(0, -1)) * idx - (AX(0, 0) - AX(0, -1)) * idx - h_at(S, p, s - nx));
-            gay -= c4 * ((AY(1, 0) - AY(0, 0)) * idx - (AX(1, 0) - AX(1, -1)) * idx - h_at(S, p, s + 1));
-        }
-#undef AX
-#undef AY
+        gax += c4 * (w.vUR * (rUR + (exu - ey0 - hu)) + w.vUL * (rUL + (exmu - ey0 - hu)) -
+                     w.vLL * (rLL + (exmd - eym - hd)) - w.vLR * (rLR + (exd - eym - hd)));
+        gay += c4 * (-w.vUR * (rUR + (ex0 - eyr - hr)) + w.vUL * (rUL + (exm - eyl - hl)) +
+                     w.vLL * (rLL + (exm - eylm - hl)) - w.vLR * (rLR + (ex0 - eyrm - hr)));
         out[0] = gax * p.dx2;
         out[1] = gay * p.dx2;
     } else {
@@ -252,12 +260,10 @@ __device__ __forceinline__ void site_gradient(const Tile<T, NC, TY> &t, int lx, 
 // Quartic coefficients of F(x + a d) at one site (polynomialExpansion,
 // nlcg.cu:997-1370): out = {A, B, C, D, E}.  compat keeps the reference's
 // x-link first-order slip and y-link halved cubic coefficient.
-template <class T, int NC, int TY>
-__device__ __forceinline__ void site_poly(const Tile<T, NC, TY> &t, const Tile<T, NC, TY> &dt, int lx, int ly,
-                          const SiteParams<T> &p, int compat, int thin_film, T *out)
+template <class T, int NC, int TYT>
+__device__ __forceinline__ void site_poly(const Tile<T, NC, TYT> &t, const Tile<T, NC, TYT> &dt, int lx, int ly,
+                                          const SiteParams<T> &p, const Wts<T> &w, int compat, int thin_film, T *out)
 {
-    const unsigned mk = t.m[ly][lx], cc = mk & 0xffu, sc = mk >> 8;
-    const T area = (T)area4(sc) * (T)0.25;
     T e = 0, b1 = 0, c2 = 0, d3 = 0, e4 = 0;
 #pragma unroll
     for (int c = 0; c < NC; ++c) {
@@ -289,7 +295,7 @@ __device__ __forceinline__ void site_poly(const Tile<T, NC, TY> &t, const Tile<T
         d3 += g * (s1 * t2 + s2 * t1) + dd * (2 * R1 * R2 - 2 * I1 * I2);
         e4 += g * (t1 * t2) + dd * (R2 * R2 - I2 * I2);
     }
-    e *= area; b1 *= area; c2 *= area; d3 *= area; e4 *= area;
+    e *= w.area; b1 *= w.area; c2 *= w.area; d3 *= w.area; e4 *= w.area;
     if (!thin_film) {
         const vec2_t<T> A0 = TA(0, 0), a0 = dt.A[ly][lx];
         const T idx = p.idx;
@@ -297,35 +303,30 @@ __device__ __forceinline__ void site_poly(const Tile<T, NC, TY> &t, const Tile<T
         const T axp = (TA(0, 1).x - A0.x) * idx, axm = (A0.x - TA(0, -1).x) * idx;
         const T dyp = (dt.A[ly][lx + 1].y - a0.y) * idx, dym = (a0.y - dt.A[ly][lx - 1].y) * idx;
         const T dxp = (dt.A[ly + 1][lx].x - a0.x) * idx, dxm = (a0.x - dt.A[ly - 1][lx].x) * idx;
-        T em0 = 0, em1 = 0, em2 = 0;
-        T m0, m1;
-#define EMV(cond, yy, xx, dyy, dxx)                                   \
-        if (cond) {                                                   \
-            m0 = yy - xx - p.h;                                       \
-            m1 = dyy - dxx;                                           \
-            em0 += (T)0.5 * m0 * m0;                                  \
-            em1 += m0 * m1;                                           \
-            em2 += (T)0.5 * m1 * m1;                                  \
-        }
-        EMV(bit(cc, 0) & bit(cc, 1) & bit(cc, 2), ayp, axp, dyp, dxp)
-        EMV(bit(cc, 2) & bit(cc, 3) & bit(cc, 4), aym, axp, dym, dxp)
-        EMV(bit(cc, 4) & bit(cc, 5) & bit(cc, 6), aym, axm, dym, dxm)
-        EMV(bit(cc, 6) & bit(cc, 7) & bit(cc, 0), ayp, axm, dyp, dxm)
+        T em0 = 0, em1 = 0, em2 = 0, m0, m1;
+#define EMV(wv, yy, xx, dyy, dxx)        \
+        m0 = yy - xx - p.h;              \
+        m1 = dyy - dxx;                  \
+        em0 += wv * (m0 * m0);           \
+        em1 += wv * (m0 * m1);           \
+        em2 += wv * (m1 * m1);
+        EMV(w.vUR, ayp, axp, dyp, dxp)
+        EMV(w.vUL, aym, axp, dym, dxp)
+        EMV(w.vLL, aym, axm, dym, dxm)
+        EMV(w.vLR, ayp, axm, dyp, dxm)
 #undef EMV
-        e += em0 * (T)0.25;
+        e += em0 * (T)0.125;
         b1 += em1 * (T)0.25;
-        c2 += em2 * (T)0.25;
+        c2 += em2 * (T)0.125;
     }
-    const T cwx = (T)(bit(sc, 1) * bit(sc, 2) + bit(sc, 6) * bit(sc, 7)) * (T)0.5;
-    const T cwy = (T)(bit(sc, 0) * bit(sc, 1) + bit(sc, 3) * bit(sc, 4)) * (T)0.5;
 #pragma unroll
     for (int dir = 0; dir < 2; ++dir) {
-        if (!bit(sc, dir == 0 ? 0 : 2)) continue;
         const int ox = dir == 0 ? 1 : 0, oy = dir == 0 ? 0 : 1;
         const T Ai = dir == 0 ? TA(0, 0).x : TA(0, 0).y;
         const T Aj = dir == 0 ? TA(ox, oy).x : TA(ox, oy).y;
         const T ai = dir == 0 ? dt.A[ly][lx].x : dt.A[ly][lx].y;
         const T aj = dir == 0 ? dt.A[ly + oy][lx + ox].x : dt.A[ly + oy][lx + ox].y;
+        const T wl = dir == 0 ? w.wfx : w.wfy;
 #pragma unroll
         for (int c = 0; c < NC; ++c) {
             const T q = p.q[c];
@@ -335,15 +336,17 @@ __device__ __forceinline__ void site_poly(const Tile<T, NC, TY> &t, const Tile<T
             T t0[4];
             link4(Ai, Aj, pi, pj, q, p.idx, t0);
             const T ddre = (dj.x - di.x) * p.idx, ddim = (dj.y - di.y) * p.idx;
+            const T qAi = q * Ai, qAj = q * Aj, qdai = qd * ai, qdaj = qd * aj;
             T t1[4], t2[4];
-            t1[0] = -ddre - q * Ai * di.y - qd * ai * pi.y;
-            t1[1] = -ddre - q * Aj * dj.y - qd * aj * pj.y;
-            t1[2] = ddim - q * Ai * di.x - qd * ai * pi.x;
-            t1[3] = ddim - q * Aj * dj.x - qd * aj * pj.x;
-            t2[0] = -q * ai * di.y;
-            t2[1] = -q * aj * dj.y;
-            t2[2] = -q * ai * di.x;
-            t2[3] = -q * aj * dj.x;
+            t1[0] = -ddre - qAi * di.y - qdai * pi.y;
+            t1[1] = -ddre - qAj * dj.y - qdaj * pj.y;
+            t1[2] = ddim - qAi * di.x - qdai * pi.x;
+            t1[3] = ddim - qAj * dj.x - qdaj * pj.x;
+            const T qai = q * ai, qaj = q * aj;
+            t2[0] = -qai * di.y;
+            t2[1] = -qaj * dj.y;
+            t2[2] = -qai * di.x;
+            t2[3] = -qaj * dj.x;
             T se = 0, sb = 0, scc = 0, sd = 0, s4 = 0;
 #pragma unroll
             for (int k = 0; k < 4; ++k) {
@@ -353,7 +356,7 @@ __device__ __forceinline__ void site_poly(const Tile<T, NC, TY> &t, const Tile<T
                 sd += t1[k] * t2[k];
                 s4 += t2[k] * t2[k];
             }
-            const T f = (dir == 0 ? p.hmx[c] * cwx : p.hmy[c] * cwy);   // = w / (2 m)
+            const T f = (dir == 0 ? p.hmx[c] : p.hmy[c]) * wl;   // = w / (2 m)
             e += (T)0.5 * se * f;
             b1 += sb * f;
             c2 += scc * f;
@@ -369,28 +372,34 @@ __device__ __forceinline__ void site_poly(const Tile<T, NC, TY> &t, const Tile<T
 }
 
 // B and J at one site (computeJBKernel, nlcg.cu:243-364).
-template <class T, int NC, int TY>
-__device__ __forceinline__ void site_jb(const Tile<T, NC, TY> &t, int lx, int ly, const SiteParams<T> &p, T *out /* 1+2NC */)
+template <class T, int NC, int TYT>
+__device__ __forceinline__ void site_jb(const Tile<T, NC, TYT> &t, int lx, int ly, const SiteParams<T> &p,
+                                        const Wts<T> &w, T *out /* 1+2NC */)
 {
-    const unsigned mk = t.m[ly][lx], cc = mk & 0xffu, sc = mk >> 8;
     const vec2_t<T> A0 = TA(0, 0);
     const T idx = p.idx;
+    const T ayp = (TA(1, 0).y - A0.y) * idx, aym = (A0.y - TA(-1, 0).y) * idx;
+    const T axp = (TA(0, 1).x - A0.x) * idx, axm = (A0.x - TA(0, -1).x) * idx;
     T bb = 0;
-    if (bit(cc, 0) & bit(cc, 1) & bit(cc, 2)) bb += (T)0.25 * ((TA(1, 0).y - A0.y) * idx - (TA(0, 1).x - A0.x) * idx);
-    if (bit(cc, 2) & bit(cc, 3) & bit(cc, 4)) bb += (T)0.25 * ((A0.y - TA(-1, 0).y) * idx - (TA(0, 1).x - A0.x) * idx);
-    if (bit(cc, 4) & bit(cc, 5) & bit(cc, 6)) bb += (T)0.25 * ((A0.y - TA(-1, 0).y) * idx - (A0.x - TA(0, -1).x) * idx);
-    if (bit(cc, 6) & bit(cc, 7) & bit(cc, 0)) bb += (T)0.25 * ((TA(1, 0).y - A0.y) * idx - (A0.x - TA(0, -1).x) * idx);
-    if (bb != (T)0) bb /= (T)area4(cc) * (T)0.25;
+    bb += w.vUR * ((T)0.25 * (ayp - axp));
+    bb += w.vUL * ((T)0.25 * (aym - axp));
+    bb += w.vLL * ((T)0.25 * (aym - axm));
+    bb += w.vLR * ((T)0.25 * (ayp - axm));
+    if (bb != (T)0) bb /= (w.vUR + w.vUL + w.vLL + w.vLR) * (T)0.25;
     out[0] = bb;
 #pragma unroll
     for (int c = 0; c < NC; ++c) {
         const vec2_t<T> P0 = TP(c, 0, 0);
         const T q = p.q[c];
         T jx = 0, jy = 0, u[4];
-        if (bit(sc, 0)) { link4(A0.x, TA(1, 0).x, P0, TP(c, 1, 0), q, idx, u); jx += p.hmx[c] * q * (P0.y * u[0] + P0.x * u[2]); }
-        if (bit(sc, 4)) { link4(TA(-1, 0).x, A0.x, TP(c, -1, 0), P0, q, idx, u); jx += p.hmx[c] * q * (P0.y * u[1] + P0.x * u[3]); }
-        if (bit(sc, 2)) { link4(A0.y, TA(0, 1).y, P0, TP(c, 0, 1), q, idx, u); jy += p.hmy[c] * q * (P0.y * u[0] + P0.x * u[2]); }
-        if (bit(sc, 6)) { link4(TA(0, -1).y, A0.y, TP(c, 0, -1), P0, q, idx, u); jy += p.hmy[c] * q * (P0.y * u[1] + P0.x * u[3]); }
+        link4(A0.x, TA(1, 0).x, P0, TP(c, 1, 0), q, idx, u);
+        jx += w.lfx * (p.hmx[c] * q * (P0.y * u[0] + P0.x * u[2]));
+        link4(TA(-1, 0).x, A0.x, TP(c, -1, 0), P0, q, idx, u);
+        jx += w.lbx * (p.hmx[c] * q * (P0.y * u[1] + P0.x * u[3]));
+        link4(A0.y, TA(0, 1).y, P0, TP(c, 0, 1), q, idx, u);
+        jy += w.lfy * (p.hmy[c] * q * (P0.y * u[0] + P0.x * u[2]));
+        link4(TA(0, -1).y, A0.y, TP(c, 0, -1), P0, q, idx, u);
+        jy += w.lby * (p.hmy[c] * q * (P0.y * u[1] + P0.x * u[3]));
         out[1 + 2 * c] = jx;
         out[2 + 2 * c] = jy;
     }

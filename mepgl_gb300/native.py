@@ -19,7 +19,8 @@ import numpy as np
 
 from .problem import Problem, StringState
 
-LIB_PATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), "_lib", "libmepgl_gb300.so")
+LIB_PATH = os.environ.get("MEPGL_LIB",
+                          os.path.join(os.path.dirname(os.path.abspath(__file__)), "_lib", "libmepgl_gb300.so"))
 
 FP32, FP64 = 0, 1
 HOST, DEVICE = 0, 1

@@ -1,0 +1,35 @@
+"""Small, self-contained NLCG run for profiler captures.
+
+    python -m mepgl_gb300.profile_case [--precision fp32|fp64] [--n 256] [--images 64] [--steps 4]
+
+Builds the two-component benchmark string (default: the full 256x256, 64
+image workload, ~0.6 GB of device state in FP32 -- larger than L2, small for
+a profiler), then runs ``--steps`` NLCG steps launched pass by pass (no CUDA
+graph), so a capture with ``-k regex:k_grad -s <n> -c 1`` sees few launches
+before the one it records.  Prints the per-pass CUDA-event times.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--precision", default="fp32", choices=("fp32", "fp64"))
+    ap.add_argument("--n", type=int, default=256)
+    ap.add_argument("--images", type=int, default=64)
+    ap.add_argument("--steps", type=int, default=4)
+    a = ap.parse_args(argv)
+    from . import native, workloads
+    prob, st = workloads.config2(n=a.n, images=a.images)
+    ctx = native.StringContext(prob, st.n_images, a.precision, use_graphs=0, line_polynomial=native.POLY_EXACT)
+    ctx.set_state(st)
+    ms_grad, ms_dir = ctx.profile_passes(a.steps)
+    fe = ctx.image_scalars()["fenergy"]
+    print(json.dumps({"precision": a.precision, "n": a.n, "images": a.images, "steps": a.steps,
+                      "ms_grad": ms_grad, "ms_dir_poly": ms_dir, "energy0": float(fe[0])}))
+
+
+if __name__ == "__main__":
+    main()

@@ -34,7 +34,7 @@ def build(force: bool = False) -> str:
     os.makedirs(LIB_DIR, exist_ok=True)
     tmp = LIB_PATH + f".{os.getpid()}.tmp"
     subprocess.run([os.environ.get("CC", "gcc"), "-std=c11", "-O2", "-ffp-contract=off", "-fPIC", "-shared",
-                    "-o", tmp, src[0], "-lm"], check=True)
+                    "-fopenmp", "-o", tmp, src[0], "-lm"], check=True)
     os.replace(tmp, LIB_PATH)
     return LIB_PATH
 
@@ -45,6 +45,15 @@ def lib():
         if _lib is None:
             _lib = C.CDLL(build())
     return _lib
+
+
+def threads() -> int:
+    """Host threads the oracle uses (OpenMP over images)."""
+    return int(lib().glo_max_threads())
+
+
+def set_threads(n: int) -> None:
+    lib().glo_set_threads(int(n))
 
 
 _P = C.c_void_p

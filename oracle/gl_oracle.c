@@ -33,6 +33,19 @@
 MEPGL_DEFINE_GTTRF(glo_gttrf_d, double)
 MEPGL_DEFINE_GTTRS(glo_gttrs_d, double)
 
+/* Images are independent in every per-image loop, so they run in parallel
+ * when built with OpenMP; results do not depend on the thread count. */
+#ifdef _OPENMP
+#include <omp.h>
+#define GLO_OMP_FOR _Pragma("omp parallel for schedule(dynamic)")
+int glo_max_threads(void) { return omp_get_max_threads(); }
+void glo_set_threads(int n) { omp_set_num_threads(n); }
+#else
+#define GLO_OMP_FOR
+int glo_max_threads(void) { return 1; }
+void glo_set_threads(int n) { (void)n; }
+#endif
+
 /* Neighbour code of every site (bit order 0:+x 1:+x+y 2:+y 3:-x+y 4:-x
  * 5:-x-y 6:-y 7:+x-y), restating buildNearestNeighbourMap
  * (mepgl/src/nlcg.cu:48-103): a bit is set when both the site and that

@@ -105,6 +105,7 @@ void FN(glo_energy)(const PROB *P, int F, const REAL *A, const REAL *p1, const R
 {
     const REAL *ps[2] = {p1, p2};
     const long M = (long)P->nx * P->ny;
+    GLO_OMP_FOR
     for (int n = 0; n < F; ++n) {
         FN(ksum) acc = {0, 0};
         for (int j = 0; j < P->ny; ++j)
@@ -140,6 +141,7 @@ void FN(glo_gradient)(const PROB *P, int F, const REAL *A, const REAL *p1, const
     const int nx = P->nx;
     const long M = (long)nx * P->ny;
     const REAL dx = P->dx;
+    GLO_OMP_FOR
     for (int n = 0; n < F; ++n)
         for (int j = 0; j < P->ny; ++j)
             for (int i = 0; i < nx; ++i) {
@@ -371,6 +373,7 @@ void FN(glo_polynomial)(const PROB *P, int F, const REAL *A, const REAL *p1, con
 {
     const REAL *ps[2] = {p1, p2}, *ds[2] = {d1, d2};
     const long M = (long)P->nx * P->ny;
+    GLO_OMP_FOR
     for (int n = 0; n < F; ++n) {
         FN(ksum) acc[5] = {{0, 0}, {0, 0}, {0, 0}, {0, 0}, {0, 0}};
         for (int j = 0; j < P->ny; ++j)
@@ -489,6 +492,7 @@ void FN(glo_jb)(const PROB *P, int F, const REAL *A, const REAL *p1, const REAL 
     const int nx = P->nx;
     const long M = (long)nx * P->ny;
     const REAL dx = P->dx;
+    GLO_OMP_FOR
     for (int n = 0; n < F; ++n)
         for (int j = 0; j < P->ny; ++j)
             for (int i = 0; i < nx; ++i) {
@@ -541,6 +545,7 @@ static void FN(arc_finish)(int F, double *s)
 void FN(glo_arc_length)(int F, long M, int nf, const REAL *const *fields, const int *width, double *s)
 {
     s[0] = 0;
+    GLO_OMP_FOR
     for (int n = 1; n < F; ++n) {
         FN(ksum) acc = {0, 0};
         for (long t = 0; t < M; ++t) {
@@ -694,6 +699,7 @@ void FN(glo_solver_nlcg_steps)(FN(glo_solver) *S, int iters, int use_cg, int max
         REAL **g = S->g[cur], **go = S->g[prev];
         FN(glo_gradient)(&S->P, F, S->x[0], S->x[1], S->x[2], g[0], g[1], g[2], maxwell);
         /* gradientDensity (nlcg.cu:919-949); absent components are zero */
+    GLO_OMP_FOR
         for (int n = 0; n < F; ++n) {
             FN(ksum) a = {0, 0}, b = {0, 0};
             for (int c = 0; c < 1 + nc; ++c)
@@ -705,6 +711,7 @@ void FN(glo_solver_nlcg_steps)(FN(glo_solver) *S, int iters, int use_cg, int max
             S->gdg[n] = FN(kval)(&b);
         }
         /* computeStepDirection (nlcg.cu:955-994), Polak-Ribiere clipped at 0 */
+    GLO_OMP_FOR
         for (int n = 0; n < F; ++n) {
             double beta = 0;
             if (use_cg) {
@@ -719,6 +726,7 @@ void FN(glo_solver_nlcg_steps)(FN(glo_solver) *S, int iters, int use_cg, int max
                            S->poly);
         FN(glo_line_search)(F, S->fe, S->poly, S->ls_mode, S->alpha);
         /* updateFields (nlcg.cu:1372-1396) */
+    GLO_OMP_FOR
         for (int n = 0; n < F; ++n) {
             const REAL al = (REAL)S->alpha[n];
             for (int c = 0; c < 1 + nc; ++c)
