@@ -173,6 +173,34 @@ mepgl_status mepgl_info(const mepgl_ctx *ctx, int *n_images, int *precision, int
  * reference has no timing facility); used by the benchmark's roofline. */
 mepgl_status mepgl_profile_passes(mepgl_ctx *ctx, int steps, int use_cg, double *ms_grad, double *ms_dir_poly);
 
+/* Allocation-free free energy.  No counterpart in the reference.  For callers
+ * that cannot allocate device memory -- code running inside someone else's
+ * CUDA-graph capture or memory pool, or an embedding that owns a fixed
+ * device arena -- this evaluates the per-image FP64 free energy of
+ * caller-owned device arrays without a context and without any allocation.
+ * Inputs (all device pointers): comp_code / sc_code are int32 neighbour
+ * codes per site (the layout of the reference's buildNearestNeighbourMap),
+ * the nine parameter arrays are per-site doubles, a / psi_1 / psi_2 are the
+ * F images as double pairs; fenergy receives F doubles.  Scratch for the
+ * reduction lives in fixed device arrays of the library (4 MiB + 16 KiB per
+ * GPU that loads it, kept until the process exits): the string must satisfy
+ * n_images <= 4096 and n_images * ceil(nx/32) * ceil(ny/8) <= 65536, else
+ * MEPGL_ERR_INVALID_ARG.  The first call on a device resolves the scratch
+ * addresses and uploads constant tables; make that first call before any
+ * stream capture.  All calls share the scratch, so calls that overlap on
+ * the GPU (different streams, no ordering) race.  Asynchronous on `stream`
+ * (a cudaStream_t, NULL = default stream).  Errors: mepgl_noalloc_last_error. */
+mepgl_status mepgl_free_energy_noalloc(int nx, int ny, int n_images, int multicomponent, int thin_film, double dx,
+                                       const int32_t *comp_code, const int32_t *sc_code, const double *a_1,
+                                       const double *b_1, const double *m_xx_1, const double *m_yy_1,
+                                       const double *a_2, const double *b_2, const double *m_xx_2,
+                                       const double *m_yy_2, const double *h, double q_1, double q_2, double eta,
+                                       double gamma, double delta, const void *a, const void *psi_1,
+                                       const void *psi_2, double *fenergy, void *stream);
+
+/* Message of the last failed mepgl_free_energy_noalloc on this thread. */
+const char *mepgl_noalloc_last_error(void);
+
 /* Wait for the context's stream. */
 mepgl_status mepgl_synchronize(mepgl_ctx *ctx);
 

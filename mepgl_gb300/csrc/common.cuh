@@ -50,6 +50,7 @@ struct StringDesc {
     Uniform<double> ud;
     const void *pa[2], *pb[2], *pmxx[2], *pmyy[2], *ph;  // per-site (type T)
     const uint16_t *mask;     // per site: comp code | sc code << 8
+    const int32_t *code_comp, *code_sc;   // used when mask is null: int32 codes per site
     void *x[2][3], *g[2][3], *d[2][3];
 
     template <class T> __host__ __device__ const Uniform<T> &u() const;

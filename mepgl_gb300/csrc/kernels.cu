@@ -86,7 +86,9 @@ __device__ __forceinline__ void stage(Tile<T, NC, TYT> &t, const StringDesc &S, 
             uint16_t m = 0;
             if (rowin && gi >= 0 && gi < S.nx) {
                 const int s = gi + S.nx * gj;
-                if (masks) m = S.mask[s];
+                if (masks)
+                    m = S.mask ? S.mask[s]
+                               : (uint16_t)((S.code_comp[s] & 0xff) | ((S.code_sc[s] & 0xff) << 8));
 #pragma unroll
                 for (int c = 0; c < 1 + NC; ++c) {
                     if (MODE == 2) {
@@ -127,6 +129,18 @@ __device__ __forceinline__ void image_ptrs(ImagePtrs<T, NC> &ip, void *const *in
         ip.aux[c] = aux ? static_cast<const vec2_t<T> *>(aux[c]) + off : nullptr;
         ip.out[c] = out ? static_cast<vec2_t<T> *>(out[c]) + off : nullptr;
     }
+}
+
+__device__ __forceinline__ TileRef flat_tile(const StringDesc &S, int tt)
+{
+    const int tpi = S.tiles_x * S.tiles_y, n = tt / tpi, r = tt - n * tpi, ty = r / S.tiles_x;
+    TileRef t;
+    t.s = 0;
+    t.ty = (int16_t)ty;
+    t.tx = (int16_t)(r - ty * S.tiles_x);
+    t.pad = 0;
+    t.n = n;
+    return t;
 }
 
 // Field h at a neighbour (per-site strings only).
@@ -363,7 +377,8 @@ __global__ void __launch_bounds__(NT) k_energy(const __grid_constant__ Batch bt,
     __shared__ Tile<T, NC, TYT> t;
     __shared__ double red[NT / 32];
     for (int tt = blockIdx.x; tt < n_tiles; tt += gridDim.x) {
-        const TileRef tr = tiles[tt];
+        // without a tile table: one string, tiles in (image, row, column) order
+        const TileRef tr = tiles ? tiles[tt] : flat_tile(bt.s[0], tt);
         const StringDesc &S = bt.s[tr.s];
         const int img = S.img_base + tr.n;
         const int i0 = tr.tx * TX, j0 = tr.ty * TYT;
@@ -846,3 +861,147 @@ cudaError_t launch_convert(const void *src, int src_prec, void *dst, int dst_pre
 }
 
 }  // namespace mepgl
+
+// ===================================================== allocation-free energy
+//
+// Some callers cannot allocate device memory: code that runs inside a
+// framework's CUDA-graph capture or a custom memory pool, embedded solvers
+// that own a fixed device arena, or plugins whose host process forbids
+// cudaMalloc after start-up.  mepgl_free_energy_noalloc serves them: it
+// evaluates the per-image free energy of caller-owned device arrays without
+// creating a context and without any allocation.  The per-tile partial sums
+// and per-image tickets of the deterministic reduction live in the fixed
+// arrays below, which every GPU that loads this library holds until the
+// process exits (4 MiB + 16 KiB per device).
+#include <cstring>
+#include <mutex>
+#include <string>
+
+#include "../../include/mepgl.h"
+
+namespace {
+
+constexpr int NOALLOC_MAX_TILES = 65536;     // images x ceil(nx/32) x ceil(ny/8)
+constexpr int NOALLOC_MAX_IMAGES = 4096;
+constexpr int NOALLOC_MAX_DEVICES = 64;
+
+static __device__ __align__(256) double g_noalloc_part[NOALLOC_MAX_TILES * 8];
+static __device__ __align__(256) unsigned g_noalloc_ticket[NOALLOC_MAX_IMAGES];
+
+struct NoallocScratch {
+    bool ready;
+    double *part;
+    unsigned *ticket;
+};
+std::mutex g_noalloc_mu;
+NoallocScratch g_noalloc[NOALLOC_MAX_DEVICES];
+thread_local std::string g_noalloc_err;
+
+// Device addresses of the scratch arrays, resolved once per device with that
+// device current (a host-side reference to the array names is not a device
+// address).  Also uploads the constant neighbour-code tables.
+cudaError_t noalloc_setup(int dev, NoallocScratch *out)
+{
+    std::lock_guard<std::mutex> lk(g_noalloc_mu);
+    NoallocScratch &s = g_noalloc[dev];
+    if (!s.ready) {
+        cudaError_t e = cudaGetSymbolAddress((void **)&s.part, g_noalloc_part);
+        if (e != cudaSuccess) return e;
+        e = cudaGetSymbolAddress((void **)&s.ticket, g_noalloc_ticket);
+        if (e != cudaSuccess) return e;
+        e = mepgl::upload_mask_tables();
+        if (e != cudaSuccess) return e;
+        s.ready = true;
+    }
+    *out = s;
+    return cudaSuccess;
+}
+
+mepgl_status noalloc_fail(mepgl_status st, const std::string &m)
+{
+    g_noalloc_err = m;
+    return st;
+}
+
+}  // namespace
+
+extern "C" const char *mepgl_noalloc_last_error(void) { return g_noalloc_err.c_str(); }
+
+extern "C" mepgl_status mepgl_free_energy_noalloc(int nx, int ny, int n_images, int multicomponent, int thin_film,
+                                                  double dx, const int32_t *comp_code, const int32_t *sc_code,
+                                                  const double *a_1, const double *b_1, const double *m_xx_1,
+                                                  const double *m_yy_1, const double *a_2, const double *b_2,
+                                                  const double *m_xx_2, const double *m_yy_2, const double *h,
+                                                  double q_1, double q_2, double eta, double gamma, double delta,
+                                                  const void *a, const void *psi_1, const void *psi_2,
+                                                  double *fenergy, void *stream)
+{
+    using namespace mepgl;
+    constexpr int rows = MEPGL_ROWS_F64;
+    if (nx < 2 || ny < 2 || n_images < 1 || !(dx > 0))
+        return noalloc_fail(MEPGL_ERR_INVALID_ARG, "need nx, ny >= 2, n_images >= 1, dx > 0");
+    if (!comp_code || !sc_code || !a_1 || !b_1 || !m_xx_1 || !m_yy_1 || !h || !a || !psi_1 || !fenergy ||
+        (multicomponent && (!a_2 || !b_2 || !m_xx_2 || !m_yy_2 || !psi_2)))
+        return noalloc_fail(MEPGL_ERR_INVALID_ARG, "null device pointer");
+    const long tiles_x = (nx + TX - 1) / TX, tiles_y = (ny + rows - 1) / rows;
+    const long n_tiles = tiles_x * tiles_y * n_images;
+    if (n_images > NOALLOC_MAX_IMAGES || n_tiles > NOALLOC_MAX_TILES || (long)nx * ny >= (1L << 31))
+        return noalloc_fail(MEPGL_ERR_INVALID_ARG,
+                            "string too large for the fixed scratch: need n_images <= 4096 and "
+                            "n_images * ceil(nx/32) * ceil(ny/8) <= 65536");
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= NOALLOC_MAX_DEVICES)
+        return noalloc_fail(MEPGL_ERR_CUDA, "no usable current device");
+    NoallocScratch scr;
+    cudaError_t e = noalloc_setup(dev, &scr);
+    if (e != cudaSuccess) return noalloc_fail(MEPGL_ERR_CUDA, std::string("scratch setup: ") + cudaGetErrorString(e));
+
+    Batch bt;
+    memset(&bt, 0, sizeof(bt));
+    bt.n = 1;
+    StringDesc &S = bt.s[0];
+    S.nx = nx;
+    S.ny = ny;
+    S.F = n_images;
+    S.ncomp = multicomponent ? 2 : 1;
+    S.tiles_x = (int)tiles_x;
+    S.tiles_y = (int)tiles_y;
+    S.thin_film = thin_film ? 1 : 0;
+    S.per_site = 1;
+    const double *pa[2] = {a_1, multicomponent ? a_2 : a_1}, *pb[2] = {b_1, multicomponent ? b_2 : b_1};
+    const double *px[2] = {m_xx_1, multicomponent ? m_xx_2 : m_xx_1}, *py[2] = {m_yy_1, multicomponent ? m_yy_2 : m_yy_1};
+    for (int c = 0; c < 2; ++c) {
+        S.pa[c] = pa[c];
+        S.pb[c] = pb[c];
+        S.pmxx[c] = px[c];
+        S.pmyy[c] = py[c];
+    }
+    S.ph = h;
+    S.ud.q[0] = q_1;
+    S.ud.q[1] = q_2;
+    S.ud.eta = eta;
+    S.ud.gamma = gamma;
+    S.ud.delta = delta;
+    S.ud.idx = 1.0 / dx;
+    S.ud.dx2 = dx * dx;
+    S.code_comp = comp_code;
+    S.code_sc = sc_code;
+    S.x[0][0] = const_cast<void *>(a);
+    S.x[0][1] = const_cast<void *>(psi_1);
+    S.x[0][2] = multicomponent ? const_cast<void *>(psi_2) : nullptr;
+    Scalars sc;
+    memset(&sc, 0, sizeof(sc));
+    sc.part = scr.part;
+    sc.ticket = scr.ticket;
+    cudaStream_t st = (cudaStream_t)stream;
+    // the tickets must start at zero; the array keeps the previous call's contents
+    e = cudaMemsetAsync(scr.ticket, 0, sizeof(unsigned) * n_images, st);
+    if (e != cudaSuccess) return noalloc_fail(MEPGL_ERR_CUDA, std::string("ticket reset: ") + cudaGetErrorString(e));
+    if (multicomponent)
+        k_energy<double, 2><<<(unsigned)n_tiles, NT, 0, st>>>(bt, nullptr, (int)n_tiles, sc, 0, fenergy);
+    else
+        k_energy<double, 1><<<(unsigned)n_tiles, NT, 0, st>>>(bt, nullptr, (int)n_tiles, sc, 0, fenergy);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return noalloc_fail(MEPGL_ERR_CUDA, std::string("launch: ") + cudaGetErrorString(e));
+    return MEPGL_OK;
+}

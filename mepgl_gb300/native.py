@@ -76,6 +76,9 @@ _SIGS = {
     "mepgl_info": (C.c_int, [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int64)]),
     "mepgl_synchronize": (C.c_int, [C.c_void_p]),
     "mepgl_profile_passes": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_void_p]),
+    "mepgl_free_energy_noalloc": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_double]
+                                  + [C.c_void_p] * 11 + [C.c_double] * 5 + [C.c_void_p] * 5),
+    "mepgl_noalloc_last_error": (C.c_char_p, []),
 }
 
 
