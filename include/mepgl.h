@@ -145,12 +145,33 @@ mepgl_status mepgl_compute_jb(mepgl_ctx *ctx, void *b, void *j_1, void *j_2, int
 mepgl_status mepgl_arc_length(mepgl_ctx *ctx, int metric, double *s);
 
 /* Reparametrize the string to F_new equidistant images in the context's
- * metric, linear or cubic.  F_new == F keeps the buffers; otherwise the
- * context is resized (the reference's final F_out resample,
- * mepgl/src/mepgl.cu:699-766).  Does NOT restart CG (see mepgl_reset_cg).
- * Replaces redistributeLinear / redistributeCubic
+ * metric, linear or cubic.  F_new == F (or F_new < 0) keeps the buffers;
+ * otherwise the context is resized (the reference's final F_out resample,
+ * mepgl/src/mepgl.cu:699-766; single-string contexts only).  With several
+ * strings and F_new < 0 every string is reparametrized.  Does NOT restart CG
+ * (see mepgl_reset_cg).  Replaces redistributeLinear / redistributeCubic
  * (mepgl/src/interpolation.cu:229-481). */
 mepgl_status mepgl_redistribute(mepgl_ctx *ctx, int kind, int F_new);
+
+/* Batched strings.  No counterpart in the reference, which runs parameter
+ * sweeps as separate processes (mepgl/batch_run.py:9-21).  One context holds
+ * n_strings strings of possibly different lattice size and image count (same
+ * component count, thin-film switch and precision); mepgl_nlcg_steps and
+ * mepgl_iteration advance all of them with the same launches (groups of 16
+ * strings per launch).  The single-string calls above act on string 0; the
+ * calls below address a string by index.  Setting any string's state
+ * restarts the NLCG history of the whole context. */
+mepgl_status mepgl_create_batch(const mepgl_problem *probs, int n_strings, const mepgl_options *opt, void *stream,
+                                mepgl_ctx **out);
+int mepgl_string_count(const mepgl_ctx *ctx);
+mepgl_status mepgl_batch_info(const mepgl_ctx *ctx, int string, int *nx, int *ny, int *n_images);
+mepgl_status mepgl_batch_set_state(mepgl_ctx *ctx, int string, const void *a, const void *psi_1, const void *psi_2,
+                                   int memory);
+mepgl_status mepgl_batch_get_state(mepgl_ctx *ctx, int string, void *a, void *psi_1, void *psi_2, int memory);
+mepgl_status mepgl_batch_free_energy(mepgl_ctx *ctx, int string, double *fenergy);
+mepgl_status mepgl_batch_image_scalars(mepgl_ctx *ctx, int string, double *fenergy, double *g_norm2,
+                                       double *alpha);
+mepgl_status mepgl_batch_arc_length(mepgl_ctx *ctx, int string, int metric, double *s);
 
 /* One outer iteration of the reference's loop() in mode 'S', 'M', 'L' or
  * 'C' (mepgl/src/mepgl.cu:148-303): optional reparametrization + CG restart

@@ -46,7 +46,10 @@ struct mepgl_ctx {
     bool own_stream = false;
     std::vector<StringHost> strings;
     std::vector<StringDesc> hdesc;
-    Batch batch{};                // descriptors passed to every lattice kernel
+    // strings are grouped MAX_STRINGS at a time; each group is one launch per
+    // pass, its descriptors passed by value to the kernels
+    std::vector<Batch> batches;
+    std::vector<int> batch_tile0, batch_ntiles, string_batch;
     TileRef *dtiles = nullptr;
     int n_tiles = 0, total_images = 0;
     std::vector<int> string_tile0, string_ntiles;
@@ -258,24 +261,36 @@ mepgl_status build_layout(mepgl_ctx *c)
     int img = 0;
     c->string_tile0.clear();
     c->string_ntiles.clear();
+    c->batches.clear();
+    c->batch_tile0.clear();
+    c->batch_ntiles.clear();
+    c->string_batch.clear();
     for (size_t si = 0; si < c->strings.size(); ++si) {
+        const int in_batch = (int)(si % MAX_STRINGS);
+        if (in_batch == 0) {
+            c->batches.emplace_back();
+            memset(&c->batches.back(), 0, sizeof(Batch));
+            c->batch_tile0.push_back((int)tiles.size());
+        }
         fill_desc(c, (int)si, img, (int)tiles.size());
         const StringDesc &D = c->hdesc[si];
+        Batch &B = c->batches.back();
+        B.s[in_batch] = D;
+        B.n = in_batch + 1;
+        c->string_batch.push_back((int)c->batches.size() - 1);
         c->string_tile0.push_back((int)tiles.size());
         for (int n = 0; n < D.F; ++n)
             for (int ty = 0; ty < D.tiles_y; ++ty)
                 for (int tx = 0; tx < D.tiles_x; ++tx)
-                    tiles.push_back(TileRef{(int16_t)si, (int16_t)ty, (int16_t)tx, 0, n});
+                    tiles.push_back(TileRef{(int16_t)in_batch, (int16_t)ty, (int16_t)tx, 0, n});
         c->string_ntiles.push_back((int)tiles.size() - c->string_tile0.back());
         img += D.F;
     }
+    for (size_t b = 0; b < c->batches.size(); ++b)
+        c->batch_ntiles.push_back((b + 1 < c->batches.size() ? c->batch_tile0[b + 1] : (int)tiles.size()) -
+                                  c->batch_tile0[b]);
     c->n_tiles = (int)tiles.size();
     c->total_images = img;
-    if (c->hdesc.size() > (size_t)MAX_STRINGS)
-        return fail(c, MEPGL_ERR_UNSUPPORTED, "too many strings in one context");
-    memset(&c->batch, 0, sizeof(c->batch));
-    c->batch.n = (int)c->hdesc.size();
-    for (size_t si = 0; si < c->hdesc.size(); ++si) c->batch.s[si] = c->hdesc[si];
     CK(c, cudaMalloc(&c->dtiles, sizeof(TileRef) * tiles.size()));
     CK(c, cudaMemcpy(c->dtiles, tiles.data(), sizeof(TileRef) * tiles.size(), cudaMemcpyHostToDevice));
     Scalars &S = c->sc;
@@ -338,12 +353,14 @@ mepgl_status reset_history(mepgl_ctx *c)
     return MEPGL_OK;
 }
 
-Launch make_launch(mepgl_ctx *c, int first_tile = 0, int ntiles = -1)
+// Launch covering a whole batch of strings, or (si >= 0) the tiles of one string.
+Launch make_launch(mepgl_ctx *c, int batch, int si = -1)
 {
     Launch L;
-    L.batch = &c->batch;
-    L.tiles = c->dtiles + first_tile;
-    L.n_tiles = ntiles < 0 ? c->n_tiles : ntiles;
+    L.batch = &c->batches[batch];
+    const int t0 = si >= 0 ? c->string_tile0[si] : c->batch_tile0[batch];
+    L.tiles = c->dtiles + t0;
+    L.n_tiles = si >= 0 ? c->string_ntiles[si] : c->batch_ntiles[batch];
     L.grid = L.n_tiles;
     L.precision = c->precision;
     L.ncomp = c->ncomp;
@@ -351,10 +368,12 @@ Launch make_launch(mepgl_ctx *c, int first_tile = 0, int ntiles = -1)
     return L;
 }
 
+Launch string_launch(mepgl_ctx *c, int si) { return make_launch(c, c->string_batch[si], si); }
+
 mepgl_status flush(mepgl_ctx *c)
 {
     if (!c->pending) return MEPGL_OK;
-    CK(c, launch_apply_update(make_launch(c), c->sc, c->hdesc.data(), (int)c->hdesc.size(), c->xi, c->di));
+    CK(c, launch_apply_update(make_launch(c, 0), c->sc, c->hdesc.data(), (int)c->hdesc.size(), c->xi, c->di));
     c->launches += (int64_t)c->strings.size() * (1 + c->ncomp);
     c->pending = false;
     return MEPGL_OK;
@@ -380,12 +399,12 @@ StepFlags step_flags(mepgl_ctx *c, int it, int use_cg, int maxwell)
 mepgl_status one_step(mepgl_ctx *c, int it, int use_cg, int maxwell)
 {
     const StepFlags f = step_flags(c, it, use_cg, maxwell);
-    const Launch L = make_launch(c);
-    CK(c, launch_grad(L, c->sc, f));
-    CK(c, launch_dir_poly(L, c->sc, f));
+    const int nb = (int)c->batches.size();
+    for (int b = 0; b < nb; ++b) CK(c, launch_grad(make_launch(c, b), c->sc, f));
+    for (int b = 0; b < nb; ++b) CK(c, launch_dir_poly(make_launch(c, b), c->sc, f));
     c->xi ^= 1;
     c->di ^= 1;
-    c->launches += 2;
+    c->launches += 2 * nb;
     c->pending = true;
     return MEPGL_OK;
 }
@@ -427,7 +446,7 @@ mepgl_status nlcg_steps(mepgl_ctx *c, int iters, int use_cg, int maxwell)
         if (st != MEPGL_OK) return st;
         for (; it + 1 <= iters; it += 2) {
             CK(c, cudaGraphLaunch(ex, c->stream));
-            c->launches += 4;
+            c->launches += 4 * (int64_t)c->batches.size();
         }
         c->pending = true;
     }
@@ -452,10 +471,10 @@ mepgl_status copy_fields(mepgl_ctx *c, StringHost &s, void *const *dst, const vo
     return MEPGL_OK;
 }
 
-// Arc length of string 0 into c->ds (fields) or c->ds_jb (B, J).
-mepgl_status arc_length(mepgl_ctx *c, int metric, double **where)
+// Arc length of string si into c->ds (fields) or c->ds_jb (B, J).
+mepgl_status arc_length(mepgl_ctx *c, int si, int metric, double **where)
 {
-    StringHost &s = c->strings[0];
+    StringHost &s = c->strings[si];
     mepgl_status st = flush(c);
     if (st != MEPGL_OK) return st;
     const void *fl[3];
@@ -468,7 +487,7 @@ mepgl_status arc_length(mepgl_ctx *c, int metric, double **where)
         // B, J into the spare direction buffer (its contents are not needed)
         void *b[1] = {s.d[c->di ^ 1][0]};
         void *j[1][2] = {{s.d[c->di ^ 1][1], c->ncomp == 2 ? s.d[c->di ^ 1][2] : s.d[c->di ^ 1][1]}};
-        CK(c, launch_jb(make_launch(c, c->string_tile0[0], c->string_ntiles[0]), c->sc, c->xi, b, j));
+        CK(c, launch_jb(string_launch(c, si), c->sc, c->xi, b, j));
         c->launches += 1;
         fl[0] = b[0]; w[0] = 1;
         fl[1] = j[0][0]; w[1] = 2;
@@ -496,18 +515,37 @@ mepgl_status ensure_plan(mepgl_ctx *c, int F, int F_new)
     return MEPGL_OK;
 }
 
+// Reparametrize string si into the spare x buffer.  The caller flips c->xi
+// once every string has been written (all strings share the buffer index).
+mepgl_status redistribute_into_spare(mepgl_ctx *c, int si, int kind);
+mepgl_status ensure_cubic_scratch(mepgl_ctx *c, size_t need);
+
 mepgl_status redistribute(mepgl_ctx *c, int kind, int F_new)
 {
-    if (c->strings.size() != 1) return fail(c, MEPGL_ERR_UNSUPPORTED, "redistribute: single-string contexts only");
+    if (c->strings.size() != 1) {
+        if (F_new >= 0) return fail(c, MEPGL_ERR_UNSUPPORTED, "resizing a string is for single-string contexts");
+        for (size_t si = 0; si < c->strings.size(); ++si) {
+            mepgl_status st = redistribute_into_spare(c, (int)si, kind);
+            if (st != MEPGL_OK) return st;
+        }
+        c->xi ^= 1;
+        return MEPGL_OK;
+    }
     StringHost &s = c->strings[0];
     const int F = s.F;
+    if (F_new < 0 || F_new == F) {
+        mepgl_status st = redistribute_into_spare(c, 0, kind);
+        if (st != MEPGL_OK) return st;
+        c->xi ^= 1;
+        return MEPGL_OK;
+    }
     if (F < 2 || F_new < 2) return fail(c, MEPGL_ERR_INVALID_ARG, "redistribute: need at least 2 images");
     if (kind == MEPGL_REDIST_CUBIC && F < 4)
         return fail(c, MEPGL_ERR_INVALID_ARG, "cubic reparametrization needs at least 4 images");
     double *sp = nullptr;
-    mepgl_status st = arc_length(c, MEPGL_METRIC_FIELDS, &sp);
+    mepgl_status st = arc_length(c, 0, MEPGL_METRIC_FIELDS, &sp);
     if (st != MEPGL_OK) return st;
-    st = arc_length(c, MEPGL_METRIC_JB, &sp);
+    st = arc_length(c, 0, MEPGL_METRIC_JB, &sp);
     if (st != MEPGL_OK) return st;
     double *s_use = c->opt.metric == MEPGL_METRIC_FIELDS ? c->ds : c->ds_jb;
     st = ensure_plan(c, F, F_new);
@@ -516,25 +554,11 @@ mepgl_status redistribute(mepgl_ctx *c, int kind, int F_new)
     CK(c, launch_redist_plan(s_use, F, F_new, cubic, c->opt.spline, c->plan, c->stream));
     c->launches += 1;
     void *target[3] = {};
-    std::vector<void *> fresh;
     const size_t rs = real_size(c->precision);
-    if (F_new == F) {
-        for (int f = 0; f < 1 + c->ncomp; ++f) target[f] = s.x[c->xi ^ 1][f];
-    } else {
-        for (int f = 0; f < 1 + c->ncomp; ++f) {
-            CK(c, cudaMalloc(&target[f], (size_t)F_new * s.M() * 2 * rs));
-            fresh.push_back(target[f]);
-        }
-    }
+    for (int f = 0; f < 1 + c->ncomp; ++f) CK(c, cudaMalloc(&target[f], (size_t)F_new * s.M() * 2 * rs));
     if (cubic) {
-        const size_t need = (size_t)2 * F * s.M() * sizeof(double);
-        if (need > c->cubic_cap) {
-            cudaFree(c->cubic_scratch);
-            c->cubic_scratch = nullptr;
-            c->cubic_cap = 0;
-            CK(c, cudaMalloc(&c->cubic_scratch, need));
-            c->cubic_cap = need;
-        }
+        st = ensure_cubic_scratch(c, (size_t)2 * F * s.M() * sizeof(double));
+        if (st != MEPGL_OK) return st;
     }
     for (int f = 0; f < 1 + c->ncomp; ++f) {
         if (cubic)
@@ -543,10 +567,6 @@ mepgl_status redistribute(mepgl_ctx *c, int kind, int F_new)
         else
             CK(c, launch_redist_linear(c->precision, s.x[c->xi][f], target[f], s.M(), F_new, c->plan, c->stream));
         c->launches += 1;
-    }
-    if (F_new == F) {
-        c->xi ^= 1;
-        return MEPGL_OK;
     }
     // resize: new buffers for F_new images, state moved in, history reset
     CK(c, cudaStreamSynchronize(c->stream));
@@ -563,6 +583,45 @@ mepgl_status redistribute(mepgl_ctx *c, int kind, int F_new)
     st = build_layout(c);
     if (st != MEPGL_OK) return st;
     return reset_history(c);
+}
+
+mepgl_status ensure_cubic_scratch(mepgl_ctx *c, size_t need)
+{
+    if (need <= c->cubic_cap) return MEPGL_OK;
+    cudaFree(c->cubic_scratch);
+    c->cubic_scratch = nullptr;
+    c->cubic_cap = 0;
+    CK(c, cudaMalloc(&c->cubic_scratch, need));
+    c->cubic_cap = need;
+    return MEPGL_OK;
+}
+
+mepgl_status redistribute_into_spare(mepgl_ctx *c, int si, int kind)
+{
+    StringHost &s = c->strings[si];
+    const int F = s.F;
+    if (F < 2) return fail(c, MEPGL_ERR_INVALID_ARG, "redistribute: need at least 2 images");
+    const int cubic = kind == MEPGL_REDIST_CUBIC;
+    if (cubic && F < 4) return fail(c, MEPGL_ERR_INVALID_ARG, "cubic reparametrization needs at least 4 images");
+    double *sp = nullptr;
+    mepgl_status st = arc_length(c, si, MEPGL_METRIC_FIELDS, &sp);
+    if (st == MEPGL_OK) st = arc_length(c, si, MEPGL_METRIC_JB, &sp);
+    if (st == MEPGL_OK) st = ensure_plan(c, F, F);
+    if (st == MEPGL_OK && cubic) st = ensure_cubic_scratch(c, (size_t)2 * F * s.M() * sizeof(double));
+    if (st != MEPGL_OK) return st;
+    double *s_use = c->opt.metric == MEPGL_METRIC_FIELDS ? c->ds : c->ds_jb;
+    CK(c, launch_redist_plan(s_use, F, F, cubic, c->opt.spline, c->plan, c->stream));
+    c->launches += 1;
+    for (int f = 0; f < 1 + c->ncomp; ++f) {
+        if (cubic)
+            CK(c, launch_redist_cubic(c->precision, s.x[c->xi][f], s.x[c->xi ^ 1][f], c->cubic_scratch, s.M(), F, F,
+                                      c->opt.spline, c->plan, c->stream));
+        else
+            CK(c, launch_redist_linear(c->precision, s.x[c->xi][f], s.x[c->xi ^ 1][f], s.M(), F, c->plan,
+                                       c->stream));
+        c->launches += 1;
+    }
+    return MEPGL_OK;
 }
 
 mepgl_status reset_cg(mepgl_ctx *c, int first, int last)
@@ -599,22 +658,36 @@ const char *mepgl_last_error(const mepgl_ctx *c) { return c ? c->err.c_str() : g
 
 mepgl_status mepgl_create(const mepgl_problem *p, const mepgl_options *opt, void *stream, mepgl_ctx **out)
 {
-    if (!p || !out) return fail(nullptr, MEPGL_ERR_INVALID_ARG, "mepgl_create: null argument");
+    return mepgl_create_batch(p, 1, opt, stream, out);
+}
+
+mepgl_status mepgl_create_batch(const mepgl_problem *probs, int n_strings, const mepgl_options *opt, void *stream,
+                                mepgl_ctx **out)
+{
+    if (!probs || !out || n_strings < 1) return fail(nullptr, MEPGL_ERR_INVALID_ARG, "mepgl_create: null argument");
     *out = nullptr;
-    if (p->nx < 2 || p->ny < 2 || p->n_images < 1 || !(p->dx > 0))
-        return fail(nullptr, MEPGL_ERR_INVALID_ARG, "mepgl_create: need nx, ny >= 2, n_images >= 1, dx > 0");
-    if (p->nx > 32767 * TX || p->ny > 32767 * 8 || (long)p->nx * p->ny >= (1L << 31))
-        return fail(nullptr, MEPGL_ERR_INVALID_ARG, "mepgl_create: lattice too large");
+    for (int si = 0; si < n_strings; ++si) {
+        const mepgl_problem *p = &probs[si];
+        if (p->nx < 2 || p->ny < 2 || p->n_images < 1 || !(p->dx > 0))
+            return fail(nullptr, MEPGL_ERR_INVALID_ARG, "mepgl_create: need nx, ny >= 2, n_images >= 1, dx > 0");
+        if (p->nx > 32767 * TX || p->ny > 32767 * 8 || (long)p->nx * p->ny >= (1L << 31))
+            return fail(nullptr, MEPGL_ERR_INVALID_ARG, "mepgl_create: lattice too large");
+        if (p->precision != MEPGL_FP32 && p->precision != MEPGL_FP64)
+            return fail(nullptr, MEPGL_ERR_INVALID_ARG, "mepgl_create: precision must be MEPGL_FP32 or MEPGL_FP64");
+        const double *arr[9] = {p->a_1, p->b_1, p->m_xx_1, p->m_yy_1, p->a_2, p->b_2, p->m_xx_2, p->m_yy_2, p->h};
+        for (int k = 0; k < 9; ++k)
+            if (!arr[k] && !(k >= 4 && k < 8 && !p->multicomponent))
+                return fail(nullptr, MEPGL_ERR_INVALID_ARG, "mepgl_create: missing parameter array");
+        if (!p->comp_domain || !p->sc_domain)
+            return fail(nullptr, MEPGL_ERR_INVALID_ARG, "mepgl_create: missing domain");
+        if (p->multicomponent != probs[0].multicomponent || p->thin_film != probs[0].thin_film ||
+            p->precision != probs[0].precision)
+            return fail(nullptr, MEPGL_ERR_UNSUPPORTED,
+                        "mepgl_create_batch: all strings need the same component count, thin-film switch and precision");
+    }
     if (upload_mask_tables() != cudaSuccess)
         return fail(nullptr, MEPGL_ERR_CUDA, "mepgl_create: cannot upload the neighbour-code tables");
-    if (p->precision != MEPGL_FP32 && p->precision != MEPGL_FP64)
-        return fail(nullptr, MEPGL_ERR_INVALID_ARG, "mepgl_create: precision must be MEPGL_FP32 or MEPGL_FP64");
-    const double *arr[9] = {p->a_1, p->b_1, p->m_xx_1, p->m_yy_1, p->a_2, p->b_2, p->m_xx_2, p->m_yy_2, p->h};
-    for (int k = 0; k < 9; ++k)
-        if (!arr[k] && !(k >= 4 && k < 8 && !p->multicomponent))
-            return fail(nullptr, MEPGL_ERR_INVALID_ARG, "mepgl_create: missing parameter array");
-    if (!p->comp_domain || !p->sc_domain) return fail(nullptr, MEPGL_ERR_INVALID_ARG, "mepgl_create: missing domain");
-
+    const mepgl_problem *p = &probs[0];
     mepgl_ctx *c = new mepgl_ctx();
     if (opt) c->opt = *opt;
     else mepgl_default_options(&c->opt);
@@ -633,29 +706,34 @@ mepgl_status mepgl_create(const mepgl_problem *p, const mepgl_options *opt, void
     int dev = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&c->sm_count, cudaDevAttrMultiProcessorCount, dev);
-    StringHost s;
-    s.nx = p->nx;
-    s.ny = p->ny;
-    s.F = p->n_images;
-    s.dx = p->dx;
-    s.q[0] = p->q_1;
-    s.q[1] = p->q_2;
-    s.eta = p->eta;
-    s.gamma = p->gamma;
-    s.delta = p->delta;
-    const long M = s.M();
-    s.uniform = true;
-    for (int k = 0; k < 9; ++k) {
-        if (arr[k]) s.params[k].assign(arr[k], arr[k] + M);
-        else s.params[k].assign(M, 1.0);
-        for (long i = 1; i < M && s.uniform; ++i)
-            if (s.params[k][i] != s.params[k][0]) s.uniform = false;
+    mepgl_status st = MEPGL_OK;
+    for (int si = 0; si < n_strings && st == MEPGL_OK; ++si) {
+        const mepgl_problem *q = &probs[si];
+        const double *arr[9] = {q->a_1, q->b_1, q->m_xx_1, q->m_yy_1, q->a_2, q->b_2, q->m_xx_2, q->m_yy_2, q->h};
+        StringHost s;
+        s.nx = q->nx;
+        s.ny = q->ny;
+        s.F = q->n_images;
+        s.dx = q->dx;
+        s.q[0] = q->q_1;
+        s.q[1] = q->q_2;
+        s.eta = q->eta;
+        s.gamma = q->gamma;
+        s.delta = q->delta;
+        const long M = s.M();
+        s.uniform = true;
+        for (int k = 0; k < 9; ++k) {
+            if (arr[k]) s.params[k].assign(arr[k], arr[k] + M);
+            else s.params[k].assign(M, 1.0);
+            for (long i = 1; i < M && s.uniform; ++i)
+                if (s.params[k][i] != s.params[k][0]) s.uniform = false;
+        }
+        s.comp.assign(q->comp_domain, q->comp_domain + M);
+        s.sc.assign(q->sc_domain, q->sc_domain + M);
+        c->strings.push_back(std::move(s));
+        st = upload_string_params(c, c->strings.back());
+        if (st == MEPGL_OK) st = alloc_string_buffers(c, c->strings.back());
     }
-    s.comp.assign(p->comp_domain, p->comp_domain + M);
-    s.sc.assign(p->sc_domain, p->sc_domain + M);
-    c->strings.push_back(std::move(s));
-    mepgl_status st = upload_string_params(c, c->strings[0]);
-    if (st == MEPGL_OK) st = alloc_string_buffers(c, c->strings[0]);
     if (st == MEPGL_OK) st = build_layout(c);
     if (st == MEPGL_OK) st = reset_history(c);
     if (st != MEPGL_OK) {
@@ -690,38 +768,67 @@ mepgl_status mepgl_set_state(mepgl_ctx *c, const void *a, const void *psi_1, con
 {
     if (!c || !a || !psi_1 || (c->ncomp == 2 && !psi_2))
         return fail(c, MEPGL_ERR_INVALID_ARG, "mepgl_set_state: null field");
-    StringHost &s = c->strings[0];
-    c->xi = 0;
-    c->di = 0;
-    void *dst[3] = {s.x[0][0], s.x[0][1], s.x[0][2]};
+    return mepgl_batch_set_state(c, 0, a, psi_1, psi_2, memory);
+}
+
+mepgl_status mepgl_batch_set_state(mepgl_ctx *c, int string, const void *a, const void *psi_1, const void *psi_2,
+                                   int memory)
+{
+    if (!c || string < 0 || string >= (int)c->strings.size() || !a || !psi_1 || (c->ncomp == 2 && !psi_2))
+        return fail(c, MEPGL_ERR_INVALID_ARG, "mepgl_batch_set_state: bad string index or null field");
+    mepgl_status st = flush(c);
+    if (st != MEPGL_OK) return st;
+    StringHost &s = c->strings[string];
+    void *dst[3] = {s.x[c->xi][0], s.x[c->xi][1], s.x[c->xi][2]};
     const void *src[3] = {a, psi_1, psi_2};
-    mepgl_status st = copy_fields(c, s, dst, src, memory, true);
+    st = copy_fields(c, s, dst, src, memory, true);
     if (st != MEPGL_OK) return st;
     return reset_history(c);
 }
 
 mepgl_status mepgl_get_state(mepgl_ctx *c, void *a, void *psi_1, void *psi_2, int memory)
 {
-    if (!c) return MEPGL_ERR_INVALID_ARG;
+    return mepgl_batch_get_state(c, 0, a, psi_1, psi_2, memory);
+}
+
+mepgl_status mepgl_batch_get_state(mepgl_ctx *c, int string, void *a, void *psi_1, void *psi_2, int memory)
+{
+    if (!c || string < 0 || string >= (int)c->strings.size())
+        return fail(c, MEPGL_ERR_INVALID_ARG, "mepgl_batch_get_state: bad string index");
     mepgl_status st = flush(c);
     if (st != MEPGL_OK) return st;
-    StringHost &s = c->strings[0];
+    StringHost &s = c->strings[string];
     void *dst[3] = {a, psi_1, psi_2};
     const void *src[3] = {s.x[c->xi][0], s.x[c->xi][1], s.x[c->xi][2]};
     return copy_fields(c, s, dst, src, memory, false);
 }
 
-mepgl_status mepgl_free_energy(mepgl_ctx *c, double *fenergy)
+mepgl_status mepgl_free_energy(mepgl_ctx *c, double *fenergy) { return mepgl_batch_free_energy(c, 0, fenergy); }
+
+mepgl_status mepgl_batch_free_energy(mepgl_ctx *c, int string, double *fenergy)
 {
-    if (!c || !fenergy) return fail(c, MEPGL_ERR_INVALID_ARG, "mepgl_free_energy: null argument");
+    if (!c || !fenergy || string < 0 || string >= (int)c->strings.size())
+        return fail(c, MEPGL_ERR_INVALID_ARG, "mepgl_free_energy: null argument or bad string index");
     mepgl_status st = flush(c);
     if (st != MEPGL_OK) return st;
-    CK(c, launch_energy(make_launch(c), c->sc, c->xi, c->dscratch));
+    CK(c, launch_energy(string_launch(c, string), c->sc, c->xi, c->dscratch));
     c->launches += 1;
-    CK(c, cudaMemcpyAsync(fenergy, c->dscratch, c->strings[0].F * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    CK(c, cudaMemcpyAsync(fenergy, c->dscratch + c->hdesc[string].img_base, c->strings[string].F * sizeof(double),
+                          cudaMemcpyDeviceToHost, c->stream));
     CK(c, cudaStreamSynchronize(c->stream));
     return MEPGL_OK;
 }
+
+mepgl_status mepgl_batch_info(const mepgl_ctx *c, int string, int *nx, int *ny, int *n_images)
+{
+    if (!c || string < 0 || string >= (int)c->strings.size()) return MEPGL_ERR_INVALID_ARG;
+    if (nx) *nx = c->strings[string].nx;
+    if (ny) *ny = c->strings[string].ny;
+    if (n_images) *n_images = c->strings[string].F;
+    return MEPGL_OK;
+}
+
+int mepgl_string_count(const mepgl_ctx *c) { return c ? (int)c->strings.size() : 0; }
 
 mepgl_status mepgl_energy_grad(mepgl_ctx *c, double *fenergy, void *g_a, void *g_psi_1, void *g_psi_2, int memory)
 {
@@ -742,7 +849,7 @@ mepgl_status mepgl_energy_grad(mepgl_ctx *c, double *fenergy, void *g_a, void *g
         out.p[1] = g_psi_1;
         out.p[2] = c->ncomp == 2 ? g_psi_2 : nullptr;
     }
-    CK(c, launch_gradient_only(make_launch(c), c->xi, out, 0));
+    CK(c, launch_gradient_only(string_launch(c, 0), c->xi, out, 0));
     c->launches += 1;
     if (direct) {
         CK(c, cudaStreamSynchronize(c->stream));
@@ -767,12 +874,17 @@ mepgl_status mepgl_reset_cg(mepgl_ctx *c, int first_image, int last_image)
 
 mepgl_status mepgl_image_scalars(mepgl_ctx *c, double *fenergy, double *g_norm2, double *alpha)
 {
-    if (!c) return MEPGL_ERR_INVALID_ARG;
-    const int F = c->strings[0].F;
-    if (fenergy) CK(c, cudaMemcpyAsync(fenergy, c->sc.fenergy, F * 8, cudaMemcpyDeviceToHost, c->stream));
+    return mepgl_batch_image_scalars(c, 0, fenergy, g_norm2, alpha);
+}
+
+mepgl_status mepgl_batch_image_scalars(mepgl_ctx *c, int string, double *fenergy, double *g_norm2, double *alpha)
+{
+    if (!c || string < 0 || string >= (int)c->strings.size()) return fail(c, MEPGL_ERR_INVALID_ARG, "bad string");
+    const int F = c->strings[string].F, o = c->hdesc[string].img_base;
+    if (fenergy) CK(c, cudaMemcpyAsync(fenergy, c->sc.fenergy + o, F * 8, cudaMemcpyDeviceToHost, c->stream));
     // loop()'s g_norm2 is the slot nlcgSteps writes on even substeps
-    if (g_norm2) CK(c, cudaMemcpyAsync(g_norm2, c->sc.gn0, F * 8, cudaMemcpyDeviceToHost, c->stream));
-    if (alpha) CK(c, cudaMemcpyAsync(alpha, c->sc.alpha, F * 8, cudaMemcpyDeviceToHost, c->stream));
+    if (g_norm2) CK(c, cudaMemcpyAsync(g_norm2, c->sc.gn0 + o, F * 8, cudaMemcpyDeviceToHost, c->stream));
+    if (alpha) CK(c, cudaMemcpyAsync(alpha, c->sc.alpha + o, F * 8, cudaMemcpyDeviceToHost, c->stream));
     CK(c, cudaStreamSynchronize(c->stream));
     return MEPGL_OK;
 }
@@ -785,7 +897,7 @@ mepgl_status mepgl_compute_jb(mepgl_ctx *c, void *b, void *j_1, void *j_2, int m
     StringHost &s = c->strings[0];
     void *bb[1] = {s.d[c->di ^ 1][0]};
     void *jj[1][2] = {{s.d[c->di ^ 1][1], c->ncomp == 2 ? s.d[c->di ^ 1][2] : s.d[c->di ^ 1][1]}};
-    CK(c, launch_jb(make_launch(c), c->sc, c->xi, bb, jj));
+    CK(c, launch_jb(string_launch(c, 0), c->sc, c->xi, bb, jj));
     c->launches += 1;
     const size_t rs = real_size(c->precision), n = (size_t)s.F * s.M();
     const cudaMemcpyKind k = memory == MEPGL_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
@@ -798,11 +910,17 @@ mepgl_status mepgl_compute_jb(mepgl_ctx *c, void *b, void *j_1, void *j_2, int m
 
 mepgl_status mepgl_arc_length(mepgl_ctx *c, int metric, double *s)
 {
-    if (!c || !s) return fail(c, MEPGL_ERR_INVALID_ARG, "mepgl_arc_length: null argument");
+    return mepgl_batch_arc_length(c, 0, metric, s);
+}
+
+mepgl_status mepgl_batch_arc_length(mepgl_ctx *c, int string, int metric, double *s)
+{
+    if (!c || !s || string < 0 || string >= (int)c->strings.size())
+        return fail(c, MEPGL_ERR_INVALID_ARG, "mepgl_arc_length: null argument or bad string index");
     double *where = nullptr;
-    mepgl_status st = arc_length(c, metric, &where);
+    mepgl_status st = arc_length(c, string, metric, &where);
     if (st != MEPGL_OK) return st;
-    CK(c, cudaMemcpyAsync(s, where, c->strings[0].F * 8, cudaMemcpyDeviceToHost, c->stream));
+    CK(c, cudaMemcpyAsync(s, where, c->strings[string].F * 8, cudaMemcpyDeviceToHost, c->stream));
     CK(c, cudaStreamSynchronize(c->stream));
     return MEPGL_OK;
 }
@@ -833,10 +951,13 @@ mepgl_status mepgl_iteration(mepgl_ctx *c, char mode, int relaxation_steps, int 
     case 'M': return mepgl_nlcg_steps(c, relaxation_steps, use_cg, 1);
     case 'L':
     case 'C': {
-        const int F = c->strings[0].F;
-        st = mepgl_redistribute(c, mode == 'L' ? MEPGL_REDIST_LINEAR : MEPGL_REDIST_CUBIC, F);
+        // every string is reparametrized, then its interior images restart CG
+        st = mepgl_redistribute(c, mode == 'L' ? MEPGL_REDIST_LINEAR : MEPGL_REDIST_CUBIC, -1);
         if (st != MEPGL_OK) return st;
-        st = reset_cg(c, 1, F - 1 > 1 ? F - 1 : 1);
+        for (size_t si = 0; si < c->strings.size() && st == MEPGL_OK; ++si) {
+            const int F = c->strings[si].F, o = c->hdesc[si].img_base;
+            st = reset_cg(c, o + 1, F - 1 > 1 ? o + F - 1 : o + 1);
+        }
         if (st != MEPGL_OK) return st;
         return mepgl_nlcg_steps(c, relaxation_steps, use_cg, 0);
     }
@@ -897,17 +1018,17 @@ mepgl_status mepgl_profile_passes(mepgl_ctx *c, int steps, int use_cg, double *m
     if (!c || steps < 1) return fail(c, MEPGL_ERR_INVALID_ARG, "mepgl_profile_passes: steps must be >= 1");
     std::vector<cudaEvent_t> ev(2 * steps + 1);
     for (auto &e : ev) CK(c, cudaEventCreate(&e));
-    const Launch L = make_launch(c);
+    const int nb = (int)c->batches.size();
     CK(c, cudaEventRecord(ev[0], c->stream));
     for (int it = 1; it <= steps; ++it) {
         const StepFlags f = step_flags(c, it, use_cg ? 1 : 0, 0);
-        CK(c, launch_grad(L, c->sc, f));
+        for (int b = 0; b < nb; ++b) CK(c, launch_grad(make_launch(c, b), c->sc, f));
         CK(c, cudaEventRecord(ev[2 * it - 1], c->stream));
-        CK(c, launch_dir_poly(L, c->sc, f));
+        for (int b = 0; b < nb; ++b) CK(c, launch_dir_poly(make_launch(c, b), c->sc, f));
         CK(c, cudaEventRecord(ev[2 * it], c->stream));
         c->xi ^= 1;
         c->di ^= 1;
-        c->launches += 2;
+        c->launches += 2 * nb;
         c->pending = true;
     }
     CK(c, cudaEventSynchronize(ev[2 * steps]));

@@ -131,6 +131,13 @@ __device__ __forceinline__ void image_ptrs(ImagePtrs<T, NC> &ip, void *const *in
     }
 }
 
+// Slot of a tile's partial sums: the global tile index of (string, image, row,
+// column), independent of which launch (whole batch or one string) covers it.
+__device__ __forceinline__ int part_slot(const StringDesc &S, const TileRef &tr)
+{
+    return S.tile_base + (tr.n * S.tiles_y + tr.ty) * S.tiles_x + tr.tx;
+}
+
 __device__ __forceinline__ TileRef flat_tile(const StringDesc &S, int tt)
 {
     const int tpi = S.tiles_x * S.tiles_y, n = tt / tpi, r = tt - n * tpi, ty = r / S.tiles_x;
@@ -291,7 +298,7 @@ __global__ void __launch_bounds__(NT, MEPGL_MINB_GRAD) k_grad(const __grid_const
         }
         const int tpi = S.tiles_x * S.tiles_y;
         double tot[2];
-        if (finish_image<2>(v, red, sc, tt, S.tile_base + tr.n * tpi, tpi, img, tot) && threadIdx.x == 0) {
+        if (finish_image<2>(v, red, sc, part_slot(S, tr), S.tile_base + tr.n * tpi, tpi, img, tot) && threadIdx.x == 0) {
             (f.gcur ? sc.gn1 : sc.gn0)[img] = tot[0];
             sc.gdg[img] = tot[1];
             double beta = 0.0;
@@ -346,7 +353,7 @@ __global__ void __launch_bounds__(NT, MEPGL_MINB_DIR) k_dir_poly(const __grid_co
         }
         const int tpi = S.tiles_x * S.tiles_y;
         double tot[5];
-        if (finish_image<5>(v, red, sc, tt, S.tile_base + tr.n * tpi, tpi, img, tot)) {
+        if (finish_image<5>(v, red, sc, part_slot(S, tr), S.tile_base + tr.n * tpi, tpi, img, tot)) {
             if (threadIdx.x == 0) {
 #pragma unroll
                 for (int k = 0; k < 5; ++k) coef[k] = tot[k];
@@ -402,7 +409,7 @@ __global__ void __launch_bounds__(NT) k_energy(const __grid_constant__ Batch bt,
         }
         const int tpi = S.tiles_x * S.tiles_y;
         double tot[1];
-        if (finish_image<1>(v, red, sc, tt, S.tile_base + tr.n * tpi, tpi, img, tot) && threadIdx.x == 0)
+        if (finish_image<1>(v, red, sc, part_slot(S, tr), S.tile_base + tr.n * tpi, tpi, img, tot) && threadIdx.x == 0)
             out[img] = tot[0];
         __syncthreads();
     }

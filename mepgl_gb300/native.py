@@ -79,6 +79,15 @@ _SIGS = {
     "mepgl_free_energy_noalloc": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_double]
                                   + [C.c_void_p] * 11 + [C.c_double] * 5 + [C.c_void_p] * 5),
     "mepgl_noalloc_last_error": (C.c_char_p, []),
+    "mepgl_create_batch": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.POINTER(C.c_void_p)]),
+    "mepgl_string_count": (C.c_int, [C.c_void_p]),
+    "mepgl_batch_info": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int),
+                                   C.POINTER(C.c_int)]),
+    "mepgl_batch_set_state": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int]),
+    "mepgl_batch_get_state": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int]),
+    "mepgl_batch_free_energy": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p]),
+    "mepgl_batch_image_scalars": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "mepgl_batch_arc_length": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_void_p]),
 }
 
 
@@ -119,30 +128,35 @@ def default_options(**kw) -> MepglOptions:
     return o
 
 
+def _fill_problem(p: MepglProblem, prob: Problem, n_images: int, prec: int, keep: list):
+    """Fill one mepgl_problem; `keep` holds the host arrays alive until create returns."""
+    prob.validate()
+
+    def arr(x, dt=np.float64):
+        a = np.ascontiguousarray(x, dtype=dt)
+        keep.append(a)
+        return a.ctypes.data
+
+    p.nx, p.ny, p.n_images = prob.nx, prob.ny, int(n_images)
+    p.multicomponent, p.thin_film, p.precision = int(prob.multicomponent), int(prob.thin_film), prec
+    p.dx, p.q_1, p.q_2, p.eta, p.gamma, p.delta = prob.dx, prob.q_1, prob.q_2, prob.eta, prob.gamma, prob.delta
+    for n in ("a_1", "b_1", "m_xx_1", "m_yy_1", "a_2", "b_2", "m_xx_2", "m_yy_2", "h"):
+        setattr(p, n, arr(getattr(prob, n)))
+    p.comp_domain = arr(prob.comp_domain, np.int32)
+    p.sc_domain = arr(prob.sc_domain, np.int32)
+
+
 class StringContext:
     """One string on the GPU: the drop-in for the reference's engine state."""
 
     def __init__(self, prob: Problem, n_images: int, precision: str = "fp64", stream=None, **options):
-        prob.validate()
         self.L = lib()
         self.prob = prob
         self.prec = FP64 if precision == "fp64" else FP32
         self.dtype = np.float64 if self.prec == FP64 else np.float32
         keep = []
-
-        def arr(x, dt=np.float64):
-            a = np.ascontiguousarray(x, dtype=dt)
-            keep.append(a)
-            return a.ctypes.data
-
         p = MepglProblem()
-        p.nx, p.ny, p.n_images = prob.nx, prob.ny, int(n_images)
-        p.multicomponent, p.thin_film, p.precision = int(prob.multicomponent), int(prob.thin_film), self.prec
-        p.dx, p.q_1, p.q_2, p.eta, p.gamma, p.delta = prob.dx, prob.q_1, prob.q_2, prob.eta, prob.gamma, prob.delta
-        for n in ("a_1", "b_1", "m_xx_1", "m_yy_1", "a_2", "b_2", "m_xx_2", "m_yy_2", "h"):
-            setattr(p, n, arr(getattr(prob, n)))
-        p.comp_domain = arr(prob.comp_domain, np.int32)
-        p.sc_domain = arr(prob.sc_domain, np.int32)
+        _fill_problem(p, prob, n_images, self.prec, keep)
         self.options = default_options(**options)
         h = C.c_void_p()
         st = self.L.mepgl_create(C.byref(p), C.byref(self.options),
@@ -280,3 +294,89 @@ class StringContext:
 
     def synchronize(self):
         self._check(self.L.mepgl_synchronize(self.h))
+
+
+class StringBatch(StringContext):
+    """Several independent strings advanced by the same launches.
+
+    The reference runs a parameter sweep as one process per string
+    (mepgl/batch_run.py:9-21); here the strings share one context and every
+    NLCG step covers all of them.  ``problems[k]`` with ``n_images[k]`` images
+    is string ``k``; the per-string calls take that index.  Whole-context
+    calls (``nlcg_steps``, ``loop_iteration``, ``set_precision``,
+    ``redistribute_*`` without a new image count) act on every string.
+    """
+
+    def __init__(self, problems, n_images, precision: str = "fp64", stream=None, **options):
+        self.L = lib()
+        self.problems = list(problems)
+        if isinstance(n_images, int):
+            n_images = [n_images] * len(self.problems)
+        self.Fs = [int(f) for f in n_images]
+        if len(self.Fs) != len(self.problems) or not self.problems:
+            raise ValueError("need one image count per problem")
+        self.prob = self.problems[0]
+        self.prec = FP64 if precision == "fp64" else FP32
+        self.dtype = np.float64 if self.prec == FP64 else np.float32
+        keep = []
+        arr = (MepglProblem * len(self.problems))()
+        for k, (pr, F) in enumerate(zip(self.problems, self.Fs)):
+            _fill_problem(arr[k], pr, F, self.prec, keep)
+        self.options = default_options(**options)
+        h = C.c_void_p()
+        st = self.L.mepgl_create_batch(arr, len(self.problems), C.byref(self.options),
+                                       None if stream is None else C.c_void_p(int(stream)), C.byref(h))
+        if st != 0:
+            raise MepglError(st, self.L.mepgl_last_error(None).decode())
+        self.h = h
+        self.F = self.Fs[0]
+
+    def __len__(self):
+        return self.L.mepgl_string_count(self.h)
+
+    def _shape_of(self, k):
+        pr = self.problems[k]
+        return (self.Fs[k], pr.ny, pr.nx, 2)
+
+    def set_string_state(self, k: int, state: StringState):
+        a = np.ascontiguousarray(state.a, self.dtype)
+        p1 = np.ascontiguousarray(state.psi_1, self.dtype)
+        p2 = np.ascontiguousarray(state.psi_2, self.dtype) if self.ncomp == 2 else None
+        if a.shape != self._shape_of(k):
+            raise ValueError(f"state shape {a.shape} != {self._shape_of(k)}")
+        self._check(self.L.mepgl_batch_set_state(self.h, int(k), _ptr(a), _ptr(p1), _ptr(p2), HOST))
+
+    def get_string_state(self, k: int) -> StringState:
+        shp = self._shape_of(k)
+        a, p1 = np.empty(shp, self.dtype), np.empty(shp, self.dtype)
+        p2 = np.empty(shp, self.dtype) if self.ncomp == 2 else None
+        self._check(self.L.mepgl_batch_get_state(self.h, int(k), _ptr(a), _ptr(p1), _ptr(p2), HOST))
+        return StringState(a=a, psi_1=p1, psi_2=p2)
+
+    def string_free_energy(self, k: int) -> np.ndarray:
+        out = np.zeros(self.Fs[k])
+        self._check(self.L.mepgl_batch_free_energy(self.h, int(k), _ptr(out)))
+        return out
+
+    def string_scalars(self, k: int):
+        F = self.Fs[k]
+        fe, gn, al = np.zeros(F), np.zeros(F), np.zeros(F)
+        self._check(self.L.mepgl_batch_image_scalars(self.h, int(k), _ptr(fe), _ptr(gn), _ptr(al)))
+        return dict(fenergy=fe, g_norm2=gn, alpha=al)
+
+    def string_arc_length(self, k: int, metric: int = METRIC_FIELDS) -> np.ndarray:
+        s = np.zeros(self.Fs[k])
+        self._check(self.L.mepgl_batch_arc_length(self.h, int(k), int(metric), _ptr(s)))
+        return s
+
+    def string_info(self, k: int):
+        nx, ny, F = C.c_int(), C.c_int(), C.c_int()
+        self._check(self.L.mepgl_batch_info(self.h, int(k), C.byref(nx), C.byref(ny), C.byref(F)))
+        return dict(nx=nx.value, ny=ny.value, n_images=F.value)
+
+    def redistribute(self, kind: int, n_new: int | None = None):
+        if n_new is not None and len(self.problems) > 1:
+            raise ValueError("a batch of strings keeps its image counts; resample one string at a time")
+        self._check(self.L.mepgl_redistribute(self.h, int(kind), -1 if n_new is None else int(n_new)))
+        if n_new is not None:
+            self.Fs[0] = self.F = int(n_new)
