@@ -44,7 +44,8 @@ typedef enum mepgl_status {
 
 enum { MEPGL_FP32 = 0, MEPGL_FP64 = 1 };          /* working precision of the fields  */
 enum { MEPGL_HOST = 0, MEPGL_DEVICE = 1 };        /* where a caller buffer lives      */
-enum { MEPGL_LS_COMPAT = 0, MEPGL_LS_EXACT = 1 }; /* step: geometric scan | minimiser */
+enum { MEPGL_LS_COMPAT = 0, MEPGL_LS_EXACT = 1 }; /* step: geometric scan | its exact
+                                                     first local minimum     */
 enum { MEPGL_POLY_COMPAT = 0, MEPGL_POLY_EXACT = 1 };       /* line polynomial        */
 enum { MEPGL_SPLINE_COMPAT = 0, MEPGL_SPLINE_FMM = 1 };     /* cubic evaluation       */
 enum { MEPGL_METRIC_FIELDS = 0, MEPGL_METRIC_JB = 1 };      /* arc-length metric      */
@@ -134,6 +135,15 @@ mepgl_status mepgl_reset_cg(mepgl_ctx *ctx, int first_image, int last_image);
  * NULL skips): energy before the step's update, |g|^2 of the slot the
  * reference's loop() reads, and the step length alpha. */
 mepgl_status mepgl_image_scalars(mepgl_ctx *ctx, double *fenergy, double *g_norm2, double *alpha);
+
+/* Parameter adjoints (no reference counterpart): per image (host arrays of
+ * F doubles, NULL skips) the partial derivatives of the free energy at the
+ * current, fixed fields with respect to a uniform shift of the applied field
+ * h (dF/dH), to eta and to gamma.  At a stationary image (a converged end
+ * state) they are the total derivatives of its energy (envelope theorem). */
+mepgl_status mepgl_param_adjoint(mepgl_ctx *ctx, double *dF_dH, double *dF_deta, double *dF_dgamma);
+mepgl_status mepgl_batch_param_adjoint(mepgl_ctx *ctx, int string, double *dF_dH, double *dF_deta,
+                                       double *dF_dgamma);
 
 /* B (F*nx*ny reals) and J_1, J_2 (pairs) of the current state; NULL skips.
  * Replaces computeJB (mepgl/src/nlcg.cu:366-380). */

@@ -1,0 +1,110 @@
+"""Barrier and end-state convergence of the string method on the GPU.
+
+One run = ``iterations`` outer iterations of loop() in mode L or C (one
+reparametrization + ``relax`` NLCG steps, mepgl/src/mepgl.cu:148-303) on a
+seeded workload, recording after each iteration the wall time, the barrier
+estimate dF = max_n F_n - F_0 (mepgl/post.py:188), its argmax image and the
+end-state difference F_{F-1} - F_0.  Schedules:
+
+* ``fp64`` / ``fp32``: one precision throughout;
+* ``mixed``: FP32 for ``--fp32-iterations`` outer iterations, then FP64.
+
+The summary gives the final values, the spread (max - min) of each quantity
+over the final tenth of the run and, when ``--target-ends`` is given, the
+time after which F_{F-1} - F_0 stays within ``--rtol`` of it.
+
+    python -m mepgl_gb300.barrier --config 2 --relax 100 --iterations 250 \
+        --schedule fp64 --out gpurun_out/barrier_c2_fp64.json
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import time
+
+import numpy as np
+
+from . import native, workloads
+
+
+def _workload(cfg: int):
+    if cfg == 1:
+        return workloads.config1()
+    if cfg == 2:
+        return workloads.config2()
+    raise SystemExit("--config must be 1 or 2")
+
+
+def time_within(t, v, target, rtol):
+    """First time after which |v - target| <= rtol |target| for the rest of the run."""
+    ok = np.abs(np.asarray(v) - target) <= rtol * abs(target)
+    bad = np.nonzero(~ok)[0]
+    k = 0 if bad.size == 0 else bad[-1] + 1
+    return None if k >= len(t) else float(t[k])
+
+
+def run(cfg: int, relax: int, iterations: int, schedule: str = "fp64", fp32_iterations: int = 0,
+        mode: str = "L"):
+    prob, st = _workload(cfg)
+    prec = "fp32" if schedule in ("fp32", "mixed") else "fp64"
+    c = native.StringContext(prob, st.n_images, prec, line_polynomial=native.POLY_EXACT,
+                             line_search=native.LS_EXACT, spline=native.SPLINE_FMM)
+    c.set_state(st)
+    c.synchronize()
+    rec = []
+    t0 = time.perf_counter()
+    for it in range(iterations):
+        if schedule == "mixed" and it == fp32_iterations:
+            c.set_precision("fp64")
+        c.loop_iteration(mode, relax)
+        fe = c.compute_free_energy()
+        rec.append((time.perf_counter() - t0, float(fe.max() - fe[0]), int(fe.argmax()), float(fe[-1] - fe[0]),
+                    c.info()["precision"]))
+    # envelope-theorem sensitivities of the final string: dF/dH of the max
+    # image and of the last image, minus that of image 0 (exact where the
+    # images are stationary; the max image of a discrete string is not)
+    adj = c.param_adjoint()
+    k = int(np.argmax(c.compute_free_energy()))
+    sens = dict(dbarrier_dH=float(adj[k, 0] - adj[0, 0]), dends_dH=float(adj[-1, 0] - adj[0, 0]))
+    c.close()
+    return rec, sens
+
+
+def summarise(rec, target_ends=None, rtol=1e-6):
+    t = np.array([r[0] for r in rec])
+    dF = np.array([r[1] for r in rec])
+    ends = np.array([r[3] for r in rec])
+    k = max(3, len(rec) // 10)
+    out = dict(iterations=len(rec), wall_s=float(t[-1]), barrier=float(dF[-1]), argmax=int(rec[-1][2]),
+               barrier_spread=float(np.ptp(dF[-k:])), ends=float(ends[-1]), ends_spread=float(np.ptp(ends[-k:])))
+    if target_ends is not None:
+        out["target_ends"] = target_ends
+        out["rtol"] = rtol
+        out["time_to_ends_s"] = time_within(t, ends, target_ends, rtol)
+    return out
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser(description=__doc__.split("\n\n")[0])
+    ap.add_argument("--config", type=int, default=1)
+    ap.add_argument("--relax", type=int, default=10)
+    ap.add_argument("--iterations", type=int, default=1000)
+    ap.add_argument("--schedule", choices=("fp64", "fp32", "mixed"), default="fp64")
+    ap.add_argument("--fp32-iterations", type=int, default=0)
+    ap.add_argument("--mode", choices=("L", "C"), default="L")
+    ap.add_argument("--target-ends", type=float, default=None)
+    ap.add_argument("--rtol", type=float, default=1e-6)
+    ap.add_argument("--out", default=None)
+    a = ap.parse_args(argv)
+    rec, sens = run(a.config, a.relax, a.iterations, a.schedule, a.fp32_iterations, a.mode)
+    s = summarise(rec, a.target_ends, a.rtol)
+    s.update(sens)
+    s.update(config=a.config, relax=a.relax, schedule=a.schedule, fp32_iterations=a.fp32_iterations, mode=a.mode)
+    print(json.dumps(s))
+    if a.out:
+        with open(a.out, "w") as f:
+            json.dump(dict(summary=s, trace=rec), f)
+
+
+if __name__ == "__main__":
+    main()

@@ -21,8 +21,8 @@ LIB = os.path.join(LIB_DIR, "libmepgl_gb300.so")
 CLI = os.path.join(LIB_DIR, "mepgl")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
-              "-Xptxas", "-warn-spills"]
+NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-Werror=return-type",
+              "--diag-error=940", "--expt-relaxed-constexpr", "-Xptxas", "-warn-spills"]
 CU_SOURCES = ["kernels.cu", "api.cu"]
 HEADERS = ["common.cuh", "site_ops.cuh", "kernels.cuh"]
 

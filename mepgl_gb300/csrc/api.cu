@@ -54,7 +54,7 @@ struct mepgl_ctx {
     int n_tiles = 0, total_images = 0;
     std::vector<int> string_tile0, string_ntiles;
     Scalars sc{};
-    double *dscratch = nullptr;   // per-image temporaries (energies)
+    double *dscratch = nullptr;   // per-image temporaries (energies, 3 adjoints)
     double *ds = nullptr, *ds_jb = nullptr;   // arc lengths of string 0
     RedistPlan plan{};
     int plan_cap = 0;
@@ -319,7 +319,7 @@ mepgl_status build_layout(mepgl_ctx *c)
     CK(c, cudaMalloc(&S.xtab_d, LS_GRID * sizeof(double)));
     CK(c, cudaMemcpy(S.xtab_f, xf.data(), LS_GRID * sizeof(double), cudaMemcpyHostToDevice));
     CK(c, cudaMemcpy(S.xtab_d, xd.data(), LS_GRID * sizeof(double), cudaMemcpyHostToDevice));
-    CK(c, cudaMalloc(&c->dscratch, (I + 64) * sizeof(double)));
+    CK(c, cudaMalloc(&c->dscratch, (3 * I + 64) * sizeof(double)));
     int fmax = 0;
     for (auto &s : c->strings) fmax = fmax > s.F ? fmax : s.F;
     CK(c, cudaMalloc(&c->ds, (fmax + 1) * sizeof(double)));
@@ -816,6 +816,32 @@ mepgl_status mepgl_batch_free_energy(mepgl_ctx *c, int string, double *fenergy)
     CK(c, cudaMemcpyAsync(fenergy, c->dscratch + c->hdesc[string].img_base, c->strings[string].F * sizeof(double),
                           cudaMemcpyDeviceToHost, c->stream));
     CK(c, cudaStreamSynchronize(c->stream));
+    return MEPGL_OK;
+}
+
+mepgl_status mepgl_param_adjoint(mepgl_ctx *c, double *dF_dH, double *dF_deta, double *dF_dgamma)
+{
+    return mepgl_batch_param_adjoint(c, 0, dF_dH, dF_deta, dF_dgamma);
+}
+
+mepgl_status mepgl_batch_param_adjoint(mepgl_ctx *c, int string, double *dF_dH, double *dF_deta, double *dF_dgamma)
+{
+    if (!c || string < 0 || string >= (int)c->strings.size())
+        return fail(c, MEPGL_ERR_INVALID_ARG, "mepgl_param_adjoint: bad string index");
+    mepgl_status st = flush(c);
+    if (st != MEPGL_OK) return st;
+    CK(c, launch_param_adjoint(string_launch(c, string), c->sc, c->xi, c->dscratch));
+    c->launches += 1;
+    const int F = c->strings[string].F;
+    std::vector<double> h(3 * (size_t)F);
+    CK(c, cudaMemcpyAsync(h.data(), c->dscratch + 3 * (size_t)c->hdesc[string].img_base, h.size() * sizeof(double),
+                          cudaMemcpyDeviceToHost, c->stream));
+    CK(c, cudaStreamSynchronize(c->stream));
+    for (int n = 0; n < F; ++n) {
+        if (dF_dH) dF_dH[n] = h[3 * n];
+        if (dF_deta) dF_deta[n] = h[3 * n + 1];
+        if (dF_dgamma) dF_dgamma[n] = h[3 * n + 2];
+    }
     return MEPGL_OK;
 }
 

@@ -67,8 +67,10 @@ struct ImagePtrs {
 };
 
 // ------------------------------------------------------------------ staging
-// Rows of the (TYT+2) x (TX+2) halo tile are spread over the warps; a warp
-// loads one row (32 columns, lanes 0 and 1 also the last two columns).
+// The (TYT+2) x (TX+2) halo tile is split into flat element indices spread
+// over the block; each thread first issues every global load of all its
+// elements (independent, so they are in flight together), then combines and
+// stores them.  Out-of-lattice elements are zero.
 // mode 0: x = in;  mode 1: x = in + alpha * aux (and interior x -> out);
 // mode 2: x = -aux + beta * in, i.e. the new direction (interior -> out).
 template <class T, int NC, int TYT, int MODE>
@@ -76,46 +78,62 @@ __device__ __forceinline__ void stage(Tile<T, NC, TYT> &t, const StringDesc &S, 
                                       int j0, T coef, bool write_out, bool masks)
 {
     using V = vec2_t<T>;
-    const int lane = threadIdx.x & 31, wrp = threadIdx.x >> 5;
-    for (int hy = wrp; hy < TYT + 2; hy += NT / 32) {
-        const int gj = j0 + hy - 1;
-        const bool rowin = gj >= 0 && gj < S.ny;
-        for (int hx = lane; hx < TX + 2; hx += 32) {
-            const int gi = i0 + hx - 1;
-            V f[1 + NC];
-            uint16_t m = 0;
-            if (rowin && gi >= 0 && gi < S.nx) {
-                const int s = gi + S.nx * gj;
-                if (masks)
-                    m = S.mask ? S.mask[s]
-                               : (uint16_t)((S.code_comp[s] & 0xff) | ((S.code_sc[s] & 0xff) << 8));
+    constexpr int HW = TX + 2, HE = (TYT + 2) * HW, NI = (HE + NT - 1) / NT;
+    const bool aux = MODE == 2 || (MODE == 1 && coef != (T)0);
+    V f[NI][1 + NC], a[NI][1 + NC];
+    uint16_t m[NI];
+    int sidx[NI];
+    bool ok[NI];
 #pragma unroll
-                for (int c = 0; c < 1 + NC; ++c) {
-                    if (MODE == 2) {
-                        const V gg = ip.aux[c][s], dd = ip.in[c][s];
-                        f[c].x = -gg.x + coef * dd.x;
-                        f[c].y = -gg.y + coef * dd.y;
-                    } else {
-                        f[c] = ip.in[c][s];
-                        if (MODE == 1 && coef != (T)0) {
-                            const V dd = ip.aux[c][s];
-                            f[c].x = f[c].x + coef * dd.x;
-                            f[c].y = f[c].y + coef * dd.y;
-                        }
-                    }
-                }
-                if (write_out && hx >= 1 && hx <= TX && hy >= 1 && hy <= TYT)
+    for (int k = 0; k < NI; ++k) {
+        const int e = threadIdx.x + k * NT;
+        const int hy = e / HW, hx = e - hy * HW;
+        const int gi = i0 + hx - 1, gj = j0 + hy - 1;
+        ok[k] = e < HE && gi >= 0 && gi < S.nx && gj >= 0 && gj < S.ny;
+        sidx[k] = ok[k] ? gi + S.nx * gj : 0;
+        m[k] = 0;
 #pragma unroll
-                    for (int c = 0; c < 1 + NC; ++c) ip.out[c][s] = f[c];
-            } else {
-#pragma unroll
-                for (int c = 0; c < 1 + NC; ++c) f[c].x = f[c].y = (T)0;
-            }
-            t.A[hy][hx] = f[0];
-#pragma unroll
-            for (int c = 0; c < NC; ++c) t.P[c][hy][hx] = f[1 + c];
-            if (masks) t.m[hy][hx] = m;
+        for (int c = 0; c < 1 + NC; ++c) {
+            f[k][c].x = f[k][c].y = (T)0;
+            a[k][c].x = a[k][c].y = (T)0;
         }
+        if (ok[k]) {
+            const int s = sidx[k];
+#pragma unroll
+            for (int c = 0; c < 1 + NC; ++c) f[k][c] = ip.in[c][s];
+            if (aux)
+#pragma unroll
+                for (int c = 0; c < 1 + NC; ++c) a[k][c] = ip.aux[c][s];
+            if (masks)
+                m[k] = S.mask ? S.mask[s]
+                              : (uint16_t)((S.code_comp[s] & 0xff) | ((S.code_sc[s] & 0xff) << 8));
+        }
+    }
+#pragma unroll
+    for (int k = 0; k < NI; ++k) {
+        const int e = threadIdx.x + k * NT;
+        if (e >= HE) continue;
+        const int hy = e / HW, hx = e - hy * HW;
+        V v[1 + NC];
+#pragma unroll
+        for (int c = 0; c < 1 + NC; ++c) {
+            if (MODE == 2) {
+                v[c].x = -a[k][c].x + coef * f[k][c].x;
+                v[c].y = -a[k][c].y + coef * f[k][c].y;
+            } else if (MODE == 1 && aux) {
+                v[c].x = f[k][c].x + coef * a[k][c].x;
+                v[c].y = f[k][c].y + coef * a[k][c].y;
+            } else {
+                v[c] = f[k][c];
+            }
+        }
+        if (write_out && ok[k] && hx >= 1 && hx <= TX && hy >= 1 && hy <= TYT)
+#pragma unroll
+            for (int c = 0; c < 1 + NC; ++c) ip.out[c][sidx[k]] = v[c];
+        t.A[hy][hx] = v[0];
+#pragma unroll
+        for (int c = 0; c < NC; ++c) t.P[c][hy][hx] = v[1 + c];
+        if (masks) t.m[hy][hx] = m[k];
     }
 }
 
@@ -192,8 +210,10 @@ __device__ double line_search_scan(const double *c, const double *xt)
     return (double)((T)xt[j] / m);
 }
 
-// Exact minimiser of the quartic on alpha > 0 (closed-form roots of the
-// cubic derivative, two Newton steps each); `fallback` when none.
+// Exact version of the reference's scan: the first local minimum of the
+// quartic downhill from alpha = 0, i.e. the smallest positive root of the
+// cubic derivative with positive curvature (closed-form roots, two Newton
+// steps each); `fallback` (the scan's answer) when p'(0) >= 0 or none exists.
 __device__ double line_search_exact(const double *c, double fallback)
 {
     const double a3 = 4 * c[4], a2 = 3 * c[3], a1 = 2 * c[2], a0 = c[1];
@@ -222,7 +242,9 @@ __device__ double line_search_exact(const double *c, double fallback)
     } else if (a1 != 0) {
         roots[nr++] = -a0 / a1;
     }
-    double best = -1, fbest = 0;
+    // the scan stops at the first increase: not a descent direction -> its answer
+    if (!(a0 < 0)) return fallback;
+    double best = -1;
     for (int t = 0; t < nr; ++t) {
         double r = roots[t];
         for (int it = 0; it < 2; ++it) {
@@ -231,8 +253,7 @@ __device__ double line_search_exact(const double *c, double fallback)
         }
         const double ddp = a1 + r * (2 * a2 + r * 3 * a3);
         if (!(r > 0) || !(ddp > 0)) continue;
-        const double fr = quartic_rn(c, r);
-        if (best < 0 || fr < fbest) { best = r; fbest = fr; }
+        if (best < 0 || r < best) best = r;   // first local minimum downhill from 0
     }
     return best < 0 ? fallback : best;
 }
@@ -411,6 +432,50 @@ __global__ void __launch_bounds__(NT) k_energy(const __grid_constant__ Batch bt,
         double tot[1];
         if (finish_image<1>(v, red, sc, part_slot(S, tr), S.tile_base + tr.n * tpi, tpi, img, tot) && threadIdx.x == 0)
             out[img] = tot[0];
+        __syncthreads();
+    }
+}
+
+// Per-image dF/dH, dF/deta, dF/dgamma at fixed fields (out[3 img + k]).
+template <class T, int NC>
+__global__ void __launch_bounds__(NT) k_param_adjoint(const __grid_constant__ Batch bt,
+                                                      const TileRef *__restrict__ tiles, int n_tiles, Scalars sc,
+                                                      int xbuf, double *out)
+{
+    constexpr int TYT = TileRows<T>::v;
+    __shared__ Tile<T, NC, TYT> t;
+    __shared__ double red[NT / 32 * 3];
+    for (int tt = blockIdx.x; tt < n_tiles; tt += gridDim.x) {
+        const TileRef tr = tiles[tt];
+        const StringDesc &S = bt.s[tr.s];
+        const int img = S.img_base + tr.n;
+        const int i0 = tr.tx * TX, j0 = tr.ty * TYT;
+        ImagePtrs<T, NC> ip;
+        image_ptrs<T, NC>(ip, S.x[xbuf], nullptr, nullptr, (size_t)tr.n * S.nx * S.ny);
+        stage<T, NC, TYT, 0>(t, S, ip, i0, j0, (T)0, false, true);
+        SiteParams<T> p;
+        p.load_uniform(S);
+        __syncthreads();
+        T v[3] = {(T)0, (T)0, (T)0};
+        const int lx = threadIdx.x & 31, gi = i0 + lx;
+#pragma unroll
+        for (int r = 0; r < TYT / 8; ++r) {
+            const int ly = (threadIdx.x >> 5) + 8 * r, gj = j0 + ly;
+            if (gi < S.nx && gj < S.ny) {
+                Wts<T> w;
+                w.load(t.m[ly + 1][lx + 1]);
+                if (S.per_site) p.load_site(S, gi + S.nx * gj, NC);
+                site_param_adjoint<T, NC, TYT>(t, lx + 1, ly + 1, p, w, S.thin_film, v);
+            }
+        }
+        const int tpi = S.tiles_x * S.tiles_y;
+        double tot[3];
+        if (finish_image<3>(v, red, sc, part_slot(S, tr), S.tile_base + tr.n * tpi, tpi, img, tot) &&
+            threadIdx.x == 0) {
+            out[3 * img] = tot[0];
+            out[3 * img + 1] = tot[1];
+            out[3 * img + 2] = tot[2];
+        }
         __syncthreads();
     }
 }
@@ -760,6 +825,12 @@ cudaError_t launch_energy(const Launch &L, const Scalars &sc, int xbuf, double *
 cudaError_t launch_gradient_only(const Launch &L, int xbuf, FieldPtrs out, int maxwell)
 {
     DISPATCH(L, k_gradient_only, *L.batch, L.tiles, L.n_tiles, xbuf, out, maxwell);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_param_adjoint(const Launch &L, const Scalars &sc, int xbuf, double *out)
+{
+    DISPATCH(L, k_param_adjoint, *L.batch, L.tiles, L.n_tiles, sc, xbuf, out);
     return cudaGetLastError();
 }
 

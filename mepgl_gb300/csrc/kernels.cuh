@@ -41,6 +41,7 @@ cudaError_t launch_apply_update(const Launch &L, const Scalars &sc, const String
                                 int xbuf, int dbuf);
 // Energy of x[xbuf] into sc.fenergy_out (per image).
 cudaError_t launch_energy(const Launch &L, const Scalars &sc, int xbuf, double *out);
+cudaError_t launch_param_adjoint(const Launch &L, const Scalars &sc, int xbuf, double *out);
 // Gradient of x[xbuf] into the three arrays of `out` (single string).
 struct FieldPtrs { void *p[3]; };
 cudaError_t launch_gradient_only(const Launch &L, int xbuf, FieldPtrs out, int maxwell);

@@ -79,11 +79,16 @@ inline void build_mask_table(MaskTable<T> &M)
     }
 }
 
-// Tile of TYT rows (+ halo) of A, psi_1[, psi_2] and the packed codes.
+// Fields of a tile of TYT rows (+ halo): A, psi_1[, psi_2].
 template <class T, int NC, int TYT>
-struct Tile {
+struct TileF {
     vec2_t<T> A[TYT + 2][TX + 2];
     vec2_t<T> P[NC][TYT + 2][TX + 2];
+};
+
+// The same with the packed neighbour codes of each site.
+template <class T, int NC, int TYT>
+struct Tile : TileF<T, NC, TYT> {
     uint16_t m[TYT + 2][TX + 2];
 };
 
@@ -166,6 +171,28 @@ __device__ __forceinline__ T site_energy(const Tile<T, NC, TYT> &t, int lx, int 
         em = (T)0.125 * (w.vUR * r0 * r0 + w.vUL * r1 * r1 + w.vLL * r2 * r2 + w.vLR * r3 * r3);
     }
     return (kx * w.wfx + ky * w.wfy + nl * w.area + em) * p.dx2;
+}
+
+// Partial derivatives of site_energy at fixed fields with respect to a
+// uniform shift of the applied field h, to eta and to gamma (no reference
+// counterpart): out[0] = -1/4 sum_views w_v (curl - h), out[1] = area Re(psi1
+// psi2*), out[2] = area |psi1|^2 |psi2|^2 / 2, each times dx^2.
+template <class T, int NC, int TYT>
+__device__ __forceinline__ void site_param_adjoint(const Tile<T, NC, TYT> &t, int lx, int ly,
+                                                   const SiteParams<T> &p, const Wts<T> &w, int thin_film, T *out)
+{
+    if (NC == 2) {
+        const vec2_t<T> P1 = TP(0, 0, 0), P2 = TP(NC - 1, 0, 0);
+        out[1] += (P1.x * P2.x + P1.y * P2.y) * w.area * p.dx2;
+        out[2] += (T)0.5 * (P1.x * P1.x + P1.y * P1.y) * (P2.x * P2.x + P2.y * P2.y) * w.area * p.dx2;
+    }
+    if (!thin_film) {
+        const vec2_t<T> A0 = TA(0, 0);
+        const T ayp = (TA(1, 0).y - A0.y) * p.idx, aym = (A0.y - TA(-1, 0).y) * p.idx;
+        const T axp = (TA(0, 1).x - A0.x) * p.idx, axm = (A0.x - TA(0, -1).x) * p.idx;
+        const T r0 = ayp - axp - p.h, r1 = aym - axp - p.h, r2 = aym - axm - p.h, r3 = ayp - axm - p.h;
+        out[0] -= (T)0.25 * (w.vUR * r0 + w.vUL * r1 + w.vLL * r2 + w.vLR * r3) * p.dx2;
+    }
 }
 
 // Gradient dF/dA (out[0..1]) and dF/dpsi_c (out[2+2c..]) at one site,
@@ -261,7 +288,7 @@ __device__ __forceinline__ void site_gradient(const Tile<T, NC, TYT> &t, int lx,
 // nlcg.cu:997-1370): out = {A, B, C, D, E}.  compat keeps the reference's
 // x-link first-order slip and y-link halved cubic coefficient.
 template <class T, int NC, int TYT>
-__device__ __forceinline__ void site_poly(const Tile<T, NC, TYT> &t, const Tile<T, NC, TYT> &dt, int lx, int ly,
+__device__ __forceinline__ void site_poly(const Tile<T, NC, TYT> &t, const TileF<T, NC, TYT> &dt, int lx, int ly,
                                           const SiteParams<T> &p, const Wts<T> &w, int compat, int thin_film, T *out)
 {
     T e = 0, b1 = 0, c2 = 0, d3 = 0, e4 = 0;

@@ -88,6 +88,8 @@ _SIGS = {
     "mepgl_batch_free_energy": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p]),
     "mepgl_batch_image_scalars": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]),
     "mepgl_batch_arc_length": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_void_p]),
+    "mepgl_param_adjoint": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "mepgl_batch_param_adjoint": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]),
 }
 
 
@@ -245,6 +247,12 @@ class StringContext:
         fe, gn, al = np.zeros(self.F), np.zeros(self.F), np.zeros(self.F)
         self._check(self.L.mepgl_image_scalars(self.h, _ptr(fe), _ptr(gn), _ptr(al)))
         return dict(fenergy=fe, g_norm2=gn, alpha=al)
+
+    def param_adjoint(self):
+        """(F, 3): per-image dF/dH (uniform shift of h), dF/deta, dF/dgamma at the current fields."""
+        h, e, g = np.zeros(self.F), np.zeros(self.F), np.zeros(self.F)
+        self._check(self.L.mepgl_param_adjoint(self.h, _ptr(h), _ptr(e), _ptr(g)))
+        return np.stack([h, e, g], axis=1)
 
     def compute_jb(self):
         b = np.empty(self._shape()[:3], self.dtype)

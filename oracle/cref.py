@@ -129,6 +129,13 @@ class Oracle:
                                  _ptr(g2), int(maxwell))
         return ga, g1, g2
 
+    def param_adjoint(self, a, p1, p2=None):
+        """(F, 3): per-image dF/dH (uniform shift of h), dF/deta, dF/dgamma at fixed fields."""
+        a, p1, p2 = self._state(a, p1, p2)
+        out = np.zeros((a.shape[0], 3))
+        self._fn("glo_param_adjoint")(C.byref(self.S), a.shape[0], _ptr(a), _ptr(p1), _ptr(p2), _ptr(out))
+        return out
+
     def polynomial(self, a, p1, p2, da, d1, d2, compat=True):
         a, p1, p2 = self._state(a, p1, p2)
         da, d1, d2 = self._state(da, d1, d2)

@@ -114,6 +114,52 @@ void FN(glo_energy)(const PROB *P, int F, const REAL *A, const REAL *p1, const R
     }
 }
 
+/* Parameter adjoints of the per-image energy (no reference counterpart):
+ * partial derivatives of glo_energy at fixed fields with respect to a uniform
+ * shift of the applied field h (dF/dH), to eta and to gamma, differentiating
+ * the terms of site_energy above: -1/4 sum_views (curl - h), and
+ * area/4 * Re(psi1 psi2*) and area/4 * |psi1|^2 |psi2|^2 / 2, each times dx^2.
+ * out[3 n + 0..2] = dF_n/dH, dF_n/deta, dF_n/dgamma. */
+void FN(glo_param_adjoint)(const PROB *P, int F, const REAL *A, const REAL *p1, const REAL *p2, double *out)
+{
+    const long M = (long)P->nx * P->ny;
+    const int nx = P->nx;
+    GLO_OMP_FOR
+    for (int n = 0; n < F; ++n) {
+        FN(ksum) dh = {0, 0}, de = {0, 0}, dg = {0, 0};
+        for (int j = 0; j < P->ny; ++j)
+            for (int i = 0; i < nx; ++i) {
+                const long s = i + (long)nx * j, k = n * M + s;
+                const unsigned sc = P->sc_nn[s], cc = P->comp_nn[s];
+                const REAL dx = P->dx, dx2 = dx * dx;
+                if (P->ncomp == 2) {
+                    const int area_n = B_(sc, 0) * B_(sc, 1) * B_(sc, 2) + B_(sc, 2) * B_(sc, 3) * B_(sc, 4)
+                                     + B_(sc, 4) * B_(sc, 5) * B_(sc, 6) + B_(sc, 6) * B_(sc, 7) * B_(sc, 0);
+                    const REAL x1 = p1[2 * k], y1 = p1[2 * k + 1], x2 = p2[2 * k], y2 = p2[2 * k + 1];
+                    const REAL w = (REAL)area_n / (REAL)4;
+                    FN(kadd)(&de, (double)((x1 * x2 + y1 * y2) * w * dx2));
+                    FN(kadd)(&dg, (double)((FN(sq)(x1) + FN(sq)(y1)) * (FN(sq)(x2) + FN(sq)(y2)) / (REAL)2 * w * dx2));
+                }
+                if (!P->thin_film) {
+                    const REAL h = P->h[s];
+                    const REAL ayp = B_(cc, 0) ? (A[2 * (k + 1) + 1] - A[2 * k + 1]) / dx : 0;
+                    const REAL aym = B_(cc, 4) ? (A[2 * k + 1] - A[2 * (k - 1) + 1]) / dx : 0;
+                    const REAL axp = B_(cc, 2) ? (A[2 * (k + nx)] - A[2 * k]) / dx : 0;
+                    const REAL axm = B_(cc, 6) ? (A[2 * k] - A[2 * (k - nx)]) / dx : 0;
+                    REAL em = 0;
+                    if (B_(cc, 0) && B_(cc, 1) && B_(cc, 2)) em += ayp - axp - h;
+                    if (B_(cc, 2) && B_(cc, 3) && B_(cc, 4)) em += aym - axp - h;
+                    if (B_(cc, 4) && B_(cc, 5) && B_(cc, 6)) em += aym - axm - h;
+                    if (B_(cc, 6) && B_(cc, 7) && B_(cc, 0)) em += ayp - axm - h;
+                    FN(kadd)(&dh, (double)(-(REAL)0.25 * em * dx2));
+                }
+            }
+        out[3 * n] = FN(kval)(&dh);
+        out[3 * n + 1] = FN(kval)(&de);
+        out[3 * n + 2] = FN(kval)(&dg);
+    }
+}
+
 /* ---------------------------------------------------------------- gradient
  * Restates gradientPsi (nlcg.cu:504-744) and gradientA (nlcg.cu:746-888).
  * On a link i -> j along direction e the reference uses, per component,
@@ -419,10 +465,11 @@ static double FN(line_search_compat)(const double c[5])
     return (double)(REAL)(x / m);
 }
 
-/* Exact minimiser of the quartic on alpha > 0: the real roots of
- * p'(a) = B + 2C a + 3D a^2 + 4E a^3 (closed form, then two Newton steps),
- * keeping the positive local minimum of lowest value; falls back to the
- * compat scan when no positive local minimum exists. */
+/* Exact version of the compat scan: the first local minimum of the quartic
+ * reached from alpha = 0 downhill, i.e. the smallest positive root of
+ * p'(a) = B + 2C a + 3D a^2 + 4E a^3 (closed form, then two Newton steps)
+ * with p'' > 0.  The scan stops at the first increase, so when p'(0) >= 0 or
+ * no such root exists this falls back to the scan itself. */
 static double FN(line_search_exact)(const double c[5])
 {
     const double a3 = 4 * c[4], a2 = 3 * c[3], a1 = 2 * c[2], a0 = c[1];
@@ -455,7 +502,8 @@ static double FN(line_search_exact)(const double c[5])
     } else if (a1 != 0) {
         roots[nr++] = -a0 / a1;
     }
-    double best = -1, fbest = 0;
+    if (!(a0 < 0)) return FN(line_search_compat)(c);
+    double best = -1;
     for (int t = 0; t < nr; ++t) {
         double r = roots[t];
         for (int it = 0; it < 2; ++it) {
@@ -465,8 +513,7 @@ static double FN(line_search_exact)(const double c[5])
         }
         const double ddp = a1 + r * (2 * a2 + r * 3 * a3);
         if (!(r > 0) || !(ddp > 0)) continue;
-        const double fr = FN(quartic)(c, r);
-        if (best < 0 || fr < fbest) { best = r; fbest = fr; }
+        if (best < 0 || r < best) best = r;
     }
     if (best < 0) return FN(line_search_compat)(c);
     return best;

@@ -88,17 +88,24 @@ def test_compat_polynomial_equals_exact_for_q_minus_one_except_cubic_y():
     assert np.all(np.abs(pc[:, 2] - pe[:, 2]) > 0)
 
 
-def test_exact_line_search_minimises_quartic():
+def test_exact_line_search_is_first_minimum_of_the_scan():
+    """LS_EXACT returns the first local minimum downhill from 0 (a stationary
+    point with positive curvature, the quartic non-increasing before it), and
+    the reference's 2.5 % scan lands within one grid step of it."""
     o = cref.Oracle(Problem.uniform(4, 4, 0.5))
     rng = np.random.default_rng(7)
-    for _ in range(20):
+    for _ in range(40):
         c = np.array([rng.uniform(1, 10), -rng.uniform(0.1, 5), rng.uniform(-1, 5), rng.uniform(-2, 2),
                       rng.uniform(0.01, 2)])
         a = o.line_search(c[None, :1], c[None, 1:], mode=cref.LS_EXACT)[0]
-        xs = np.linspace(0, 20, 200001)
+        a_scan = o.line_search(c[None, :1], c[None, 1:], mode=cref.LS_COMPAT)[0]
+        dp = c[1] + 2 * c[2] * a + 3 * c[3] * a ** 2 + 4 * c[4] * a ** 3
+        ddp = 2 * c[2] + 6 * c[3] * a + 12 * c[4] * a ** 2
+        assert abs(dp) <= 1e-9 * (abs(c[1]) + 1) and ddp > 0
+        xs = np.linspace(0, a, 20001)
         f = c[0] + c[1] * xs + c[2] * xs ** 2 + c[3] * xs ** 3 + c[4] * xs ** 4
-        f_at = c[0] + c[1] * a + c[2] * a ** 2 + c[3] * a ** 3 + c[4] * a ** 4
-        assert f_at <= f.min() + 1e-9 * abs(f.min())
+        assert np.all(np.diff(f) <= 1e-12 * abs(c[0]))
+        assert abs(np.log(a / a_scan)) < np.log(1.025) * 1.0001
 
 
 def test_linear_spline_reproduces_linear_data():
