@@ -38,7 +38,7 @@ namespace mepgl {
 #define MEPGL_MINB_GRAD 4
 #endif
 #ifndef MEPGL_MINB_DIR
-#define MEPGL_MINB_DIR 3
+#define MEPGL_MINB_DIR 4
 #endif
 
 template <class T> struct TileRows { static constexpr int v = sizeof(T) == 4 ? MEPGL_ROWS_F32 : MEPGL_ROWS_F64; };
