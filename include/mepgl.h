@@ -50,6 +50,11 @@ enum { MEPGL_POLY_COMPAT = 0, MEPGL_POLY_EXACT = 1 };       /* line polynomial  
 enum { MEPGL_SPLINE_COMPAT = 0, MEPGL_SPLINE_FMM = 1 };     /* cubic evaluation       */
 enum { MEPGL_METRIC_FIELDS = 0, MEPGL_METRIC_JB = 1 };      /* arc-length metric      */
 enum { MEPGL_REDIST_LINEAR = 0, MEPGL_REDIST_CUBIC = 1 };
+/* Kinetic and magnetic terms: the reference's linearised covariant differences
+ * with four collocated curl views (mepgl/src/nlcg.cu:149-203), or gauge links
+ * U = exp(i q A dx) with one curl per plaquette (exactly gauge invariant; no
+ * reference counterpart; energy, gradient and adjoints only, no NLCG). */
+enum { MEPGL_DISC_REFERENCE = 0, MEPGL_DISC_LINK = 1 };
 
 /* The physical problem.  Replaces the generated headers config.cuh/real.cuh
  * (N, dx, MULTICOMPONENT, NO_SELF_FIELD, DOUBLE_PRECISION) and the lattice
@@ -80,6 +85,7 @@ typedef struct mepgl_options {
     int32_t metric;            /* MEPGL_METRIC_*                                */
     int32_t use_graphs;        /* capture NLCG steps as CUDA graphs (default 1) */
     int32_t tile_rows;         /* rows per stencil tile: 0 = auto, 4, 8 or 16   */
+    int32_t discretization;    /* MEPGL_DISC_*                                  */
 } mepgl_options;
 
 typedef struct mepgl_ctx mepgl_ctx;

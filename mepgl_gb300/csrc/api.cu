@@ -208,6 +208,7 @@ void fill_desc(mepgl_ctx *c, int si, int img_base, int tile_base)
     U.h = s.params[8][0];
     U.idx = 1.0 / s.dx;
     U.dx2 = s.dx * s.dx;
+    U.dx = s.dx;
     Uniform<float> &Uf = D.uf;
     for (int k = 0; k < 2; ++k) {
         Uf.a[k] = (float)U.a[k];
@@ -223,6 +224,8 @@ void fill_desc(mepgl_ctx *c, int si, int img_base, int tile_base)
     Uf.h = (float)U.h;
     Uf.idx = (float)U.idx;
     Uf.dx2 = (float)s.dx * (float)s.dx;
+    Uf.dx = (float)s.dx;
+    D.disc = c->opt.discretization;
     D.ph = s.dparams[8];
     D.mask = s.dmask;
     for (int b = 0; b < 2; ++b)
@@ -650,6 +653,7 @@ void mepgl_default_options(mepgl_options *o)
     o->metric = MEPGL_METRIC_JB;
     o->use_graphs = 1;
     o->tile_rows = 0;
+    o->discretization = MEPGL_DISC_REFERENCE;
 }
 
 const char *mepgl_version(void) { return "mepgl_gb300 0.1 (sm_103a)"; }
@@ -691,6 +695,10 @@ mepgl_status mepgl_create_batch(const mepgl_problem *probs, int n_strings, const
     mepgl_ctx *c = new mepgl_ctx();
     if (opt) c->opt = *opt;
     else mepgl_default_options(&c->opt);
+    if (c->opt.discretization != MEPGL_DISC_REFERENCE && c->opt.discretization != MEPGL_DISC_LINK) {
+        delete c;
+        return fail(nullptr, MEPGL_ERR_INVALID_ARG, "mepgl_create: unknown discretization");
+    }
     c->ncomp = p->multicomponent ? 2 : 1;
     c->thin_film = p->thin_film ? 1 : 0;
     c->precision = p->precision;
@@ -889,6 +897,9 @@ mepgl_status mepgl_energy_grad(mepgl_ctx *c, double *fenergy, void *g_a, void *g
 mepgl_status mepgl_nlcg_steps(mepgl_ctx *c, int iterations, int use_cg, int maxwell_only)
 {
     if (!c || iterations < 0) return fail(c, MEPGL_ERR_INVALID_ARG, "mepgl_nlcg_steps: bad argument");
+    if (c->opt.discretization == MEPGL_DISC_LINK)
+        return fail(c, MEPGL_ERR_UNSUPPORTED,
+                    "mepgl_nlcg_steps: the link discretisation has no quartic line polynomial; use mepgl_energy_grad");
     return nlcg_steps(c, iterations, use_cg ? 1 : 0, maxwell_only ? 1 : 0);
 }
 
@@ -971,6 +982,8 @@ mepgl_status mepgl_redistribute(mepgl_ctx *c, int kind, int F_new)
 mepgl_status mepgl_iteration(mepgl_ctx *c, char mode, int relaxation_steps, int use_cg)
 {
     if (!c || relaxation_steps < 0) return fail(c, MEPGL_ERR_INVALID_ARG, "mepgl_iteration: bad argument");
+    if (c->opt.discretization == MEPGL_DISC_LINK)
+        return fail(c, MEPGL_ERR_UNSUPPORTED, "mepgl_iteration: not available with the link discretisation");
     mepgl_status st = MEPGL_OK;
     switch (mode) {
     case 'S': return mepgl_nlcg_steps(c, relaxation_steps, use_cg, 0);
@@ -1041,6 +1054,8 @@ mepgl_status mepgl_info(const mepgl_ctx *c, int *n_images, int *precision, int64
 
 mepgl_status mepgl_profile_passes(mepgl_ctx *c, int steps, int use_cg, double *ms_grad, double *ms_dir_poly)
 {
+    if (c && c->opt.discretization == MEPGL_DISC_LINK)
+        return fail(c, MEPGL_ERR_UNSUPPORTED, "mepgl_profile_passes: not available with the link discretisation");
     if (!c || steps < 1) return fail(c, MEPGL_ERR_INVALID_ARG, "mepgl_profile_passes: steps must be >= 1");
     std::vector<cudaEvent_t> ev(2 * steps + 1);
     for (auto &e : ev) CK(c, cudaEventCreate(&e));

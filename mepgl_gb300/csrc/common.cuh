@@ -32,7 +32,7 @@ template <class T> using vec2_t = typename Vec2<T>::type;
 template <class T>
 struct Uniform {
     T a[2], b[2], hmx[2], hmy[2], aob[2], q[2];
-    T eta, gamma, delta, h, idx, dx2;
+    T eta, gamma, delta, h, idx, dx2, dx;
 };
 
 // One string (one lattice, F images) as seen by the kernels.  Field buffers
@@ -45,6 +45,7 @@ struct StringDesc {
     int img_base;             // first global image index of this string
     int tile_base;            // first global tile index of this string
     int thin_film;
+    int disc;                 // 0: the reference's linearised differences, 1: gauge links
     int per_site;             // 1: parameters read from the arrays below
     Uniform<float> uf;
     Uniform<double> ud;

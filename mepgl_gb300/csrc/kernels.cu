@@ -425,7 +425,8 @@ __global__ void __launch_bounds__(NT) k_energy(const __grid_constant__ Batch bt,
                 Wts<T> w;
                 w.load(t.m[ly + 1][lx + 1]);
                 if (S.per_site) p.load_site(S, gi + S.nx * gj, NC);
-                v[0] += site_energy<T, NC, TYT>(t, lx + 1, ly + 1, p, w, S.thin_film);
+                v[0] += S.disc ? site_energy_link<T, NC, TYT>(t, lx + 1, ly + 1, p, w, S.thin_film)
+                               : site_energy<T, NC, TYT>(t, lx + 1, ly + 1, p, w, S.thin_film);
             }
         }
         const int tpi = S.tiles_x * S.tiles_y;
@@ -465,7 +466,15 @@ __global__ void __launch_bounds__(NT) k_param_adjoint(const __grid_constant__ Ba
                 Wts<T> w;
                 w.load(t.m[ly + 1][lx + 1]);
                 if (S.per_site) p.load_site(S, gi + S.nx * gj, NC);
-                site_param_adjoint<T, NC, TYT>(t, lx + 1, ly + 1, p, w, S.thin_film, v);
+                if (S.disc) {
+                    T u[3] = {(T)0, v[1], v[2]};
+                    site_param_adjoint<T, NC, TYT>(t, lx + 1, ly + 1, p, w, 1, u);
+                    v[1] = u[1];
+                    v[2] = u[2];
+                    if (!S.thin_film) v[0] += site_dh_link<T, NC, TYT>(t, lx + 1, ly + 1, p, w);
+                } else {
+                    site_param_adjoint<T, NC, TYT>(t, lx + 1, ly + 1, p, w, S.thin_film, v);
+                }
             }
         }
         const int tpi = S.tiles_x * S.tiles_y;
@@ -516,7 +525,18 @@ __global__ void __launch_bounds__(NT) k_gradient_only(const __grid_constant__ Ba
                     hd = h_site(S, p, gj > 0 ? s - S.nx : s);
                 }
                 T g[2 + 2 * NC];
-                site_gradient<T, NC, TYT>(t, lx + 1, ly + 1, p, w, hr, hl, hu, hd, maxwell, S.thin_film, g);
+                if (S.disc) {
+                    T hmx_l[2] = {p.hmx[0], p.hmx[1]}, hmy_d[2] = {p.hmy[0], p.hmy[1]};
+                    if (S.per_site)
+                        for (int c = 0; c < NC; ++c) {
+                            if (gi > 0) hmx_l[c] = (T)0.5 / static_cast<const T *>(S.pmxx[c])[s - 1];
+                            if (gj > 0) hmy_d[c] = (T)0.5 / static_cast<const T *>(S.pmyy[c])[s - S.nx];
+                        }
+                    site_gradient_link<T, NC, TYT>(t, lx + 1, ly + 1, p, w, hl, hd, hmx_l, hmy_d, maxwell,
+                                                   S.thin_film, g);
+                } else {
+                    site_gradient<T, NC, TYT>(t, lx + 1, ly + 1, p, w, hr, hl, hu, hd, maxwell, S.thin_film, g);
+                }
 #pragma unroll
                 for (int c = 0; c < 1 + NC; ++c) {
                     V gv;
@@ -1062,6 +1082,7 @@ extern "C" mepgl_status mepgl_free_energy_noalloc(int nx, int ny, int n_images, 
     S.ud.delta = delta;
     S.ud.idx = 1.0 / dx;
     S.ud.dx2 = dx * dx;
+    S.ud.dx = dx;
     S.code_comp = comp_code;
     S.code_sc = sc_code;
     S.x[0][0] = const_cast<void *>(a);

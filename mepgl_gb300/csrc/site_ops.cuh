@@ -96,7 +96,7 @@ struct Tile : TileF<T, NC, TYT> {
 template <class T>
 struct SiteParams {
     T a[2], b[2], hmx[2], hmy[2], aob[2];  // hmx = 0.5 / m_xx
-    T q[2], eta, gamma, delta, h, idx, dx2;
+    T q[2], eta, gamma, delta, h, idx, dx2, dx;
     __device__ __forceinline__ void load_uniform(const StringDesc &S)
     {
         const Uniform<T> &U = S.template u<T>();
@@ -104,7 +104,7 @@ struct SiteParams {
         for (int c = 0; c < 2; ++c) {
             a[c] = U.a[c]; b[c] = U.b[c]; hmx[c] = U.hmx[c]; hmy[c] = U.hmy[c]; aob[c] = U.aob[c]; q[c] = U.q[c];
         }
-        eta = U.eta; gamma = U.gamma; delta = U.delta; h = U.h; idx = U.idx; dx2 = U.dx2;
+        eta = U.eta; gamma = U.gamma; delta = U.delta; h = U.h; idx = U.idx; dx2 = U.dx2; dx = U.dx;
     }
     // per-site overrides (strings whose parameter arrays are not uniform)
     __device__ __forceinline__ void load_site(const StringDesc &S, int s, int nc)
@@ -193,6 +193,142 @@ __device__ __forceinline__ void site_param_adjoint(const Tile<T, NC, TYT> &t, in
         const T r0 = ayp - axp - p.h, r1 = aym - axp - p.h, r2 = aym - axm - p.h, r3 = ayp - axm - p.h;
         out[0] -= (T)0.25 * (w.vUR * r0 + w.vUL * r1 + w.vLL * r2 + w.vLR * r3) * p.dx2;
     }
+}
+
+// ------------------------------------------------------- gauge links
+// The link (Peierls) discretisation of the same functional (no reference
+// counterpart): A_e at a site is the variable of the link to its +e
+// neighbour; per link and component the kinetic energy is
+// w_e / (2 m_e) |psi_t - U psi_s|^2 with U = exp(i q A_e dx); per plaquette
+// (lower-left corner s) 1/2 v_UR (B - h)^2 dx^2 with
+// B = (A_x(s) + A_y(s+x) - A_x(s+y) - A_y(s)) / dx.  Exactly invariant under
+// psi -> psi e^{i q chi}, A_e(s) -> A_e(s) + (chi(s+e) - chi(s)) / dx.
+template <class T> __device__ __forceinline__ void cis(T a, T &c, T &s);
+template <> __device__ __forceinline__ void cis<float>(float a, float &c, float &s) { sincosf(a, &s, &c); }
+template <> __device__ __forceinline__ void cis<double>(double a, double &c, double &s) { sincos(a, &s, &c); }
+
+template <class T>
+__device__ __forceinline__ T cond_density(const vec2_t<T> *P, int nc, const SiteParams<T> &p)
+{
+    T nl = 0;
+    for (int c = 0; c < nc; ++c) {
+        const T r = p.aob[c] + P[c].x * P[c].x + P[c].y * P[c].y;
+        nl += p.b[c] * (T)0.5 * r * r;
+    }
+    if (nc == 2) {
+        const T R = P[0].x * P[1].x + P[0].y * P[1].y, I = P[0].x * P[1].y - P[0].y * P[1].x;
+        nl += p.eta * R + p.gamma * (T)0.5 * (P[0].x * P[0].x + P[0].y * P[0].y) * (P[1].x * P[1].x + P[1].y * P[1].y)
+            + p.delta * (T)0.5 * (R * R - I * I);
+    }
+    return nl;
+}
+
+template <class T, int NC, int TYT>
+__device__ __forceinline__ T site_energy_link(const Tile<T, NC, TYT> &t, int lx, int ly, const SiteParams<T> &p,
+                                              const Wts<T> &w, int thin_film)
+{
+    vec2_t<T> P0[NC];
+#pragma unroll
+    for (int c = 0; c < NC; ++c) P0[c] = TP(c, 0, 0);
+    const T nl = cond_density<T>(P0, NC, p);
+    T kin = 0;
+#pragma unroll
+    for (int dir = 0; dir < 2; ++dir) {
+        const int ox = dir == 0 ? 1 : 0, oy = 1 - ox;
+        const T Ae = dir == 0 ? TA(0, 0).x : TA(0, 0).y, wl = dir == 0 ? w.wfx : w.wfy;
+#pragma unroll
+        for (int c = 0; c < NC; ++c) {
+            T cu, su;
+            cis<T>(p.q[c] * Ae * p.dx, cu, su);
+            const vec2_t<T> ps = P0[c], pt = TP(c, ox, oy);
+            const T zr = pt.x - (cu * ps.x - su * ps.y), zi = pt.y - (su * ps.x + cu * ps.y);
+            kin += wl * (dir == 0 ? p.hmx[c] : p.hmy[c]) * (zr * zr + zi * zi);
+        }
+    }
+    T em = 0;
+    if (!thin_film) {
+        const T B = (TA(0, 0).x + TA(1, 0).y - TA(0, 1).x - TA(0, 0).y) * p.idx - p.h;
+        em = (T)0.5 * w.vUR * B * B;
+    }
+    return kin + (nl * w.area + em) * p.dx2;
+}
+
+// Gradient of the link functional at one site (gather form): its own
+// forward links, the backward links owned by its -x / -y neighbours (whose
+// masses are hmx_l / hmy_d = 1 / (2 m) there), and the plaquettes with
+// lower-left corners s, s-x, s-y (applied fields h, hl, hd).
+template <class T, int NC, int TYT>
+__device__ __forceinline__ void site_gradient_link(const Tile<T, NC, TYT> &t, int lx, int ly, const SiteParams<T> &p,
+                                                   const Wts<T> &w, T hl, T hd, const T *hmx_l, const T *hmy_d,
+                                                   int maxwell, int thin_film, T *out)
+{
+#pragma unroll
+    for (int k = 0; k < 2 + 2 * NC; ++k) out[k] = 0;
+    const T ar = w.area * p.dx2;
+    vec2_t<T> P0[NC];
+#pragma unroll
+    for (int c = 0; c < NC; ++c) P0[c] = TP(c, 0, 0);
+    if (!maxwell) {
+#pragma unroll
+        for (int c = 0; c < NC; ++c) {
+            const T x = P0[c].x, y = P0[c].y, r2 = x * x + y * y;
+            out[2 + 2 * c] += (T)2 * x * (p.a[c] + p.b[c] * r2) * ar;
+            out[3 + 2 * c] += (T)2 * y * (p.a[c] + p.b[c] * r2) * ar;
+        }
+        if (NC == 2) {
+            const T x1 = P0[0].x, y1 = P0[0].y, x2 = P0[NC - 1].x, y2 = P0[NC - 1].y;
+            const T R = x1 * x2 + y1 * y2, I = x1 * y2 - y1 * x2, r1 = x1 * x1 + y1 * y1, r2 = x2 * x2 + y2 * y2;
+            out[2] += (p.eta * x2 + p.gamma * x1 * r2 + p.delta * (R * x2 - I * y2)) * ar;
+            out[3] += (p.eta * y2 + p.gamma * y1 * r2 + p.delta * (R * y2 + I * x2)) * ar;
+            out[2 + 2 * (NC - 1)] += (p.eta * x1 + p.gamma * x2 * r1 + p.delta * (R * x1 + I * y1)) * ar;
+            out[3 + 2 * (NC - 1)] += (p.eta * y1 + p.gamma * y2 * r1 + p.delta * (R * y1 - I * x1)) * ar;
+        }
+    }
+#pragma unroll
+    for (int dir = 0; dir < 2; ++dir) {
+        const int ox = dir == 0 ? 1 : 0, oy = 1 - ox;
+        const T Ae = dir == 0 ? TA(0, 0).x : TA(0, 0).y, wf = dir == 0 ? w.wfx : w.wfy;
+        const T Ab = dir == 0 ? TA(-1, 0).x : TA(0, -1).y, wb = dir == 0 ? w.wbx : w.wby;
+        T ga = 0;
+#pragma unroll
+        for (int c = 0; c < NC; ++c) {
+            const T q = p.q[c];
+            // own forward link s -> s + e
+            const T kf = wf * (dir == 0 ? p.hmx[c] : p.hmy[c]);
+            T cu, su;
+            cis<T>(q * Ae * p.dx, cu, su);
+            const vec2_t<T> ps = P0[c], pt = TP(c, ox, oy);
+            const T ur = cu * ps.x - su * ps.y, ui = su * ps.x + cu * ps.y;
+            const T zr = pt.x - ur, zi = pt.y - ui;
+            ga += (T)2 * kf * q * p.dx * (zr * ui - zi * ur);
+            // backward link s - e -> s, owned by the neighbour
+            const T kb = wb * (dir == 0 ? hmx_l[c] : hmy_d[c]);
+            T cb, sb;
+            cis<T>(q * Ab * p.dx, cb, sb);
+            const vec2_t<T> pb = TP(c, -ox, -oy);
+            const T br = ps.x - (cb * pb.x - sb * pb.y), bi = ps.y - (sb * pb.x + cb * pb.y);
+            if (!maxwell) {
+                out[2 + 2 * c] += (T)2 * kb * br - (T)2 * kf * (cu * zr + su * zi);
+                out[3 + 2 * c] += (T)2 * kb * bi - (T)2 * kf * (cu * zi - su * zr);
+            }
+        }
+        if (!thin_film) out[dir] += ga;
+    }
+    if (!thin_film) {
+        const T r0 = w.vUR * ((TA(0, 0).x + TA(1, 0).y - TA(0, 1).x - TA(0, 0).y) * p.idx - p.h) * p.dx;
+        const T rd = w.vLR * ((TA(0, -1).x + TA(1, -1).y - TA(0, 0).x - TA(0, -1).y) * p.idx - hd) * p.dx;
+        const T rl = w.vUL * ((TA(-1, 0).x + TA(0, 0).y - TA(-1, 1).x - TA(-1, 0).y) * p.idx - hl) * p.dx;
+        out[0] += r0 - rd;
+        out[1] += rl - r0;
+    }
+}
+
+// dF/dH of the link functional at one site: -v_UR (B - h) dx^2.
+template <class T, int NC, int TYT>
+__device__ __forceinline__ T site_dh_link(const Tile<T, NC, TYT> &t, int lx, int ly, const SiteParams<T> &p,
+                                          const Wts<T> &w)
+{
+    return -w.vUR * ((TA(0, 0).x + TA(1, 0).y - TA(0, 1).x - TA(0, 0).y) * p.idx - p.h) * p.dx2;
 }
 
 // Gradient dF/dA (out[0..1]) and dF/dpsi_c (out[2+2c..]) at one site,

@@ -129,6 +129,20 @@ class Oracle:
                                  _ptr(g2), int(maxwell))
         return ga, g1, g2
 
+    def energy_link(self, a, p1, p2=None):
+        """Per-image energy of the gauge-link (Peierls) discretisation."""
+        a, p1, p2 = self._state(a, p1, p2)
+        out = np.zeros(a.shape[0])
+        self._fn("glo_energy_link")(C.byref(self.S), a.shape[0], _ptr(a), _ptr(p1), _ptr(p2), _ptr(out))
+        return out
+
+    def gradient_link(self, a, p1, p2=None, maxwell=False):
+        a, p1, p2 = self._state(a, p1, p2)
+        ga, g1, g2 = (np.zeros_like(a) for _ in range(3))
+        self._fn("glo_gradient_link")(C.byref(self.S), a.shape[0], _ptr(a), _ptr(p1), _ptr(p2), _ptr(ga), _ptr(g1),
+                                      _ptr(g2), int(maxwell))
+        return ga, g1, g2
+
     def param_adjoint(self, a, p1, p2=None):
         """(F, 3): per-image dF/dH (uniform shift of h), dF/deta, dF/dgamma at fixed fields."""
         a, p1, p2 = self._state(a, p1, p2)

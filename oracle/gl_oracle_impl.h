@@ -160,6 +160,156 @@ void FN(glo_param_adjoint)(const PROB *P, int F, const REAL *A, const REAL *p1, 
     }
 }
 
+/* ------------------------------------------------- link discretisation
+ * Gauge-link (Peierls) form of the same functional, no reference
+ * counterpart.  A_e at site s is the link variable of the link s -> s + e;
+ * per link and component the kinetic energy is w_e / (2 m_e) |psi_t - U psi_s|^2
+ * with U = exp(i q A_e dx) (w_e, m_e: the reference's link weight and the mass
+ * at s); per plaquette with lower-left corner s, 1/2 v (B - h)^2 dx^2 with
+ * B = (A_x(s) + A_y(s+x) - A_x(s+y) - A_y(s)) / dx and v the validity of the
+ * reference's upper-right curl view; the condensation terms are unchanged.
+ * Under psi_c -> psi_c exp(i q_c chi), A_e(s) -> A_e(s) + (chi(s+e) - chi(s))/dx
+ * every term is invariant exactly (the eta and delta terms when q_1 = q_2). */
+static void FN(cis)(REAL a, REAL *c, REAL *s)
+{
+    *c = (REAL)cos((double)a);
+    *s = (REAL)sin((double)a);
+}
+
+static REAL FN(link_weight)(unsigned sc, int dir)
+{
+    return dir == 0 ? (REAL)(B_(sc, 0) ? (B_(sc, 1) * B_(sc, 2) + B_(sc, 6) * B_(sc, 7)) : 0) / (REAL)2
+                    : (REAL)(B_(sc, 2) ? (B_(sc, 0) * B_(sc, 1) + B_(sc, 3) * B_(sc, 4)) : 0) / (REAL)2;
+}
+
+static REAL FN(condensation)(const PROB *P, const REAL *const ps[2], long k, long s)
+{
+    REAL nl = 0;
+    for (int c = 0; c < P->ncomp; ++c) {
+        const REAL x = ps[c][2 * k], y = ps[c][2 * k + 1];
+        nl += P->b[c][s] / (REAL)2 * FN(sq)(P->a[c][s] / P->b[c][s] + FN(sq)(x) + FN(sq)(y));
+    }
+    if (P->ncomp == 2) {
+        const REAL x1 = ps[0][2 * k], y1 = ps[0][2 * k + 1], x2 = ps[1][2 * k], y2 = ps[1][2 * k + 1];
+        nl += P->eta * (x1 * x2 + y1 * y2);
+        nl += P->gamma / (REAL)2 * (FN(sq)(x1) + FN(sq)(y1)) * (FN(sq)(x2) + FN(sq)(y2));
+        nl += P->delta / (REAL)2 * (FN(sq)(x1 * x2 + y1 * y2) - FN(sq)(x1 * y2 - y1 * x2));
+    }
+    return nl;
+}
+
+static REAL FN(area)(unsigned sc)
+{
+    return (REAL)(B_(sc, 0) * B_(sc, 1) * B_(sc, 2) + B_(sc, 2) * B_(sc, 3) * B_(sc, 4)
+                  + B_(sc, 4) * B_(sc, 5) * B_(sc, 6) + B_(sc, 6) * B_(sc, 7) * B_(sc, 0)) / (REAL)4;
+}
+
+void FN(glo_energy_link)(const PROB *P, int F, const REAL *A, const REAL *p1, const REAL *p2, double *out)
+{
+    const REAL *ps[2] = {p1, p2};
+    const int nx = P->nx;
+    const long M = (long)nx * P->ny;
+    const REAL dx = P->dx;
+    GLO_OMP_FOR
+    for (int n = 0; n < F; ++n) {
+        FN(ksum) acc = {0, 0};
+        for (int j = 0; j < P->ny; ++j)
+            for (int i = 0; i < nx; ++i) {
+                const long s = i + (long)nx * j, k = n * M + s;
+                const unsigned sc = P->sc_nn[s], cc = P->comp_nn[s];
+                REAL e = FN(condensation)(P, ps, k, s) * FN(area)(sc) * dx * dx;
+                for (int dir = 0; dir < 2; ++dir) {
+                    const REAL w = FN(link_weight)(sc, dir);
+                    if (w == 0) continue;
+                    const long t = k + (dir == 0 ? 1 : nx);
+                    for (int c = 0; c < P->ncomp; ++c) {
+                        const REAL m = dir == 0 ? P->mxx[c][s] : P->myy[c][s];
+                        REAL cu, su;
+                        FN(cis)(P->q[c] * A[2 * k + dir] * dx, &cu, &su);
+                        const REAL *p = ps[c];
+                        const REAL zr = p[2 * t] - (cu * p[2 * k] - su * p[2 * k + 1]);
+                        const REAL zi = p[2 * t + 1] - (su * p[2 * k] + cu * p[2 * k + 1]);
+                        e += w / ((REAL)2 * m) * (zr * zr + zi * zi);
+                    }
+                }
+                if (!P->thin_film && B_(cc, 0) && B_(cc, 1) && B_(cc, 2)) {
+                    const REAL B = (A[2 * k] + A[2 * (k + 1) + 1] - A[2 * (k + nx)] - A[2 * k + 1]) / dx;
+                    e += (REAL)0.5 * FN(sq)(B - P->h[s]) * dx * dx;
+                }
+                FN(kadd)(&acc, (double)e);
+            }
+        out[n] = FN(kval)(&acc);
+    }
+}
+
+void FN(glo_gradient_link)(const PROB *P, int F, const REAL *A, const REAL *p1, const REAL *p2, REAL *gA,
+                           REAL *g1, REAL *g2, int maxwell)
+{
+    const REAL *ps[2] = {p1, p2};
+    REAL *gp[2] = {g1, g2};
+    const int nx = P->nx, nc = P->ncomp;
+    const long M = (long)nx * P->ny;
+    const REAL dx = P->dx;
+    GLO_OMP_FOR
+    for (int n = 0; n < F; ++n) {
+        memset(gA + 2 * n * M, 0, 2 * M * sizeof(REAL));
+        for (int c = 0; c < nc; ++c) memset(gp[c] + 2 * n * M, 0, 2 * M * sizeof(REAL));
+        for (int j = 0; j < P->ny; ++j)
+            for (int i = 0; i < nx; ++i) {
+                const long s = i + (long)nx * j, k = n * M + s;
+                const unsigned sc = P->sc_nn[s], cc = P->comp_nn[s];
+                const REAL ar = FN(area)(sc) * dx * dx;
+                if (!maxwell) {
+                    for (int c = 0; c < nc; ++c) {
+                        const REAL x = ps[c][2 * k], y = ps[c][2 * k + 1], r2 = x * x + y * y;
+                        gp[c][2 * k] += (REAL)2 * x * (P->a[c][s] + P->b[c][s] * r2) * ar;
+                        gp[c][2 * k + 1] += (REAL)2 * y * (P->a[c][s] + P->b[c][s] * r2) * ar;
+                    }
+                    if (nc == 2) {
+                        const REAL x1 = ps[0][2 * k], y1 = ps[0][2 * k + 1], x2 = ps[1][2 * k], y2 = ps[1][2 * k + 1];
+                        const REAL R = x1 * x2 + y1 * y2, I = x1 * y2 - y1 * x2;
+                        const REAL r1 = x1 * x1 + y1 * y1, r2 = x2 * x2 + y2 * y2;
+                        gp[0][2 * k] += (P->eta * x2 + P->gamma * x1 * r2 + P->delta * (R * x2 - I * y2)) * ar;
+                        gp[0][2 * k + 1] += (P->eta * y2 + P->gamma * y1 * r2 + P->delta * (R * y2 + I * x2)) * ar;
+                        gp[1][2 * k] += (P->eta * x1 + P->gamma * x2 * r1 + P->delta * (R * x1 + I * y1)) * ar;
+                        gp[1][2 * k + 1] += (P->eta * y1 + P->gamma * y2 * r1 + P->delta * (R * y1 - I * x1)) * ar;
+                    }
+                }
+                for (int dir = 0; dir < 2; ++dir) {
+                    const REAL w = FN(link_weight)(sc, dir);
+                    if (w == 0) continue;
+                    const long t = k + (dir == 0 ? 1 : nx);
+                    for (int c = 0; c < nc; ++c) {
+                        const REAL m = dir == 0 ? P->mxx[c][s] : P->myy[c][s], q = P->q[c];
+                        const REAL kk = w / ((REAL)2 * m);
+                        REAL cu, su;
+                        FN(cis)(q * A[2 * k + dir] * dx, &cu, &su);
+                        const REAL *p = ps[c];
+                        const REAL ur = cu * p[2 * k] - su * p[2 * k + 1], ui = su * p[2 * k] + cu * p[2 * k + 1];
+                        const REAL zr = p[2 * t] - ur, zi = p[2 * t + 1] - ui;
+                        if (!maxwell) {
+                            gp[c][2 * t] += (REAL)2 * kk * zr;
+                            gp[c][2 * t + 1] += (REAL)2 * kk * zi;
+                            /* -2k conj(U) z */
+                            gp[c][2 * k] += -(REAL)2 * kk * (cu * zr + su * zi);
+                            gp[c][2 * k + 1] += -(REAL)2 * kk * (cu * zi - su * zr);
+                        }
+                        /* 2k q dx Im(conj(z) U psi_s) */
+                        if (!P->thin_film) gA[2 * k + dir] += (REAL)2 * kk * q * dx * (zr * ui - zi * ur);
+                    }
+                }
+                if (!P->thin_film && B_(cc, 0) && B_(cc, 1) && B_(cc, 2)) {
+                    const REAL B = (A[2 * k] + A[2 * (k + 1) + 1] - A[2 * (k + nx)] - A[2 * k + 1]) / dx;
+                    const REAL r = (B - P->h[s]) * dx;
+                    gA[2 * k] += r;
+                    gA[2 * (k + 1) + 1] += r;
+                    gA[2 * (k + nx)] -= r;
+                    gA[2 * k + 1] -= r;
+                }
+            }
+    }
+}
+
 /* ---------------------------------------------------------------- gradient
  * Restates gradientPsi (nlcg.cu:504-744) and gradientA (nlcg.cu:746-888).
  * On a link i -> j along direction e the reference uses, per component,
