@@ -44,7 +44,10 @@ def time_within(t, v, target, rtol):
 
 
 def run(cfg: int, relax: int, iterations: int, schedule: str = "fp64", fp32_iterations: int = 0,
-        mode: str = "L"):
+        mode: str = "L", switch_window: int = 10, switch_tol: float = 1e-5):
+    """fp32_iterations < 0 (mixed): switch to FP64 once F_{F-1} - F_0 has
+    changed by at most switch_tol (relative) over switch_window iterations,
+    i.e. when FP32 has reached its resolution."""
     prob, st = _workload(cfg)
     prec = "fp32" if schedule in ("fp32", "mixed") else "fp64"
     c = native.StringContext(prob, st.n_images, prec, line_polynomial=native.POLY_EXACT,
@@ -53,9 +56,16 @@ def run(cfg: int, relax: int, iterations: int, schedule: str = "fp64", fp32_iter
     c.synchronize()
     rec = []
     t0 = time.perf_counter()
+    switched = schedule != "mixed"
     for it in range(iterations):
-        if schedule == "mixed" and it == fp32_iterations:
-            c.set_precision("fp64")
+        if not switched:
+            if fp32_iterations >= 0:
+                switched = it == fp32_iterations
+            elif len(rec) > switch_window:
+                e_now, e_old = rec[-1][3], rec[-1 - switch_window][3]
+                switched = abs(e_now - e_old) <= switch_tol * abs(e_now)
+            if switched:
+                c.set_precision("fp64")
         c.loop_iteration(mode, relax)
         fe = c.compute_free_energy()
         rec.append((time.perf_counter() - t0, float(fe.max() - fe[0]), int(fe.argmax()), float(fe[-1] - fe[0]),
@@ -84,22 +94,47 @@ def summarise(rec, target_ends=None, rtol=1e-6):
     return out
 
 
+def compare(paths, rtol=1e-6):
+    """Time for each saved run to bring F_{F-1} - F_0 within rtol of the first
+    run's final value (the first run is the long FP64 reference)."""
+    runs = [json.load(open(p)) for p in paths]
+    target = runs[0]["trace"][-1][3]
+    out = []
+    for p, r in zip(paths, runs):
+        tr = r["trace"]
+        out.append(dict(run=p, schedule=r["summary"]["schedule"], target_ends=target, rtol=rtol,
+                        time_to_ends_s=time_within([x[0] for x in tr], [x[3] for x in tr], target, rtol),
+                        wall_s=tr[-1][0], final_barrier=tr[-1][1]))
+    return out
+
+
 def main(argv=None):
     ap = argparse.ArgumentParser(description=__doc__.split("\n\n")[0])
+    ap.add_argument("--compare", nargs="+", default=None,
+                    help="saved runs (first = reference); print each run's time to its end-state value")
     ap.add_argument("--config", type=int, default=1)
     ap.add_argument("--relax", type=int, default=10)
     ap.add_argument("--iterations", type=int, default=1000)
     ap.add_argument("--schedule", choices=("fp64", "fp32", "mixed"), default="fp64")
-    ap.add_argument("--fp32-iterations", type=int, default=0)
+    ap.add_argument("--fp32-iterations", type=int, default=-1,
+                    help="mixed: outer iterations in FP32 (< 0: until F_end - F_0 plateaus)")
+    ap.add_argument("--switch-window", type=int, default=10)
+    ap.add_argument("--switch-tol", type=float, default=1e-5)
     ap.add_argument("--mode", choices=("L", "C"), default="L")
     ap.add_argument("--target-ends", type=float, default=None)
     ap.add_argument("--rtol", type=float, default=1e-6)
     ap.add_argument("--out", default=None)
     a = ap.parse_args(argv)
-    rec, sens = run(a.config, a.relax, a.iterations, a.schedule, a.fp32_iterations, a.mode)
+    if a.compare:
+        for row in compare(a.compare, a.rtol):
+            print(json.dumps(row))
+        return
+    rec, sens = run(a.config, a.relax, a.iterations, a.schedule, a.fp32_iterations, a.mode, a.switch_window,
+                    a.switch_tol)
     s = summarise(rec, a.target_ends, a.rtol)
     s.update(sens)
-    s.update(config=a.config, relax=a.relax, schedule=a.schedule, fp32_iterations=a.fp32_iterations, mode=a.mode)
+    fp32_its = sum(1 for r in rec if r[4] == "fp32")
+    s.update(config=a.config, relax=a.relax, schedule=a.schedule, fp32_iterations=fp32_its, mode=a.mode)
     print(json.dumps(s))
     if a.out:
         with open(a.out, "w") as f:

@@ -7,6 +7,7 @@ cmake; ``nvcc`` and ``g++`` are invoked directly.
 from __future__ import annotations
 
 import concurrent.futures as cf
+import json
 import os
 import shutil
 import subprocess
@@ -48,16 +49,31 @@ def _run(cmd):
     return r.stdout + r.stderr
 
 
+TUNING = os.path.join(PKG, "tuning.json")
+
+
+def tuned_flags() -> list:
+    """-D definitions chosen by mepgl_gb300.autotune (tuning.json), unless
+    MEPGL_NO_TUNING is set; MEPGL_NVCC_FLAGS given later on the command line wins."""
+    if os.environ.get("MEPGL_NO_TUNING") or not os.path.exists(TUNING):
+        return []
+    with open(TUNING) as f:
+        sel = json.load(f).get("selected", {})
+    return ["-D%s=%d" % (k, int(v)) for k, v in sorted(sel.items())]
+
+
 def build(force: bool = False, verbose: bool = False, ptxas_info: bool = False) -> str:
     os.makedirs(LIB_DIR, exist_ok=True)
     hdrs = [os.path.join(CSRC, h) for h in HEADERS] + [os.path.join(ROOT, "include", "mepgl.h")]
+    if os.path.exists(TUNING):
+        hdrs.append(TUNING)
     objs, jobs = [], []
     for src in CU_SOURCES:
         s = os.path.join(CSRC, src)
         o = os.path.join(LIB_DIR, src.replace(".cu", ".o"))
         objs.append(o)
         if force or ptxas_info or _stale(o, [s] + hdrs):
-            extra = os.environ.get("MEPGL_NVCC_FLAGS", "").split()
+            extra = tuned_flags() + os.environ.get("MEPGL_NVCC_FLAGS", "").split()
             cmd = [nvcc()] + ARCH + NVCC_FLAGS + extra + (["-Xptxas", "-v"] if ptxas_info else []) + ["-c", s, "-o", o]
             jobs.append(cmd)
     with cf.ThreadPoolExecutor(max_workers=max(1, len(jobs))) as ex:

@@ -1,0 +1,66 @@
+"""The large workload: a 2048x2048 two-component string of 128 images.
+
+q1 = 1, q2 = 0.5, delta = 0.1, eta = 0, gamma = 0.3, H = 1.1, dx = 0.25,
+superconducting domain a disk of radius 1000 lattice units, Meissner to one
+composite vortex 20 units inside the rim (built on the device,
+mepgl_gb300.workloads.config5_device).  The FP32 state (x, g, d, two
+buffers each) takes 77 GB, the FP64 state 155 GB, inside 180 GB.
+
+Reports, per precision, the NLCG step time (CUDA events on the context's
+stream), the site·image throughput and the HBM rate of each pass in
+algorithmic bytes (k_grad 5S + M, k_dir_poly 4S + M per site·image).
+
+    python -m mepgl_gb300.large [--n 2048] [--images 128] [--steps 6] [--fp64-steps 2]
+"""
+from __future__ import annotations
+
+import argparse
+import json
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser(description=__doc__.split("\n\n")[0])
+    ap.add_argument("--n", type=int, default=2048)
+    ap.add_argument("--images", type=int, default=128)
+    ap.add_argument("--steps", type=int, default=6)
+    ap.add_argument("--fp64-steps", type=int, default=2)
+    a = ap.parse_args(argv)
+    import torch
+    from . import native, workloads
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    units = a.n * a.n * a.images
+    out = dict(workload="two-component GL %dx%d dx=0.25, %d images, disk domain" % (a.n, a.n, a.images),
+               site_images=units)
+    for prec, steps, tdt in (("fp32", a.steps, torch.float32), ("fp64", a.fp64_steps, torch.float64)):
+        if steps <= 0:
+            continue
+        prob, (fa, f1, f2) = workloads.config5_device(a.n, a.images, dtype=tdt)
+        ctx = native.StringContext(prob, a.images, prec, stream=stream.cuda_stream, line_polynomial=native.POLY_EXACT)
+        torch.cuda.synchronize()
+        ctx.set_state_device(fa.data_ptr(), f1.data_ptr(), f2.data_ptr())
+        ctx.synchronize()
+        del fa, f1, f2
+        torch.cuda.empty_cache()
+        ctx.nlcg_steps(2)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        ctx.nlcg_steps(steps)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / steps
+        mg, md = ctx.profile_passes(2)
+        S = 6 * (4 if prec == "fp32" else 8)
+        bg, bd = (5 * S + 2) * units, (4 * S + 2) * units
+        out[prec] = dict(ms_per_step=ms, value=units / (ms / 1e3), unit="site·image/s",
+                         k_grad=dict(ms=mg, gbs=bg / mg / 1e6), k_dir_poly=dict(ms=md, gbs=bd / md / 1e6),
+                         step_gbs=(bg + bd) / ms / 1e6, device_gb=torch.cuda.mem_get_info()[1] / 1e9 -
+                         torch.cuda.mem_get_info()[0] / 1e9)
+        ctx.close()
+        torch.cuda.empty_cache()
+    print(json.dumps(out))
+
+
+if __name__ == "__main__":
+    main()

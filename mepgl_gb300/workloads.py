@@ -194,3 +194,35 @@ def random_state(rng, prob, images=4, amp=0.3):
     p1 = 0.8 + amp * rng.standard_normal(sh)
     p2 = 0.6 + amp * rng.standard_normal(sh) if prob.multicomponent else None
     return StringState(a=a, psi_1=p1, psi_2=p2)
+
+
+def config5_device(n: int = 2048, images: int = 128, seed: int = 1005, dx: float = 0.25, dtype=None,
+                   device="cuda"):
+    """The large workload built directly in device memory: ``config5``'s
+    problem and end states, the linear interpolation and the noise formed by
+    torch on the GPU (a 2048^2 x 128 string is 13 GB in FP32; the noise comes
+    from torch's generator seeded with ``seed``, not from numpy's stream).
+    Returns (Problem, (a, psi_1, psi_2)) with CUDA tensors (F, n, n, 2)."""
+    import torch
+    dtype = dtype or torch.float32
+    r0 = 1000.0 * n / 2048.0
+    jj, ii = np.meshgrid(np.arange(n), np.arange(n), indexing="ij")
+    c = (n - 1) / 2.0
+    disk = (((ii - c) ** 2 + (jj - c) ** 2) <= r0 ** 2).astype(np.int32)
+    comp = np.ones((n, n), np.int32)
+    prob = Problem.uniform(n, n, dx, a=(-1.0, -1.0), b=(1.0, 1.0), h=1.1, q=(1.0, 0.5), eta=0.0, gamma=0.3,
+                           delta=0.1, multicomponent=True, comp_domain=comp, sc_domain=disk)
+    i0 = c - r0 + 20 * n / 2048.0
+    end = torch.tensor(_vortex(n, dx, i0=i0, j0=c, psi_inf=1.0), dtype=dtype, device=device)
+    start = torch.tensor(_meissner(n, 1.0), dtype=dtype, device=device)
+    sc = torch.tensor(disk, dtype=dtype, device=device)[None, :, :, None]
+    g = torch.Generator(device=device)
+    g.manual_seed(seed)
+    t = torch.linspace(0.0, 1.0, images, dtype=dtype, device=device)[:, None, None, None]
+    out = []
+    for k in range(2):
+        p = (1 - t) * start[None] + t * end[None]
+        p += 1e-4 * torch.randn(p.shape, generator=g, dtype=dtype, device=device)
+        out.append((p * sc).contiguous())
+    a = (1e-4 * torch.randn((images, n, n, 2), generator=g, dtype=dtype, device=device)).contiguous()
+    return prob, (a, out[0], out[1])
