@@ -29,17 +29,19 @@ PKG = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(PKG)
 TUNING = os.path.join(PKG, "tuning.json")
 
-# (rows per FP32 tile, min blocks per SM for the gradient pass, for the direction pass)
-CANDIDATES = [(16, 4, 4), (16, 4, 3), (16, 3, 3), (16, 5, 4), (8, 4, 4), (8, 5, 4), (32, 3, 3), (32, 4, 3)]
+# (rows per FP32 tile, min blocks per SM for the gradient pass, for the
+# direction pass, gradient-pass halo copy: 0 through registers, 1 cp.async)
+CANDIDATES = [(16, 4, 4, 0), (16, 4, 4, 1), (16, 3, 4, 1), (16, 5, 4, 1), (16, 5, 4, 0), (16, 4, 3, 0),
+              (8, 5, 4, 1), (32, 4, 3, 1)]
 
 
 def defines(c):
-    rows, g, d = c
-    return {"MEPGL_ROWS_F32": rows, "MEPGL_MINB_GRAD": g, "MEPGL_MINB_DIR": d}
+    rows, g, d, a = c
+    return {"MEPGL_ROWS_F32": rows, "MEPGL_MINB_GRAD": g, "MEPGL_MINB_DIR": d, "MEPGL_GRAD_ASYNC": a}
 
 
 def _build(c, base):
-    d = os.path.join(base, "r%d_g%d_d%d" % c)
+    d = os.path.join(base, "r%d_g%d_d%d_a%d" % c)
     env = dict(os.environ, MEPGL_LIB_DIR=d,
                MEPGL_NVCC_FLAGS=" ".join("-D%s=%d" % kv for kv in defines(c).items()), MEPGL_NO_TUNING="1")
     r = subprocess.run([sys.executable, "-c", "from mepgl_gb300 import build; build.build(force=True)"], cwd=ROOT,

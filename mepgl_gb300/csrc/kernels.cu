@@ -41,6 +41,12 @@ namespace mepgl {
 #define MEPGL_MINB_DIR 4
 #endif
 
+// 1: the gradient pass copies the raw x and d halo tiles with cp.async and
+// forms x + alpha d in shared memory; 0: through registers (stage mode 1)
+#ifndef MEPGL_GRAD_ASYNC
+#define MEPGL_GRAD_ASYNC 0
+#endif
+
 template <class T> struct TileRows { static constexpr int v = sizeof(T) == 4 ? MEPGL_ROWS_F32 : MEPGL_ROWS_F64; };
 
 int tile_rows(int precision) { return precision == 1 ? TileRows<double>::v : TileRows<float>::v; }
@@ -134,6 +140,62 @@ __device__ __forceinline__ void stage(Tile<T, NC, TYT> &t, const StringDesc &S, 
 #pragma unroll
         for (int c = 0; c < NC; ++c) t.P[c][hy][hx] = v[1 + c];
         if (masks) t.m[hy][hx] = m[k];
+    }
+}
+
+// Asynchronous copy of a plain halo tile (no arithmetic on the values):
+// cp.async per element, zero-filled outside the lattice, so its latency
+// overlaps the register-staged arrays that follow.  The neighbour codes
+// (2 bytes, below the 4-byte copy size) are loaded into m[] for the caller
+// to store; cp_async_wait_all() + a barrier complete the tile.
+__device__ __forceinline__ unsigned smem_u32(const void *p) { return (unsigned)__cvta_generic_to_shared(p); }
+
+template <int BYTES>
+__device__ __forceinline__ void cp_async(void *dst, const void *src, bool valid)
+{
+    const int n = valid ? BYTES : 0;
+    if (BYTES == 16)
+        asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(smem_u32(dst)), "l"(src), "r"(n)
+                     : "memory");
+    else
+        asm volatile("cp.async.ca.shared.global [%0], [%1], %2, %3;\n" ::"r"(smem_u32(dst)), "l"(src), "n"(BYTES),
+                     "r"(n)
+                     : "memory");
+}
+
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
+
+template <class T, int NC, int TYT>
+__device__ __forceinline__ void stage_async(TileF<T, NC, TYT> &t, const StringDesc &S,
+                                            const vec2_t<T> *const *src, int i0, int j0, uint16_t *m)
+{
+    using V = vec2_t<T>;
+    constexpr int HW = TX + 2, HE = (TYT + 2) * HW, NI = (HE + NT - 1) / NT;
+#pragma unroll
+    for (int k = 0; k < NI; ++k) {
+        const int e = threadIdx.x + k * NT;
+        if (m) m[k] = 0;
+        if (e >= HE) continue;
+        const int hy = e / HW, hx = e - hy * HW;
+        const int gi = i0 + hx - 1, gj = j0 + hy - 1;
+        const bool ok = gi >= 0 && gi < S.nx && gj >= 0 && gj < S.ny;
+        const int s = ok ? gi + S.nx * gj : 0;
+        cp_async<sizeof(V)>(&t.A[hy][hx], src[0] + s, ok);
+#pragma unroll
+        for (int c = 0; c < NC; ++c) cp_async<sizeof(V)>(&t.P[c][hy][hx], src[1 + c] + s, ok);
+        if (m && ok) m[k] = S.mask[s];
+    }
+}
+
+template <class T, int NC, int TYT>
+__device__ __forceinline__ void store_codes(Tile<T, NC, TYT> &t,
+                                            const uint16_t (&m)[(((TYT + 2) * (TX + 2)) + NT - 1) / NT])
+{
+    constexpr int HW = TX + 2, HE = (TYT + 2) * HW, NI = (HE + NT - 1) / NT;
+#pragma unroll
+    for (int k = 0; k < NI; ++k) {
+        const int e = threadIdx.x + k * NT;
+        if (e < HE) t.m[e / HW][e % HW] = m[k];
     }
 }
 
@@ -266,6 +328,9 @@ __global__ void __launch_bounds__(NT, MEPGL_MINB_GRAD) k_grad(const __grid_const
     constexpr int TYT = TileRows<T>::v;
     using V = vec2_t<T>;
     __shared__ Tile<T, NC, TYT> t;
+#if MEPGL_GRAD_ASYNC
+    __shared__ TileF<T, NC, TYT> dt;
+#endif
     __shared__ double red[NT / 32 * 2];
     for (int tt = blockIdx.x; tt < n_tiles; tt += gridDim.x) {
         const TileRef tr = tiles[tt];
@@ -275,7 +340,48 @@ __global__ void __launch_bounds__(NT, MEPGL_MINB_GRAD) k_grad(const __grid_const
         const size_t off = (size_t)tr.n * S.nx * S.ny;
         ImagePtrs<T, NC> ip;
         image_ptrs<T, NC>(ip, S.x[f.xin], S.d[f.din], S.x[f.xout], off);
+#if MEPGL_GRAD_ASYNC
+        {
+            constexpr int HW = TX + 2, HE = (TYT + 2) * HW, NI = (HE + NT - 1) / NT;
+            const T alpha = (T)sc.alpha_pend[img];
+            uint16_t codes[NI];
+            stage_async<T, NC, TYT>(t, S, ip.in, i0, j0, codes);
+            if (alpha != (T)0) stage_async<T, NC, TYT>(dt, S, ip.aux, i0, j0, nullptr);
+            store_codes<T, NC, TYT>(t, codes);
+            cp_async_wait_all();
+            __syncthreads();
+            // x <- x + alpha d over the halo tile; interior x -> x[xout]
+#pragma unroll
+            for (int k = 0; k < NI; ++k) {
+                const int e = threadIdx.x + k * NT;
+                if (e >= HE) continue;
+                const int hy = e / HW, hx = e - hy * HW;
+                V v[1 + NC];
+                v[0] = t.A[hy][hx];
+#pragma unroll
+                for (int c = 0; c < NC; ++c) v[1 + c] = t.P[c][hy][hx];
+                if (alpha != (T)0) {
+                    V dv = dt.A[hy][hx];
+                    v[0].x = v[0].x + alpha * dv.x;
+                    v[0].y = v[0].y + alpha * dv.y;
+                    t.A[hy][hx] = v[0];
+#pragma unroll
+                    for (int c = 0; c < NC; ++c) {
+                        dv = dt.P[c][hy][hx];
+                        v[1 + c].x = v[1 + c].x + alpha * dv.x;
+                        v[1 + c].y = v[1 + c].y + alpha * dv.y;
+                        t.P[c][hy][hx] = v[1 + c];
+                    }
+                }
+                const int gi = i0 + hx - 1, gj = j0 + hy - 1;
+                if (hx >= 1 && hx <= TX && hy >= 1 && hy <= TYT && gi < S.nx && gj < S.ny)
+#pragma unroll
+                    for (int c = 0; c < 1 + NC; ++c) ip.out[c][gi + S.nx * gj] = v[c];
+            }
+        }
+#else
         stage<T, NC, TYT, 1>(t, S, ip, i0, j0, (T)sc.alpha_pend[img], true, true);
+#endif
         V *gcur[1 + NC];
         const V *gprev[1 + NC];
 #pragma unroll
@@ -288,6 +394,17 @@ __global__ void __launch_bounds__(NT, MEPGL_MINB_GRAD) k_grad(const __grid_const
         __syncthreads();
         T v[2] = {(T)0, (T)0};
         const int lx = threadIdx.x & 31, gi = i0 + lx;
+        // previous gradient of this thread's sites, loaded before the stencil
+        V gold[TYT / 8][1 + NC];
+#pragma unroll
+        for (int r = 0; r < TYT / 8; ++r) {
+            const int gj = j0 + (threadIdx.x >> 5) + 8 * r;
+#pragma unroll
+            for (int c = 0; c < 1 + NC; ++c) {
+                gold[r][c].x = gold[r][c].y = (T)0;
+                if (gi < S.nx && gj < S.ny) gold[r][c] = gprev[c][gi + S.nx * gj];
+            }
+        }
 #pragma unroll
         for (int r = 0; r < TYT / 8; ++r) {
             const int ly = (threadIdx.x >> 5) + 8 * r, gj = j0 + ly;
@@ -311,7 +428,7 @@ __global__ void __launch_bounds__(NT, MEPGL_MINB_GRAD) k_grad(const __grid_const
                     gv.x = g[2 * c];
                     gv.y = g[2 * c + 1];
                     gcur[c][s] = gv;
-                    const V go = gprev[c][s];
+                    const V go = gold[r][c];
                     v[0] += gv.x * gv.x + gv.y * gv.y;
                     v[1] += gv.x * (gv.x - go.x) + gv.y * (gv.y - go.y);
                 }
@@ -352,8 +469,11 @@ __global__ void __launch_bounds__(NT, MEPGL_MINB_DIR) k_dir_poly(const __grid_co
         ImagePtrs<T, NC> ipx, ipd;
         image_ptrs<T, NC>(ipx, S.x[f.xout], nullptr, nullptr, off);
         image_ptrs<T, NC>(ipd, S.d[f.din], S.g[f.gcur], S.d[f.dout], off);
-        stage<T, NC, TYT, 0>(tx, S, ipx, i0, j0, (T)0, false, true);
+        uint16_t codes[((TYT + 2) * (TX + 2) + NT - 1) / NT];
+        stage_async<T, NC, TYT>(tx, S, ipx.in, i0, j0, codes);
         stage<T, NC, TYT, 2>(td, S, ipd, i0, j0, (T)sc.beta[img], true, false);
+        store_codes<T, NC, TYT>(tx, codes);
+        cp_async_wait_all();
         SiteParams<T> p;
         p.load_uniform(S);
         __syncthreads();
