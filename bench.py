@@ -115,6 +115,21 @@ def dist_env():
     return world, rank, local
 
 
+def max_over_ranks(x: float, world: int, device="cuda") -> float:
+    """The largest of each rank's x (the slowest replica's time); identity for one rank."""
+    if world == 1:
+        return x
+    import torch
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replicas_value(world: int, units_per_step: int, steps: int, ms_max: float) -> float:
+    """Whole-job throughput of `world` replicas: every rank's units over the slowest rank's time."""
+    return world * units_per_step * steps / (ms_max / 1e3)
+
+
 def cpu_oracle_step_rate(prob, st, images: int, steps: int, dtype, budget_s: float = 12.0):
     """Time the C oracle (OpenMP over images) on a sample of `images` images."""
     import numpy as np
@@ -197,11 +212,7 @@ def run_ours(args):
             torch.distributed.barrier()
 
     def maxed(x):
-        if world == 1:
-            return x
-        t = torch.tensor([x], dtype=torch.float64, device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        return float(t.item())
+        return max_over_ranks(x, world, "cuda")
 
     # ---- device-resident timed region (FP32 bulk relaxation) ----------------
     ctx.nlcg_steps(max(args.warmup, 3))
@@ -216,7 +227,7 @@ def run_ours(args):
         barrier()
     ms = maxed(ev0.elapsed_time(ev1))
     launches = ctx.info()["kernel_launches"] - l0
-    value = world * units_per_step * args.steps / (ms / 1e3)
+    value = replicas_value(world, units_per_step, args.steps, ms)
     fe = ctx.image_scalars()["fenergy"]
     assert np.all(np.isfinite(fe)), "non-finite energies"
 
