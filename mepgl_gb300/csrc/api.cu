@@ -407,7 +407,7 @@ mepgl_status one_step(mepgl_ctx *c, int it, int use_cg, int maxwell)
     for (int b = 0; b < nb; ++b) CK(c, launch_dir_poly(make_launch(c, b), c->sc, f));
     c->xi ^= 1;
     c->di ^= 1;
-    c->launches += 2 * nb;
+    c->launches += (int64_t)nlcg_step_launches() * nb;
     c->pending = true;
     return MEPGL_OK;
 }
@@ -449,7 +449,7 @@ mepgl_status nlcg_steps(mepgl_ctx *c, int iters, int use_cg, int maxwell)
         if (st != MEPGL_OK) return st;
         for (; it + 1 <= iters; it += 2) {
             CK(c, cudaGraphLaunch(ex, c->stream));
-            c->launches += 4 * (int64_t)c->batches.size();
+            c->launches += 2 * (int64_t)nlcg_step_launches() * c->batches.size();
         }
         c->pending = true;
     }
@@ -1069,7 +1069,7 @@ mepgl_status mepgl_profile_passes(mepgl_ctx *c, int steps, int use_cg, double *m
         CK(c, cudaEventRecord(ev[2 * it], c->stream));
         c->xi ^= 1;
         c->di ^= 1;
-        c->launches += 2 * nb;
+        c->launches += (int64_t)nlcg_step_launches() * nb;
         c->pending = true;
     }
     CK(c, cudaEventSynchronize(ev[2 * steps]));

@@ -41,6 +41,12 @@ namespace mepgl {
 #define MEPGL_MINB_DIR 4
 #endif
 
+// 1: the direction d = -g + beta d is formed by a pointwise pass and the
+// polynomial pass copies the x and d halo tiles with cp.async; 0: one fused
+// pass forms d over the halo tile in registers
+#ifndef MEPGL_SPLIT_DIR
+#define MEPGL_SPLIT_DIR 0
+#endif
 // 1: the gradient pass copies the raw x and d halo tiles with cp.async and
 // forms x + alpha d in shared memory; 0: through registers (stage mode 1)
 #ifndef MEPGL_GRAD_ASYNC
@@ -48,6 +54,8 @@ namespace mepgl {
 #endif
 
 template <class T> struct TileRows { static constexpr int v = sizeof(T) == 4 ? MEPGL_ROWS_F32 : MEPGL_ROWS_F64; };
+
+int nlcg_step_launches() { return 2 + MEPGL_SPLIT_DIR; }
 
 int tile_rows(int precision) { return precision == 1 ? TileRows<double>::v : TileRows<float>::v; }
 
@@ -471,7 +479,14 @@ __global__ void __launch_bounds__(NT, MEPGL_MINB_DIR) k_dir_poly(const __grid_co
         image_ptrs<T, NC>(ipd, S.d[f.din], S.g[f.gcur], S.d[f.dout], off);
         uint16_t codes[((TYT + 2) * (TX + 2) + NT - 1) / NT];
         stage_async<T, NC, TYT>(tx, S, ipx.in, i0, j0, codes);
+#if MEPGL_SPLIT_DIR
+        const vec2_t<T> *dsrc[1 + NC];
+#pragma unroll
+        for (int c = 0; c < 1 + NC; ++c) dsrc[c] = ipd.out[c];
+        stage_async<T, NC, TYT>(td, S, dsrc, i0, j0, nullptr);
+#else
         stage<T, NC, TYT, 2>(td, S, ipd, i0, j0, (T)sc.beta[img], true, false);
+#endif
         store_codes<T, NC, TYT>(tx, codes);
         cp_async_wait_all();
         SiteParams<T> p;
@@ -514,6 +529,49 @@ __global__ void __launch_bounds__(NT, MEPGL_MINB_DIR) k_dir_poly(const __grid_co
             }
         }
         __syncthreads();
+    }
+}
+
+// d[dout] = -g + beta d[din] at every site of the launch's tiles (the
+// pointwise half of computeStepDirection, nlcg.cu:955-994, when the
+// direction and polynomial passes are split).
+template <class T, int NC>
+__global__ void __launch_bounds__(NT) k_dir_update(const __grid_constant__ Batch bt,
+                                                   const TileRef *__restrict__ tiles, int n_tiles, Scalars sc,
+                                                   StepFlags f)
+{
+    constexpr int TYT = TileRows<T>::v;
+    using V = vec2_t<T>;
+    for (int tt = blockIdx.x; tt < n_tiles; tt += gridDim.x) {
+        const TileRef tr = tiles[tt];
+        const StringDesc &S = bt.s[tr.s];
+        const T beta = (T)sc.beta[S.img_base + tr.n];
+        const size_t off = (size_t)tr.n * S.nx * S.ny;
+        const int gi = tr.tx * TX + (threadIdx.x & 31);
+        V gv[TYT / 8][1 + NC], dv[TYT / 8][1 + NC];
+#pragma unroll
+        for (int r = 0; r < TYT / 8; ++r) {
+            const int gj = tr.ty * TYT + (threadIdx.x >> 5) + 8 * r;
+            if (gi < S.nx && gj < S.ny)
+#pragma unroll
+                for (int c = 0; c < 1 + NC; ++c) {
+                    const int s = gi + S.nx * gj;
+                    gv[r][c] = (static_cast<const V *>(S.g[f.gcur][c]) + off)[s];
+                    dv[r][c] = (static_cast<const V *>(S.d[f.din][c]) + off)[s];
+                }
+        }
+#pragma unroll
+        for (int r = 0; r < TYT / 8; ++r) {
+            const int gj = tr.ty * TYT + (threadIdx.x >> 5) + 8 * r;
+            if (gi < S.nx && gj < S.ny)
+#pragma unroll
+                for (int c = 0; c < 1 + NC; ++c) {
+                    V v;
+                    v.x = -gv[r][c].x + beta * dv[r][c].x;
+                    v.y = -gv[r][c].y + beta * dv[r][c].y;
+                    (static_cast<V *>(S.d[f.dout][c]) + off)[gi + S.nx * gj] = v;
+                }
+        }
     }
 }
 
@@ -952,6 +1010,15 @@ cudaError_t launch_grad(const Launch &L, const Scalars &sc, const StepFlags &f)
 
 cudaError_t launch_dir_poly(const Launch &L, const Scalars &sc, const StepFlags &f)
 {
+#if MEPGL_SPLIT_DIR
+    {
+        Launch U = L;
+        U.grid = L.n_tiles < 152 * 16 ? L.n_tiles : 152 * 16;
+        DISPATCH(U, k_dir_update, *U.batch, U.tiles, U.n_tiles, sc, f);
+        cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) return e;
+    }
+#endif
     DISPATCH(L, k_dir_poly, *L.batch, L.tiles, L.n_tiles, sc, f);
     return cudaGetLastError();
 }

@@ -9,6 +9,8 @@ constexpr int LS_GRID = 2001;         // line-search grid points x_0 .. x_2000
 
 // Rows per lattice tile for a precision (0 float, 1 double); tiles are TX wide.
 int tile_rows(int precision);
+// Kernel launches per NLCG step and launch group (2, or 3 with the split direction pass).
+int nlcg_step_launches();
 // Copy the neighbour-code weight tables to constant memory (idempotent).
 cudaError_t upload_mask_tables();
 
