@@ -55,6 +55,12 @@ enum { MEPGL_REDIST_LINEAR = 0, MEPGL_REDIST_CUBIC = 1 };
  * U = exp(i q A dx) with one curl per plaquette (exactly gauge invariant; no
  * reference counterpart; energy, gradient and adjoints only, no NLCG). */
 enum { MEPGL_DISC_REFERENCE = 0, MEPGL_DISC_LINK = 1 };
+/* Arithmetic of the two NLCG passes for FP64 fields: IEEE double, or
+ * float-float pairs on the FP32 pipes (about 48 significant bits, several
+ * times faster on GPUs whose FP64 rate is a small fraction of FP32).  Fields,
+ * reductions, line search and every other kernel stay double.  No
+ * reference counterpart. */
+enum { MEPGL_FP64_NATIVE = 0, MEPGL_FP64_PAIRED = 1 };
 
 /* The physical problem.  Replaces the generated headers config.cuh/real.cuh
  * (N, dx, MULTICOMPONENT, NO_SELF_FIELD, DOUBLE_PRECISION) and the lattice
@@ -86,6 +92,7 @@ typedef struct mepgl_options {
     int32_t use_graphs;        /* capture NLCG steps as CUDA graphs (default 1) */
     int32_t tile_rows;         /* rows per stencil tile: 0 = auto, 4, 8 or 16   */
     int32_t discretization;    /* MEPGL_DISC_*                                  */
+    int32_t fp64_arith;        /* MEPGL_FP64_*                                  */
 } mepgl_options;
 
 typedef struct mepgl_ctx mepgl_ctx;

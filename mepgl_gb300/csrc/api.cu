@@ -225,6 +225,22 @@ void fill_desc(mepgl_ctx *c, int si, int img_base, int tile_base)
     Uf.idx = (float)U.idx;
     Uf.dx2 = (float)s.dx * (float)s.dx;
     Uf.dx = (float)s.dx;
+    Uniform<ff> &Up = D.uff;      // the double values split into float pairs
+    for (int k = 0; k < 2; ++k) {
+        Up.a[k] = ff(U.a[k]);
+        Up.b[k] = ff(U.b[k]);
+        Up.hmx[k] = ff(U.hmx[k]);
+        Up.hmy[k] = ff(U.hmy[k]);
+        Up.aob[k] = ff(U.aob[k]);
+        Up.q[k] = ff(U.q[k]);
+    }
+    Up.eta = ff(U.eta);
+    Up.gamma = ff(U.gamma);
+    Up.delta = ff(U.delta);
+    Up.h = ff(U.h);
+    Up.idx = ff(U.idx);
+    Up.dx2 = ff(U.dx2);
+    Up.dx = ff(U.dx);
     D.disc = c->opt.discretization;
     D.ph = s.dparams[8];
     D.mask = s.dmask;
@@ -366,6 +382,7 @@ Launch make_launch(mepgl_ctx *c, int batch, int si = -1)
     L.n_tiles = si >= 0 ? c->string_ntiles[si] : c->batch_ntiles[batch];
     L.grid = L.n_tiles;
     L.precision = c->precision;
+    L.paired = c->opt.fp64_arith == MEPGL_FP64_PAIRED ? 1 : 0;
     L.ncomp = c->ncomp;
     L.stream = c->stream;
     return L;
@@ -654,6 +671,7 @@ void mepgl_default_options(mepgl_options *o)
     o->use_graphs = 1;
     o->tile_rows = 0;
     o->discretization = MEPGL_DISC_REFERENCE;
+    o->fp64_arith = MEPGL_FP64_NATIVE;
 }
 
 const char *mepgl_version(void) { return "mepgl_gb300 0.1 (sm_103a)"; }
@@ -695,9 +713,10 @@ mepgl_status mepgl_create_batch(const mepgl_problem *probs, int n_strings, const
     mepgl_ctx *c = new mepgl_ctx();
     if (opt) c->opt = *opt;
     else mepgl_default_options(&c->opt);
-    if (c->opt.discretization != MEPGL_DISC_REFERENCE && c->opt.discretization != MEPGL_DISC_LINK) {
+    if ((c->opt.discretization != MEPGL_DISC_REFERENCE && c->opt.discretization != MEPGL_DISC_LINK) ||
+        (c->opt.fp64_arith != MEPGL_FP64_NATIVE && c->opt.fp64_arith != MEPGL_FP64_PAIRED)) {
         delete c;
-        return fail(nullptr, MEPGL_ERR_INVALID_ARG, "mepgl_create: unknown discretization");
+        return fail(nullptr, MEPGL_ERR_INVALID_ARG, "mepgl_create: unknown discretization or fp64_arith");
     }
     c->ncomp = p->multicomponent ? 2 : 1;
     c->thin_film = p->thin_film ? 1 : 0;

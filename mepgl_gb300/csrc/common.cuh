@@ -17,6 +17,8 @@
 #include <cstdint>
 #include <cuda_runtime.h>
 
+#include "pair_float.cuh"
+
 namespace mepgl {
 
 constexpr int TX = 32;        // tile width: one warp per tile row
@@ -26,7 +28,34 @@ constexpr int MAX_STRINGS = 16;   // strings per launch (descriptors travel as a
 template <class T> struct Vec2;
 template <> struct Vec2<float> { using type = float2; };
 template <> struct Vec2<double> { using type = double2; };
+template <> struct Vec2<ff> { using type = ff2; };
 template <class T> using vec2_t = typename Vec2<T>::type;
+
+// Storage type of a compute type: float-float arithmetic works on double
+// fields (the paired FP64 mode); float and double are stored as computed.
+template <class T> struct Store { using type = T; };
+template <> struct Store<ff> { using type = double; };
+template <class T> using store_t = typename Store<T>::type;
+
+template <class T> __device__ __forceinline__ T from_store(store_t<T> v) { return v; }
+template <> __device__ __forceinline__ ff from_store<ff>(double v) { return to_ff(v); }
+template <class T> __device__ __forceinline__ store_t<T> to_store(T v) { return v; }
+template <> __device__ __forceinline__ double to_store<ff>(ff v) { return to_double(v); }
+
+template <class T> __device__ __forceinline__ vec2_t<T> load2(const vec2_t<store_t<T>> *p) { return *p; }
+template <> __device__ __forceinline__ ff2 load2<ff>(const double2 *p)
+{
+    const double2 d = *p;
+    ff2 r;
+    r.x = to_ff(d.x);
+    r.y = to_ff(d.y);
+    return r;
+}
+template <class T> __device__ __forceinline__ void store2(vec2_t<store_t<T>> *p, vec2_t<T> v) { *p = v; }
+template <> __device__ __forceinline__ void store2<ff>(double2 *p, ff2 v)
+{
+    *p = make_double2(to_double(v.x), to_double(v.y));
+}
 
 // Uniform GL parameters in one precision (hm* = 0.5 / m, aob = a / b).
 template <class T>
@@ -49,6 +78,7 @@ struct StringDesc {
     int per_site;             // 1: parameters read from the arrays below
     Uniform<float> uf;
     Uniform<double> ud;
+    Uniform<ff> uff;          // ud split into float pairs (paired FP64 mode)
     const void *pa[2], *pb[2], *pmxx[2], *pmyy[2], *ph;  // per-site (type T)
     const uint16_t *mask;     // per site: comp code | sc code << 8
     const int32_t *code_comp, *code_sc;   // used when mask is null: int32 codes per site
@@ -58,6 +88,7 @@ struct StringDesc {
 };
 template <> __host__ __device__ inline const Uniform<float> &StringDesc::u<float>() const { return uf; }
 template <> __host__ __device__ inline const Uniform<double> &StringDesc::u<double>() const { return ud; }
+template <> __host__ __device__ inline const Uniform<ff> &StringDesc::u<ff>() const { return uff; }
 
 // Descriptors of the strings covered by one launch; passed by value as a
 // __grid_constant__ kernel parameter, i.e. read through the constant cache.
@@ -101,7 +132,7 @@ __device__ __forceinline__ void block_sum(const T (&v)[NV], double (&out)[NV], d
     for (int k = 0; k < NV; ++k) {
         w[k] = v[k];
 #pragma unroll
-        for (int o = 16; o > 0; o >>= 1) w[k] += __shfl_down_sync(0xffffffffu, w[k], o);
+        for (int o = 16; o > 0; o >>= 1) w[k] += shfl_down(w[k], o);
     }
     const int wi = threadIdx.x >> 5, l = threadIdx.x & 31;
     if (l == 0)

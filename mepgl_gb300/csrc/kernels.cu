@@ -21,6 +21,8 @@
 // a one-site halo in shared memory; each thread computes TileRows/8 sites of
 // one column.  Addresses inside an image are 32-bit offsets from per-tile
 // base pointers.
+#include <type_traits>
+
 #include "kernels.cuh"
 #include "site_ops.cuh"
 
@@ -53,7 +55,18 @@ namespace mepgl {
 #define MEPGL_GRAD_ASYNC 0
 #endif
 
+// the float-float passes hold twice the registers of FP32 ones
+#ifndef MEPGL_MINB_GRAD_FF
+#define MEPGL_MINB_GRAD_FF 4
+#endif
+#ifndef MEPGL_MINB_DIR_FF
+#define MEPGL_MINB_DIR_FF 4
+#endif
+template <class T> struct MinBlocks { static constexpr int grad = MEPGL_MINB_GRAD, dir = MEPGL_MINB_DIR; };
+template <> struct MinBlocks<ff> { static constexpr int grad = MEPGL_MINB_GRAD_FF, dir = MEPGL_MINB_DIR_FF; };
+
 template <class T> struct TileRows { static constexpr int v = sizeof(T) == 4 ? MEPGL_ROWS_F32 : MEPGL_ROWS_F64; };
+template <> struct TileRows<ff> { static constexpr int v = MEPGL_ROWS_F64; };
 
 int nlcg_step_launches() { return 2 + MEPGL_SPLIT_DIR; }
 
@@ -74,10 +87,10 @@ namespace {
 
 // Base pointers of one image's fields for one tile.
 template <class T, int NC>
-struct ImagePtrs {
-    const vec2_t<T> *in[1 + NC];
-    const vec2_t<T> *aux[1 + NC];
-    vec2_t<T> *out[1 + NC];
+struct ImagePtrs {                  // storage type (double for float-float)
+    const vec2_t<store_t<T>> *in[1 + NC];
+    const vec2_t<store_t<T>> *aux[1 + NC];
+    vec2_t<store_t<T>> *out[1 + NC];
 };
 
 // ------------------------------------------------------------------ staging
@@ -114,10 +127,10 @@ __device__ __forceinline__ void stage(Tile<T, NC, TYT> &t, const StringDesc &S, 
         if (ok[k]) {
             const int s = sidx[k];
 #pragma unroll
-            for (int c = 0; c < 1 + NC; ++c) f[k][c] = ip.in[c][s];
+            for (int c = 0; c < 1 + NC; ++c) f[k][c] = load2<T>(ip.in[c] + s);
             if (aux)
 #pragma unroll
-                for (int c = 0; c < 1 + NC; ++c) a[k][c] = ip.aux[c][s];
+                for (int c = 0; c < 1 + NC; ++c) a[k][c] = load2<T>(ip.aux[c] + s);
             if (masks)
                 m[k] = S.mask ? S.mask[s]
                               : (uint16_t)((S.code_comp[s] & 0xff) | ((S.code_sc[s] & 0xff) << 8));
@@ -143,7 +156,7 @@ __device__ __forceinline__ void stage(Tile<T, NC, TYT> &t, const StringDesc &S, 
         }
         if (write_out && ok[k] && hx >= 1 && hx <= TX && hy >= 1 && hy <= TYT)
 #pragma unroll
-            for (int c = 0; c < 1 + NC; ++c) ip.out[c][sidx[k]] = v[c];
+            for (int c = 0; c < 1 + NC; ++c) store2<T>(ip.out[c] + sidx[k], v[c]);
         t.A[hy][hx] = v[0];
 #pragma unroll
         for (int c = 0; c < NC; ++c) t.P[c][hy][hx] = v[1 + c];
@@ -213,9 +226,10 @@ __device__ __forceinline__ void image_ptrs(ImagePtrs<T, NC> &ip, void *const *in
 {
 #pragma unroll
     for (int c = 0; c < 1 + NC; ++c) {
-        ip.in[c] = in ? static_cast<const vec2_t<T> *>(in[c]) + off : nullptr;
-        ip.aux[c] = aux ? static_cast<const vec2_t<T> *>(aux[c]) + off : nullptr;
-        ip.out[c] = out ? static_cast<vec2_t<T> *>(out[c]) + off : nullptr;
+        using W = vec2_t<store_t<T>>;
+        ip.in[c] = in ? static_cast<const W *>(in[c]) + off : nullptr;
+        ip.aux[c] = aux ? static_cast<const W *>(aux[c]) + off : nullptr;
+        ip.out[c] = out ? static_cast<W *>(out[c]) + off : nullptr;
     }
 }
 
@@ -242,7 +256,7 @@ __device__ __forceinline__ TileRef flat_tile(const StringDesc &S, int tt)
 template <class T>
 __device__ __forceinline__ T h_site(const StringDesc &S, const SiteParams<T> &p, int s)
 {
-    return S.per_site ? static_cast<const T *>(S.ph)[s] : p.h;
+    return S.per_site ? from_store<T>(static_cast<const store_t<T> *>(S.ph)[s]) : p.h;
 }
 
 // --------------------------------------------------------------- line search
@@ -330,7 +344,7 @@ __device__ double line_search_exact(const double *c, double fallback)
 
 // ------------------------------------------------------------------ kernels
 template <class T, int NC>
-__global__ void __launch_bounds__(NT, MEPGL_MINB_GRAD) k_grad(const __grid_constant__ Batch bt, const TileRef *__restrict__ tiles,
+__global__ void __launch_bounds__(NT, MinBlocks<T>::grad) k_grad(const __grid_constant__ Batch bt, const TileRef *__restrict__ tiles,
                                              int n_tiles, Scalars sc, StepFlags f)
 {
     constexpr int TYT = TileRows<T>::v;
@@ -349,7 +363,9 @@ __global__ void __launch_bounds__(NT, MEPGL_MINB_GRAD) k_grad(const __grid_const
         ImagePtrs<T, NC> ip;
         image_ptrs<T, NC>(ip, S.x[f.xin], S.d[f.din], S.x[f.xout], off);
 #if MEPGL_GRAD_ASYNC
-        {
+        if constexpr (std::is_same<T, ff>::value) {
+            stage<T, NC, TYT, 1>(t, S, ip, i0, j0, (T)sc.alpha_pend[img], true, true);
+        } else {
             constexpr int HW = TX + 2, HE = (TYT + 2) * HW, NI = (HE + NT - 1) / NT;
             const T alpha = (T)sc.alpha_pend[img];
             uint16_t codes[NI];
@@ -390,12 +406,13 @@ __global__ void __launch_bounds__(NT, MEPGL_MINB_GRAD) k_grad(const __grid_const
 #else
         stage<T, NC, TYT, 1>(t, S, ip, i0, j0, (T)sc.alpha_pend[img], true, true);
 #endif
-        V *gcur[1 + NC];
-        const V *gprev[1 + NC];
+        using W = vec2_t<store_t<T>>;
+        W *gcur[1 + NC];
+        const W *gprev[1 + NC];
 #pragma unroll
         for (int c = 0; c < 1 + NC; ++c) {
-            gcur[c] = static_cast<V *>(S.g[f.gcur][c]) + off;
-            gprev[c] = static_cast<const V *>(S.g[f.gprev][c]) + off;
+            gcur[c] = static_cast<W *>(S.g[f.gcur][c]) + off;
+            gprev[c] = static_cast<const W *>(S.g[f.gprev][c]) + off;
         }
         SiteParams<T> p;
         p.load_uniform(S);
@@ -410,7 +427,7 @@ __global__ void __launch_bounds__(NT, MEPGL_MINB_GRAD) k_grad(const __grid_const
 #pragma unroll
             for (int c = 0; c < 1 + NC; ++c) {
                 gold[r][c].x = gold[r][c].y = (T)0;
-                if (gi < S.nx && gj < S.ny) gold[r][c] = gprev[c][gi + S.nx * gj];
+                if (gi < S.nx && gj < S.ny) gold[r][c] = load2<T>(gprev[c] + gi + S.nx * gj);
             }
         }
 #pragma unroll
@@ -435,7 +452,7 @@ __global__ void __launch_bounds__(NT, MEPGL_MINB_GRAD) k_grad(const __grid_const
                     V gv;
                     gv.x = g[2 * c];
                     gv.y = g[2 * c + 1];
-                    gcur[c][s] = gv;
+                    store2<T>(gcur[c] + s, gv);
                     const V go = gold[r][c];
                     v[0] += gv.x * gv.x + gv.y * gv.y;
                     v[1] += gv.x * (gv.x - go.x) + gv.y * (gv.y - go.y);
@@ -459,7 +476,7 @@ __global__ void __launch_bounds__(NT, MEPGL_MINB_GRAD) k_grad(const __grid_const
 }
 
 template <class T, int NC>
-__global__ void __launch_bounds__(NT, MEPGL_MINB_DIR) k_dir_poly(const __grid_constant__ Batch bt,
+__global__ void __launch_bounds__(NT, MinBlocks<T>::dir) k_dir_poly(const __grid_constant__ Batch bt,
                                                  const TileRef *__restrict__ tiles, int n_tiles, Scalars sc,
                                                  StepFlags f)
 {
@@ -477,18 +494,30 @@ __global__ void __launch_bounds__(NT, MEPGL_MINB_DIR) k_dir_poly(const __grid_co
         ImagePtrs<T, NC> ipx, ipd;
         image_ptrs<T, NC>(ipx, S.x[f.xout], nullptr, nullptr, off);
         image_ptrs<T, NC>(ipd, S.d[f.din], S.g[f.gcur], S.d[f.dout], off);
-        uint16_t codes[((TYT + 2) * (TX + 2) + NT - 1) / NT];
-        stage_async<T, NC, TYT>(tx, S, ipx.in, i0, j0, codes);
+        if constexpr (std::is_same<T, ff>::value) {
+            // float-float tiles are converted from double: staged through registers
+            stage<T, NC, TYT, 0>(tx, S, ipx, i0, j0, (T)0, false, true);
 #if MEPGL_SPLIT_DIR
-        const vec2_t<T> *dsrc[1 + NC];
-#pragma unroll
-        for (int c = 0; c < 1 + NC; ++c) dsrc[c] = ipd.out[c];
-        stage_async<T, NC, TYT>(td, S, dsrc, i0, j0, nullptr);
+            ImagePtrs<T, NC> ipn;
+            image_ptrs<T, NC>(ipn, S.d[f.dout], nullptr, nullptr, off);
+            stage<T, NC, TYT, 0>(td, S, ipn, i0, j0, (T)0, false, false);
 #else
-        stage<T, NC, TYT, 2>(td, S, ipd, i0, j0, (T)sc.beta[img], true, false);
+            stage<T, NC, TYT, 2>(td, S, ipd, i0, j0, (T)sc.beta[img], true, false);
 #endif
-        store_codes<T, NC, TYT>(tx, codes);
-        cp_async_wait_all();
+        } else {
+            uint16_t codes[((TYT + 2) * (TX + 2) + NT - 1) / NT];
+            stage_async<T, NC, TYT>(tx, S, ipx.in, i0, j0, codes);
+#if MEPGL_SPLIT_DIR
+            const vec2_t<T> *dsrc[1 + NC];
+#pragma unroll
+            for (int c = 0; c < 1 + NC; ++c) dsrc[c] = ipd.out[c];
+            stage_async<T, NC, TYT>(td, S, dsrc, i0, j0, nullptr);
+#else
+            stage<T, NC, TYT, 2>(td, S, ipd, i0, j0, (T)sc.beta[img], true, false);
+#endif
+            store_codes<T, NC, TYT>(tx, codes);
+            cp_async_wait_all();
+        }
         SiteParams<T> p;
         p.load_uniform(S);
         __syncthreads();
@@ -519,8 +548,9 @@ __global__ void __launch_bounds__(NT, MEPGL_MINB_DIR) k_dir_poly(const __grid_co
             }
             __syncthreads();
             if (threadIdx.x < 32) {
-                const double *xt = sizeof(T) == 8 ? sc.xtab_d : sc.xtab_f;
-                double alpha = line_search_scan<T>(coef, xt);
+                // the scan's grid and rounding follow the stored precision
+                const double *xt = sizeof(store_t<T>) == 8 ? sc.xtab_d : sc.xtab_f;
+                double alpha = line_search_scan<store_t<T>>(coef, xt);
                 if (f.ls_exact) alpha = line_search_exact(coef, alpha);
                 if (threadIdx.x == 0) {
                     sc.alpha[img] = alpha;
@@ -556,8 +586,9 @@ __global__ void __launch_bounds__(NT) k_dir_update(const __grid_constant__ Batch
 #pragma unroll
                 for (int c = 0; c < 1 + NC; ++c) {
                     const int s = gi + S.nx * gj;
-                    gv[r][c] = (static_cast<const V *>(S.g[f.gcur][c]) + off)[s];
-                    dv[r][c] = (static_cast<const V *>(S.d[f.din][c]) + off)[s];
+                    using W = vec2_t<store_t<T>>;
+                    gv[r][c] = load2<T>(static_cast<const W *>(S.g[f.gcur][c]) + off + s);
+                    dv[r][c] = load2<T>(static_cast<const W *>(S.d[f.din][c]) + off + s);
                 }
         }
 #pragma unroll
@@ -569,7 +600,7 @@ __global__ void __launch_bounds__(NT) k_dir_update(const __grid_constant__ Batch
                     V v;
                     v.x = -gv[r][c].x + beta * dv[r][c].x;
                     v.y = -gv[r][c].y + beta * dv[r][c].y;
-                    (static_cast<V *>(S.d[f.dout][c]) + off)[gi + S.nx * gj] = v;
+                    store2<T>(static_cast<vec2_t<store_t<T>> *>(S.d[f.dout][c]) + off + gi + S.nx * gj, v);
                 }
         }
     }
@@ -1002,9 +1033,20 @@ inline int grid_for(long n, int cap = 152 * 16)
         }                                                                                           \
     } while (0)
 
+// The NLCG passes also exist in float-float arithmetic (paired FP64 mode).
+#define DISPATCH_NLCG(L, KERNEL, ...)                                                               \
+    do {                                                                                            \
+        if ((L).paired && (L).precision == 1) {                                                     \
+            if ((L).ncomp == 2) KERNEL<ff, 2><<<(L).grid, NT, 0, (L).stream>>>(__VA_ARGS__);        \
+            else KERNEL<ff, 1><<<(L).grid, NT, 0, (L).stream>>>(__VA_ARGS__);                       \
+        } else {                                                                                    \
+            DISPATCH(L, KERNEL, __VA_ARGS__);                                                       \
+        }                                                                                           \
+    } while (0)
+
 cudaError_t launch_grad(const Launch &L, const Scalars &sc, const StepFlags &f)
 {
-    DISPATCH(L, k_grad, *L.batch, L.tiles, L.n_tiles, sc, f);
+    DISPATCH_NLCG(L, k_grad, *L.batch, L.tiles, L.n_tiles, sc, f);
     return cudaGetLastError();
 }
 
@@ -1014,12 +1056,12 @@ cudaError_t launch_dir_poly(const Launch &L, const Scalars &sc, const StepFlags 
     {
         Launch U = L;
         U.grid = L.n_tiles < 152 * 16 ? L.n_tiles : 152 * 16;
-        DISPATCH(U, k_dir_update, *U.batch, U.tiles, U.n_tiles, sc, f);
+        DISPATCH_NLCG(U, k_dir_update, *U.batch, U.tiles, U.n_tiles, sc, f);
         cudaError_t e = cudaGetLastError();
         if (e != cudaSuccess) return e;
     }
 #endif
-    DISPATCH(L, k_dir_poly, *L.batch, L.tiles, L.n_tiles, sc, f);
+    DISPATCH_NLCG(L, k_dir_poly, *L.batch, L.tiles, L.n_tiles, sc, f);
     return cudaGetLastError();
 }
 

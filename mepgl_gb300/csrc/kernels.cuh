@@ -20,6 +20,7 @@ struct Launch {
     int n_tiles;
     int grid;                    // blocks launched (grid-stride over tiles)
     int precision;               // 0 float, 1 double
+    int paired;                  // 1: NLCG passes in float-float arithmetic on double fields
     int ncomp;                   // 1 or 2 (uniform over the strings of a context)
     cudaStream_t stream;
 };

@@ -40,6 +40,9 @@ __constant__ MaskTable<double> c_mask_d;
 template <class T> __device__ __forceinline__ const MaskTable<T> &mask_table();
 template <> __device__ __forceinline__ const MaskTable<float> &mask_table<float>() { return c_mask_f; }
 template <> __device__ __forceinline__ const MaskTable<double> &mask_table<double>() { return c_mask_d; }
+// the weights are multiples of 1/4, exact in float: float-float reads the float table
+template <class T> struct MaskOf { using type = T; };
+template <> struct MaskOf<ff> { using type = float; };
 
 template <class T>
 struct Wts {
@@ -47,7 +50,7 @@ struct Wts {
     T vUR, vUL, vLL, vLR;
     __device__ __forceinline__ void load(unsigned mk)
     {
-        const MaskTable<T> &M = mask_table<T>();
+        const auto &M = mask_table<typename MaskOf<T>::type>();
         const unsigned s = mk >> 8, c = mk & 0xffu;
         area = M.sc[s][0]; wfx = M.sc[s][1]; wbx = M.sc[s][2]; wfy = M.sc[s][3]; wby = M.sc[s][4];
         lfx = M.sc[s][5]; lbx = M.sc[s][6]; lfy = M.sc[s][7]; lby = M.sc[s][8];
@@ -109,14 +112,16 @@ struct SiteParams {
     // per-site overrides (strings whose parameter arrays are not uniform)
     __device__ __forceinline__ void load_site(const StringDesc &S, int s, int nc)
     {
+        using St = store_t<T>;
         for (int c = 0; c < nc; ++c) {
-            a[c] = static_cast<const T *>(S.pa[c])[s];
-            b[c] = static_cast<const T *>(S.pb[c])[s];
-            hmx[c] = (T)0.5 / static_cast<const T *>(S.pmxx[c])[s];
-            hmy[c] = (T)0.5 / static_cast<const T *>(S.pmyy[c])[s];
-            aob[c] = a[c] / b[c];
+            const St av = static_cast<const St *>(S.pa[c])[s], bv = static_cast<const St *>(S.pb[c])[s];
+            a[c] = from_store<T>(av);
+            b[c] = from_store<T>(bv);
+            hmx[c] = from_store<T>((St)0.5 / static_cast<const St *>(S.pmxx[c])[s]);
+            hmy[c] = from_store<T>((St)0.5 / static_cast<const St *>(S.pmyy[c])[s]);
+            aob[c] = from_store<T>(av / bv);
         }
-        h = static_cast<const T *>(S.ph)[s];
+        h = from_store<T>(static_cast<const St *>(S.ph)[s]);
     }
 };
 

@@ -20,14 +20,18 @@ def main(argv=None):
     ap.add_argument("--n", type=int, default=256)
     ap.add_argument("--images", type=int, default=64)
     ap.add_argument("--steps", type=int, default=4)
+    ap.add_argument("--fp64-arith", choices=("native", "paired"), default="native",
+                    help="FP64 NLCG passes in double or in float-float pairs")
     a = ap.parse_args(argv)
     from . import native, workloads
     prob, st = workloads.config2(n=a.n, images=a.images)
-    ctx = native.StringContext(prob, st.n_images, a.precision, use_graphs=0, line_polynomial=native.POLY_EXACT)
+    ctx = native.StringContext(prob, st.n_images, a.precision, use_graphs=0, line_polynomial=native.POLY_EXACT,
+                               fp64_arith=native.FP64_PAIRED if a.fp64_arith == "paired" else native.FP64_NATIVE)
     ctx.set_state(st)
     ms_grad, ms_dir = ctx.profile_passes(a.steps)
     fe = ctx.image_scalars()["fenergy"]
-    print(json.dumps({"precision": a.precision, "n": a.n, "images": a.images, "steps": a.steps,
+    print(json.dumps({"precision": a.precision, "fp64_arith": a.fp64_arith, "n": a.n, "images": a.images,
+                      "steps": a.steps,
                       "ms_grad": ms_grad, "ms_dir_poly": ms_dir, "energy0": float(fe[0])}))
 
 
