@@ -250,21 +250,26 @@ def run_ours(args):
                 "peak_source": f"{peak_kind} hbm_gbs",
                 "step_gbs": (bytes_grad + bytes_dir) / (ms_grad + ms_dir) / 1e6}
 
-    # ---- FP64 polish throughput (same string) ---------------------------------
-    ctx64 = native.StringContext(prob, F, "fp64", stream=stream.cuda_stream, line_polynomial=native.POLY_EXACT)
-    ctx64.set_state(st)
-    ctx64.nlcg_steps(3)
-    k64 = max(2, args.steps // 4)
-    barrier()
-    ev0.record(stream)
-    ctx64.nlcg_steps(k64)
-    ev1.record(stream)
-    barrier()
-    ms64 = maxed(ev0.elapsed_time(ev1))
-    g64, d64 = ctx64.profile_passes(3)
-    fp64 = {"value": world * units_per_step * k64 / (ms64 / 1e3), "ms_per_step": ms64 / k64, "steps": k64,
-            "ms_grad": g64, "ms_dir_poly": d64}
-    ctx64.close()
+    # ---- FP64 polish throughput (same string): IEEE double and float-float ----
+    def fp64_leg(arith):
+        c64 = native.StringContext(prob, F, "fp64", stream=stream.cuda_stream, line_polynomial=native.POLY_EXACT,
+                                   fp64_arith=arith)
+        c64.set_state(st)
+        c64.nlcg_steps(3)
+        k64 = max(2, args.steps // 4)
+        barrier()
+        ev0.record(stream)
+        c64.nlcg_steps(k64)
+        ev1.record(stream)
+        barrier()
+        ms64 = maxed(ev0.elapsed_time(ev1))
+        g64, d64 = c64.profile_passes(3)
+        c64.close()
+        return {"value": replicas_value(world, units_per_step, k64, ms64), "ms_per_step": ms64 / k64, "steps": k64,
+                "ms_grad": g64, "ms_dir_poly": d64}
+
+    fp64 = fp64_leg(native.FP64_NATIVE)
+    fp64["paired"] = fp64_leg(native.FP64_PAIRED)
 
     # ---- end to end through the C ABI with pinned host buffers -----------------
     shape = (F, prob.ny, prob.nx, 2)

@@ -44,14 +44,15 @@ def time_within(t, v, target, rtol):
 
 
 def run(cfg: int, relax: int, iterations: int, schedule: str = "fp64", fp32_iterations: int = 0,
-        mode: str = "L", switch_window: int = 10, switch_tol: float = 1e-5):
+        mode: str = "L", switch_window: int = 10, switch_tol: float = 1e-5, fp64_arith: str = "native"):
     """fp32_iterations < 0 (mixed): switch to FP64 once F_{F-1} - F_0 has
     changed by at most switch_tol (relative) over switch_window iterations,
     i.e. when FP32 has reached its resolution."""
     prob, st = _workload(cfg)
     prec = "fp32" if schedule in ("fp32", "mixed") else "fp64"
     c = native.StringContext(prob, st.n_images, prec, line_polynomial=native.POLY_EXACT,
-                             line_search=native.LS_EXACT, spline=native.SPLINE_FMM)
+                             line_search=native.LS_EXACT, spline=native.SPLINE_FMM,
+                             fp64_arith=native.FP64_PAIRED if fp64_arith == "paired" else native.FP64_NATIVE)
     c.set_state(st)
     c.synchronize()
     rec = []
@@ -120,6 +121,8 @@ def main(argv=None):
                     help="mixed: outer iterations in FP32 (< 0: until F_end - F_0 plateaus)")
     ap.add_argument("--switch-window", type=int, default=10)
     ap.add_argument("--switch-tol", type=float, default=1e-5)
+    ap.add_argument("--fp64-arith", choices=("native", "paired"), default="native",
+                    help="FP64 NLCG passes in double or in float-float pairs")
     ap.add_argument("--mode", choices=("L", "C"), default="L")
     ap.add_argument("--target-ends", type=float, default=None)
     ap.add_argument("--rtol", type=float, default=1e-6)
@@ -130,11 +133,12 @@ def main(argv=None):
             print(json.dumps(row))
         return
     rec, sens = run(a.config, a.relax, a.iterations, a.schedule, a.fp32_iterations, a.mode, a.switch_window,
-                    a.switch_tol)
+                    a.switch_tol, a.fp64_arith)
     s = summarise(rec, a.target_ends, a.rtol)
     s.update(sens)
     fp32_its = sum(1 for r in rec if r[4] == "fp32")
-    s.update(config=a.config, relax=a.relax, schedule=a.schedule, fp32_iterations=fp32_its, mode=a.mode)
+    s.update(config=a.config, relax=a.relax, schedule=a.schedule, fp32_iterations=fp32_its, mode=a.mode,
+             fp64_arith=a.fp64_arith)
     print(json.dumps(s))
     if a.out:
         with open(a.out, "w") as f:

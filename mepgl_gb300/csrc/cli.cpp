@@ -54,7 +54,8 @@ void usage()
                 "  --iterations arg  Number of iterations\n"
                 "  --precision arg   fp32 | fp64 | mixed (FP32, then FP64 for the last iterations)\n"
                 "  --relaxation-steps n, --polish-iterations n\n"
-                "  --line-polynomial compat|exact, --line-search compat|exact, --spline compat|fmm\n");
+                "  --line-polynomial compat|exact, --line-search compat|exact, --spline compat|fmm\n"
+                "  --fp64-arith native|paired (FP64 NLCG passes in float-float pairs)\n");
 }
 
 Args parse(int argc, char **argv)
@@ -255,6 +256,7 @@ int run(const Args &A)
     O.line_polynomial = opt("line_polynomial", "compat") == "exact" ? MEPGL_POLY_EXACT : MEPGL_POLY_COMPAT;
     O.line_search = opt("line_search", "compat") == "exact" ? MEPGL_LS_EXACT : MEPGL_LS_COMPAT;
     O.spline = opt("spline", "compat") == "fmm" ? MEPGL_SPLINE_FMM : MEPGL_SPLINE_COMPAT;
+    O.fp64_arith = opt("fp64_arith", "native") == "paired" ? MEPGL_FP64_PAIRED : MEPGL_FP64_NATIVE;
 
     std::printf("%s\n\nSimulation name: %s\n", mepgl_version(), A.simname.c_str());
     std::printf("Lattice %zu x %zu, dx = %g, %d images, %d component(s), precision %s\n", nx, ny, dx, F, nc,

@@ -24,6 +24,7 @@ def main(argv=None):
     ap.add_argument("--images", type=int, default=128)
     ap.add_argument("--steps", type=int, default=6)
     ap.add_argument("--fp64-steps", type=int, default=2)
+    ap.add_argument("--no-paired", action="store_true", help="skip the paired (float-float) FP64 leg")
     a = ap.parse_args(argv)
     import torch
     from . import native, workloads
@@ -32,11 +33,16 @@ def main(argv=None):
     units = a.n * a.n * a.images
     out = dict(workload="two-component GL %dx%d dx=0.25, %d images, disk domain" % (a.n, a.n, a.images),
                site_images=units)
-    for prec, steps, tdt in (("fp32", a.steps, torch.float32), ("fp64", a.fp64_steps, torch.float64)):
+    legs = [("fp32", "fp32", a.steps, torch.float32, native.FP64_NATIVE),
+            ("fp64", "fp64", a.fp64_steps, torch.float64, native.FP64_NATIVE)]
+    if not a.no_paired:
+        legs.append(("fp64_paired", "fp64", a.fp64_steps, torch.float64, native.FP64_PAIRED))
+    for key, prec, steps, tdt, arith in legs:
         if steps <= 0:
             continue
         prob, (fa, f1, f2) = workloads.config5_device(a.n, a.images, dtype=tdt)
-        ctx = native.StringContext(prob, a.images, prec, stream=stream.cuda_stream, line_polynomial=native.POLY_EXACT)
+        ctx = native.StringContext(prob, a.images, prec, stream=stream.cuda_stream, line_polynomial=native.POLY_EXACT,
+                                   fp64_arith=arith)
         torch.cuda.synchronize()
         ctx.set_state_device(fa.data_ptr(), f1.data_ptr(), f2.data_ptr())
         ctx.synchronize()
@@ -53,7 +59,7 @@ def main(argv=None):
         mg, md = ctx.profile_passes(2)
         S = 6 * (4 if prec == "fp32" else 8)
         bg, bd = (5 * S + 2) * units, (4 * S + 2) * units
-        out[prec] = dict(ms_per_step=ms, value=units / (ms / 1e3), unit="site·image/s",
+        out[key] = dict(ms_per_step=ms, value=units / (ms / 1e3), unit="site·image/s",
                          k_grad=dict(ms=mg, gbs=bg / mg / 1e6), k_dir_poly=dict(ms=md, gbs=bd / md / 1e6),
                          step_gbs=(bg + bd) / ms / 1e6, device_gb=torch.cuda.mem_get_info()[1] / 1e9 -
                          torch.cuda.mem_get_info()[0] / 1e9)
