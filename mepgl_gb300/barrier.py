@@ -14,7 +14,7 @@ over the final tenth of the run and, when ``--target-ends`` is given, the
 time after which F_{F-1} - F_0 stays within ``--rtol`` of it.
 
     python -m mepgl_gb300.barrier --config 2 --relax 100 --iterations 250 \
-        --schedule fp64 --out gpurun_out/barrier_c2_fp64.json
+        --schedule fp64 --out barrier_c2_fp64.json
 """
 from __future__ import annotations
 
