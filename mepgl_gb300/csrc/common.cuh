@@ -9,12 +9,13 @@
 // image) sums that image's partials in a fixed order.
 //
 // Precision.  Fields are float or double (T).  Sums are formed in T inside
-// a warp (a fixed pairwise shuffle tree), then in double across warps,
-// tiles and images.  GB300's FP64 pipe is a small fraction of its FP32
+// a block (fixed pairwise shuffle trees), then in double across tiles and
+// images.  GB300's FP64 pipe is a small fraction of its FP32
 // rate, so FP32 kernels avoid any per-site double arithmetic or conversion.
 #pragma once
 
 #include <cstdint>
+#include <type_traits>
 #include <cuda_runtime.h>
 
 #include "pair_float.cuh"
@@ -123,7 +124,8 @@ struct Scalars {
 __device__ __forceinline__ unsigned bit(unsigned c, int n) { return (c >> n) & 1u; }
 
 // Block-wide sum of NV values; a pairwise tree in T inside each warp, then
-// double across warps.  Result (double) valid in thread 0.
+// across the warps in float (FP32 fields) or double (the others).  Result
+// (double) valid in thread 0.
 template <int NV, class T>
 __device__ __forceinline__ void block_sum(const T (&v)[NV], double (&out)[NV], double *smem /* NT/32*NV */)
 {
@@ -135,17 +137,36 @@ __device__ __forceinline__ void block_sum(const T (&v)[NV], double (&out)[NV], d
         for (int o = 16; o > 0; o >>= 1) w[k] += shfl_down(w[k], o);
     }
     const int wi = threadIdx.x >> 5, l = threadIdx.x & 31;
-    if (l == 0)
+    if constexpr (std::is_same<T, float>::value) {
+        // FP32 fields: the eight warp sums are added in float too (the FP64
+        // pipe is scarce; one conversion per quantity and block)
+        float *fs = reinterpret_cast<float *>(smem);
+        if (l == 0)
 #pragma unroll
-        for (int k = 0; k < NV; ++k) smem[wi * NV + k] = (double)w[k];
-    __syncthreads();
-    if (threadIdx.x < 32) {
+            for (int k = 0; k < NV; ++k) fs[wi * NV + k] = w[k];
+        __syncthreads();
+        if (threadIdx.x < 32) {
 #pragma unroll
-        for (int k = 0; k < NV; ++k) {
-            double t = (l < NT / 32) ? smem[l * NV + k] : 0.0;
+            for (int k = 0; k < NV; ++k) {
+                float t = (l < NT / 32) ? fs[l * NV + k] : 0.0f;
 #pragma unroll
-            for (int o = 16; o > 0; o >>= 1) t += __shfl_down_sync(0xffffffffu, t, o);
-            out[k] = t;
+                for (int o = NT / 64; o > 0; o >>= 1) t += __shfl_down_sync(0xffffffffu, t, o);
+                out[k] = (double)t;
+            }
+        }
+    } else {
+        if (l == 0)
+#pragma unroll
+            for (int k = 0; k < NV; ++k) smem[wi * NV + k] = (double)w[k];
+        __syncthreads();
+        if (threadIdx.x < 32) {
+#pragma unroll
+            for (int k = 0; k < NV; ++k) {
+                double t = (l < NT / 32) ? smem[l * NV + k] : 0.0;
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) t += __shfl_down_sync(0xffffffffu, t, o);
+                out[k] = t;
+            }
         }
     }
     __syncthreads();
