@@ -31,19 +31,21 @@ TUNING = os.path.join(PKG, "tuning.json")
 
 # (rows per FP32 tile, min blocks per SM for the gradient pass, for the
 # direction pass, gradient-pass halo copy: 0 through registers, 1 cp.async,
-# direction pass: 0 fused, 1 split into a pointwise update + polynomial pass)
-CANDIDATES = [(16, 4, 4, 0, 0), (16, 4, 4, 0, 1), (16, 4, 3, 0, 1), (16, 4, 5, 0, 1), (16, 5, 4, 0, 1),
-              (16, 4, 4, 1, 1), (32, 4, 3, 0, 1), (16, 4, 3, 0, 0)]
+# direction pass: 0 fused, 1 split into a pointwise update + polynomial pass,
+# fused direction pass halo copy: 0 x by cp.async and g, d through
+# registers, 1 all three by cp.async)
+CANDIDATES = [(16, 4, 4, 0, 0, 0), (16, 4, 4, 0, 0, 1), (16, 4, 3, 0, 0, 1), (16, 5, 4, 0, 0, 1),
+              (16, 4, 5, 0, 0, 1), (16, 4, 4, 1, 0, 1), (16, 4, 3, 0, 0, 0), (16, 4, 4, 0, 1, 0)]
 
 
 def defines(c):
-    rows, g, d, a, sp = c
+    rows, g, d, a, sp, da = c
     return {"MEPGL_ROWS_F32": rows, "MEPGL_MINB_GRAD": g, "MEPGL_MINB_DIR": d, "MEPGL_GRAD_ASYNC": a,
-            "MEPGL_SPLIT_DIR": sp}
+            "MEPGL_SPLIT_DIR": sp, "MEPGL_DIR_ASYNC": da}
 
 
 def _build(c, base):
-    d = os.path.join(base, "r%d_g%d_d%d_a%d_s%d" % c)
+    d = os.path.join(base, "r%d_g%d_d%d_a%d_s%d_da%d" % c)
     env = dict(os.environ, MEPGL_LIB_DIR=d,
                MEPGL_NVCC_FLAGS=" ".join("-D%s=%d" % kv for kv in defines(c).items()), MEPGL_NO_TUNING="1")
     r = subprocess.run([sys.executable, "-c", "from mepgl_gb300 import build; build.build(force=True)"], cwd=ROOT,

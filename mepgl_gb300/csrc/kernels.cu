@@ -49,6 +49,12 @@ namespace mepgl {
 #ifndef MEPGL_SPLIT_DIR
 #define MEPGL_SPLIT_DIR 0
 #endif
+// 1: the direction pass of FP32 strings copies the raw x, g and d halo tiles
+// with cp.async and forms -g + beta d in shared memory; 0: x by cp.async,
+// g and d through registers
+#ifndef MEPGL_DIR_ASYNC
+#define MEPGL_DIR_ASYNC 0
+#endif
 // 1: the gradient pass copies the raw x and d halo tiles with cp.async and
 // forms x + alpha d in shared memory; 0: through registers (stage mode 1)
 #ifndef MEPGL_GRAD_ASYNC
@@ -483,6 +489,9 @@ __global__ void __launch_bounds__(NT, MinBlocks<T>::dir) k_dir_poly(const __grid
     constexpr int TYT = TileRows<T>::v;
     __shared__ Tile<T, NC, TYT> tx;
     __shared__ Tile<T, NC, TYT> td;
+    // raw gradient tile of the all-asynchronous FP32 variant (16 bytes otherwise)
+    constexpr bool DIR_ASYNC = MEPGL_DIR_ASYNC && !MEPGL_SPLIT_DIR && std::is_same<T, float>::value;
+    __shared__ __align__(16) unsigned char g_raw[DIR_ASYNC ? sizeof(TileF<T, NC, TYT>) : 16];
     __shared__ double red[NT / 32 * 5];
     __shared__ double coef[5];
     for (int tt = blockIdx.x; tt < n_tiles; tt += gridDim.x) {
@@ -507,6 +516,42 @@ __global__ void __launch_bounds__(NT, MinBlocks<T>::dir) k_dir_poly(const __grid
         } else {
             uint16_t codes[((TYT + 2) * (TX + 2) + NT - 1) / NT];
             stage_async<T, NC, TYT>(tx, S, ipx.in, i0, j0, codes);
+            if constexpr (DIR_ASYNC) {
+                TileF<T, NC, TYT> &tg = *reinterpret_cast<TileF<T, NC, TYT> *>(g_raw);
+                stage_async<T, NC, TYT>(tg, S, ipd.aux, i0, j0, nullptr);
+                stage_async<T, NC, TYT>(td, S, ipd.in, i0, j0, nullptr);
+                store_codes<T, NC, TYT>(tx, codes);
+                cp_async_wait_all();
+                __syncthreads();
+                // d <- -g + beta d over the halo tile; interior d -> d[dout]
+                using V = vec2_t<T>;
+                constexpr int HW = TX + 2, HE = (TYT + 2) * HW, NI = (HE + NT - 1) / NT;
+                const T beta = (T)sc.beta[img];
+#pragma unroll
+                for (int k = 0; k < NI; ++k) {
+                    const int e = threadIdx.x + k * NT;
+                    if (e >= HE) continue;
+                    const int hy = e / HW, hx = e - hy * HW;
+                    V v[1 + NC];
+                    {
+                        const V gv = tg.A[hy][hx], dv = td.A[hy][hx];
+                        v[0].x = -gv.x + beta * dv.x;
+                        v[0].y = -gv.y + beta * dv.y;
+                        td.A[hy][hx] = v[0];
+                    }
+#pragma unroll
+                    for (int c = 0; c < NC; ++c) {
+                        const V gv = tg.P[c][hy][hx], dv = td.P[c][hy][hx];
+                        v[1 + c].x = -gv.x + beta * dv.x;
+                        v[1 + c].y = -gv.y + beta * dv.y;
+                        td.P[c][hy][hx] = v[1 + c];
+                    }
+                    const int gi = i0 + hx - 1, gj = j0 + hy - 1;
+                    if (hx >= 1 && hx <= TX && hy >= 1 && hy <= TYT && gi < S.nx && gj < S.ny)
+#pragma unroll
+                        for (int c = 0; c < 1 + NC; ++c) ipd.out[c][gi + S.nx * gj] = v[c];
+                }
+            } else {
 #if MEPGL_SPLIT_DIR
             const vec2_t<T> *dsrc[1 + NC];
 #pragma unroll
@@ -517,6 +562,7 @@ __global__ void __launch_bounds__(NT, MinBlocks<T>::dir) k_dir_poly(const __grid
 #endif
             store_codes<T, NC, TYT>(tx, codes);
             cp_async_wait_all();
+            }
         }
         SiteParams<T> p;
         p.load_uniform(S);
