@@ -313,7 +313,7 @@ def run_ours(args):
     if rank == 0 and not args.no_ttb:
         from mepgl_gb300 import barrier as B
         r64, _ = B.run(1, 50, 150, "fp64")
-        rmx, _ = B.run(1, 50, 150, "mixed")
+        rmx, _ = B.run(1, 50, 150, "mixed", -1)
         target = r64[-1][3]
 
         def t_to(rec):
