@@ -43,7 +43,7 @@ def time_within(t, v, target, rtol):
     return None if k >= len(t) else float(t[k])
 
 
-def run(cfg: int, relax: int, iterations: int, schedule: str = "fp64", fp32_iterations: int = 0,
+def run(cfg: int, relax: int, iterations: int, schedule: str = "fp64", fp32_iterations: int = -1,
         mode: str = "L", switch_window: int = 10, switch_tol: float = 1e-5, fp64_arith: str = "native"):
     """fp32_iterations < 0 (mixed): switch to FP64 once F_{F-1} - F_0 has
     changed by at most switch_tol (relative) over switch_window iterations,
