@@ -149,6 +149,19 @@ mepgl_status mepgl_reset_cg(mepgl_ctx *ctx, int first_image, int last_image);
  * reference's loop() reads, and the step length alpha. */
 mepgl_status mepgl_image_scalars(mepgl_ctx *ctx, double *fenergy, double *g_norm2, double *alpha);
 
+/* Observables of the current state, per image (host arrays of F doubles,
+ * NULL skips), computed on the device: the magnetic flux dx^2 * sum B
+ * (mepgl/post.py:131-133) and, for each component, the winding sum of
+ * compute_winding (mepgl/mepgl_lib/gl_utils.py:10-41): the linearised phase
+ * steps (u dv - v du) / (u^2 + v^2) around a rectangle, about 2 pi per
+ * enclosed vortex.  inset = 0 walks the lattice edge as the reference does
+ * (NaN where |psi| = 0 there, e.g. outside the superconductor); inset > 0
+ * walks the rectangle that many sites inside.  winding_2 is ignored for
+ * one component. */
+mepgl_status mepgl_observables(mepgl_ctx *ctx, int inset, double *flux, double *winding_1, double *winding_2);
+mepgl_status mepgl_batch_observables(mepgl_ctx *ctx, int string, int inset, double *flux, double *winding_1,
+                                     double *winding_2);
+
 /* Parameter adjoints (no reference counterpart): per image (host arrays of
  * F doubles, NULL skips) the partial derivatives of the free energy at the
  * current, fixed fields with respect to a uniform shift of the applied field

@@ -964,6 +964,44 @@ mepgl_status mepgl_compute_jb(mepgl_ctx *c, void *b, void *j_1, void *j_2, int m
     return MEPGL_OK;
 }
 
+mepgl_status mepgl_observables(mepgl_ctx *c, int inset, double *flux, double *winding_1, double *winding_2)
+{
+    return mepgl_batch_observables(c, 0, inset, flux, winding_1, winding_2);
+}
+
+mepgl_status mepgl_batch_observables(mepgl_ctx *c, int string, int inset, double *flux, double *winding_1,
+                                     double *winding_2)
+{
+    if (!c || string < 0 || string >= (int)c->strings.size())
+        return fail(c, MEPGL_ERR_INVALID_ARG, "mepgl_observables: bad string index");
+    StringHost &s = c->strings[string];
+    if (inset < 0 || s.nx - 2 * inset < 2 || s.ny - 2 * inset < 2)
+        return fail(c, MEPGL_ERR_INVALID_ARG, "mepgl_observables: the winding loop needs nx, ny > 2 inset + 1");
+    mepgl_status st = flush(c);
+    if (st != MEPGL_OK) return st;
+    const int F = s.F;
+    double *out = c->dscratch;      // flux, winding 1, winding 2: 3F doubles
+    if (flux) {
+        void *bb[1] = {s.d[c->di ^ 1][0]};
+        void *jj[1][2] = {{s.d[c->di ^ 1][1], c->ncomp == 2 ? s.d[c->di ^ 1][2] : s.d[c->di ^ 1][1]}};
+        CK(c, launch_jb(string_launch(c, string), c->sc, c->xi, bb, jj));
+        CK(c, launch_flux(c->precision, bb[0], s.M(), F, s.dx * s.dx, out, c->stream));
+        c->launches += 2;
+    }
+    for (int k = 0; k < c->ncomp; ++k) {
+        if (!(k == 0 ? winding_1 : winding_2)) continue;
+        CK(c, launch_winding(c->precision, s.x[c->xi][1 + k], s.nx, s.ny, F, inset, out + (size_t)(1 + k) * F,
+                             c->stream));
+        c->launches += 1;
+    }
+    if (flux) CK(c, cudaMemcpyAsync(flux, out, F * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    if (winding_1) CK(c, cudaMemcpyAsync(winding_1, out + F, F * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    if (winding_2 && c->ncomp == 2)
+        CK(c, cudaMemcpyAsync(winding_2, out + 2 * (size_t)F, F * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    CK(c, cudaStreamSynchronize(c->stream));
+    return MEPGL_OK;
+}
+
 mepgl_status mepgl_arc_length(mepgl_ctx *c, int metric, double *s)
 {
     return mepgl_batch_arc_length(c, 0, metric, s);

@@ -908,6 +908,62 @@ __global__ void __launch_bounds__(NT) k_arc_partial(const T *f0, const T *f1, co
     }
 }
 
+// Magnetic flux of every image: Phi_n = dx^2 sum_sites B (post.py:131-133);
+// one block per image, double sums in a fixed order.
+template <class T>
+__global__ void k_flux(const T *__restrict__ b, long M, int F, double dx2, double *out)
+{
+    __shared__ double red[NT / 32];
+    for (int n = blockIdx.x; n < F; n += gridDim.x) {
+        const T *bn = b + (size_t)n * M;
+        double v[1] = {0.0};
+        for (long s = threadIdx.x; s < M; s += NT) v[0] += (double)bn[s];
+        double tot[1];
+        block_sum<1>(v, tot, red);
+        if (threadIdx.x == 0) out[n] = tot[0] * dx2;
+    }
+}
+
+// Winding sum of one field per image (compute_winding, gl_utils.py:10-41):
+// around the rectangle `inset` sites inside the lattice edge, counter-
+// clockwise from the lower-left corner, sum of the linearised phase steps
+// (u dv - v du) / (u^2 + v^2) taken at the start of each step (2 pi per
+// vortex enclosed, approximately).  The loop visits (W - 1) steps along
+// each horizontal side and (H - 1) along each vertical side.
+template <class T>
+__global__ void k_winding(const vec2_t<T> *__restrict__ psi, int nx, int ny, int F, int inset, double *out)
+{
+    __shared__ double red[NT / 32];
+    const int W = nx - 2 * inset, H = ny - 2 * inset, i0 = inset, j0 = inset, i1 = nx - 1 - inset,
+              j1 = ny - 1 - inset;
+    const int L = 2 * (W - 1) + 2 * (H - 1);
+    for (int n = blockIdx.x; n < F; n += gridDim.x) {
+        const vec2_t<T> *pn = psi + (size_t)n * nx * ny;
+        double v[1] = {0.0};
+        for (int t = threadIdx.x; t < L; t += NT) {
+            int ia, ja, ib, jb;
+            if (t < W - 1) {
+                ia = i0 + t; ja = j0; ib = ia + 1; jb = ja;
+            } else if (t < (W - 1) + (H - 1)) {
+                const int k = t - (W - 1);
+                ia = i1; ja = j0 + k; ib = ia; jb = ja + 1;
+            } else if (t < 2 * (W - 1) + (H - 1)) {
+                const int k = t - (W - 1) - (H - 1);
+                ia = i1 - k; ja = j1; ib = ia - 1; jb = ja;
+            } else {
+                const int k = t - 2 * (W - 1) - (H - 1);
+                ia = i0; ja = j1 - k; ib = ia; jb = ja - 1;
+            }
+            const vec2_t<T> a = pn[ia + (size_t)nx * ja], b = pn[ib + (size_t)nx * jb];
+            const double u = a.x, w = a.y, du = (double)b.x - u, dv = (double)b.y - w;
+            v[0] += (u * dv - w * du) / (u * u + w * w);
+        }
+        double tot[1];
+        block_sum<1>(v, tot, red);
+        if (threadIdx.x == 0) out[n] = tot[0];
+    }
+}
+
 // computeArcLength (interpolation.cu:126-140): cumulative sqrt, s[F-1] = 1.
 __global__ void k_arc_finish(const double *part, int nblocks, int F, double *s)
 {
@@ -1186,6 +1242,23 @@ cudaError_t launch_arc_length(int precision, const void *const *fields, const in
         k_arc_partial<float><<<nb, NT, 0, st>>>((const float *)f[0], (const float *)f[1], (const float *)f[2], w[0],
                                                 w[1], w[2], sites, F, part);
     k_arc_finish<<<1, NT, 0, st>>>(part, nb, F, s);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_flux(int precision, const void *b, long M, int F, double dx2, double *out, cudaStream_t st)
+{
+    const int grid = F < 152 * 4 ? F : 152 * 4;
+    if (precision == 1) k_flux<double><<<grid, NT, 0, st>>>((const double *)b, M, F, dx2, out);
+    else k_flux<float><<<grid, NT, 0, st>>>((const float *)b, M, F, dx2, out);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_winding(int precision, const void *psi, int nx, int ny, int F, int inset, double *out,
+                           cudaStream_t st)
+{
+    const int grid = F < 152 * 4 ? F : 152 * 4;
+    if (precision == 1) k_winding<double><<<grid, NT, 0, st>>>((const double2 *)psi, nx, ny, F, inset, out);
+    else k_winding<float><<<grid, NT, 0, st>>>((const float2 *)psi, nx, ny, F, inset, out);
     return cudaGetLastError();
 }
 

@@ -56,6 +56,12 @@ cudaError_t launch_jb(const Launch &L, const Scalars &sc, int xbuf, void *const 
 // part (>= tiles_per_image * F doubles) as scratch.
 cudaError_t launch_arc_length(int precision, const void *const *fields, const int *width, int nf, long sites, int F,
                               double *part, double *s, cudaStream_t st);
+// out[n] = dx2 * sum of b over image n (M reals per image, context precision).
+cudaError_t launch_flux(int precision, const void *b, long M, int F, double dx2, double *out, cudaStream_t st);
+// out[n] = winding sum of psi (pairs) of image n around the rectangle `inset`
+// sites inside the lattice edge (requires nx, ny > 2 inset + 1).
+cudaError_t launch_winding(int precision, const void *psi, int nx, int ny, int F, int inset, double *out,
+                           cudaStream_t st);
 // Plan of a redistribution from F to F_new images on the arc length s:
 // segment k and weight w per output image; for cubic also h and the
 // factorised spline matrix (dl, d, du, du2, ipiv) -- all in `plan`.

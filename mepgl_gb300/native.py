@@ -92,6 +92,8 @@ _SIGS = {
     "mepgl_batch_image_scalars": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]),
     "mepgl_batch_arc_length": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_void_p]),
     "mepgl_param_adjoint": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "mepgl_observables": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "mepgl_batch_observables": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]),
     "mepgl_batch_param_adjoint": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]),
 }
 
@@ -256,6 +258,14 @@ class StringContext:
         h, e, g = np.zeros(self.F), np.zeros(self.F), np.zeros(self.F)
         self._check(self.L.mepgl_param_adjoint(self.h, _ptr(h), _ptr(e), _ptr(g)))
         return np.stack([h, e, g], axis=1)
+
+    def observables(self, inset: int = 0):
+        """Per-image flux dx^2 sum B and winding sums of psi_1 (and psi_2) around
+        the rectangle `inset` sites inside the lattice edge."""
+        phi, w1 = np.zeros(self.F), np.zeros(self.F)
+        w2 = np.zeros(self.F) if self.ncomp == 2 else None
+        self._check(self.L.mepgl_observables(self.h, int(inset), _ptr(phi), _ptr(w1), _ptr(w2)))
+        return dict(phi=phi, w_1=w1, w_2=w2)
 
     def compute_jb(self):
         b = np.empty(self._shape()[:3], self.dtype)
