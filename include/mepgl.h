@@ -123,6 +123,42 @@ const char *mepgl_last_error(const mepgl_ctx *ctx);
 mepgl_status mepgl_set_state(mepgl_ctx *ctx, const void *a, const void *psi_1, const void *psi_2, int memory);
 mepgl_status mepgl_get_state(mepgl_ctx *ctx, void *a, void *psi_1, void *psi_2, int memory);
 
+/* Initial string built on the device, for lattices too large to build on the
+ * host.  Replaces StringBuilder.generate_matter_fields /
+ * generate_vector_potential (mepgl/mepgl_lib/builder.py:107-223): for each
+ * image and component |psi| = psi_abs * prod over that component's vortices
+ * with a nonzero winding in the image of f(r), theta = sum winding *
+ * atan2(y - y_v, x - x_v), plus Gaussian noise of deviation `noise` on Re and
+ * Im (Philox4x32-10 keyed by `seed`: reproducible, independent of the launch),
+ * times the superconducting domain; A from the gauge of b_z (0: A = 0,
+ * 1: Landau_x, 2: Landau_y, 3: symmetric) times the computational domain.
+ * Site (i, j) sits at (x0 + i dx, y0 + j dx).  profile 0: f = tanh(-r^2), the
+ * builder's envelope; 1: f = tanh(r / sqrt 2).  The builder's component-2
+ * phase function is not available (phase 0).  Sets the state and resets the
+ * NLCG history like mepgl_set_state. */
+typedef struct mepgl_vortex {
+    int32_t component;         /* 1 or 2                                         */
+    int32_t pad;
+    const double *x, *y;       /* host arrays of F positions                     */
+    const int32_t *winding;    /* host array of F windings (0: absent)           */
+} mepgl_vortex;
+
+typedef struct mepgl_guess {
+    double x0, y0;
+    double psi_abs_1, psi_abs_2;
+    double noise;
+    double b_z;
+    int32_t gauge;
+    int32_t profile;
+    uint64_t seed;
+    const mepgl_vortex *vortices;
+    int32_t n_vortices;
+    int32_t pad;
+} mepgl_guess;
+
+mepgl_status mepgl_generate_string(mepgl_ctx *ctx, const mepgl_guess *guess);
+mepgl_status mepgl_batch_generate_string(mepgl_ctx *ctx, int string, const mepgl_guess *guess);
+
 /* Per-image free energy of the current state (host array of F doubles).
  * Replaces computeFreeEnergy (mepgl/src/nlcg.cu:217-240). */
 mepgl_status mepgl_free_energy(mepgl_ctx *ctx, double *fenergy);

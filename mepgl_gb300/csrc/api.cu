@@ -813,6 +813,64 @@ mepgl_status mepgl_batch_set_state(mepgl_ctx *c, int string, const void *a, cons
     return reset_history(c);
 }
 
+mepgl_status mepgl_generate_string(mepgl_ctx *c, const mepgl_guess *g)
+{
+    return mepgl_batch_generate_string(c, 0, g);
+}
+
+mepgl_status mepgl_batch_generate_string(mepgl_ctx *c, int string, const mepgl_guess *g)
+{
+    if (!c || !g || string < 0 || string >= (int)c->strings.size() || (g->n_vortices > 0 && !g->vortices) ||
+        g->n_vortices < 0 || g->gauge < 0 || g->gauge > 3 || g->profile < 0 || g->profile > 1)
+        return fail(c, MEPGL_ERR_INVALID_ARG, "mepgl_generate_string: bad string index or guess");
+    mepgl_status st = flush(c);
+    if (st != MEPGL_OK) return st;
+    StringHost &s = c->strings[string];
+    const int F = s.F;
+    std::vector<double> tr((size_t)g->n_vortices * F * 4);
+    for (int v = 0; v < g->n_vortices; ++v) {
+        const mepgl_vortex &V = g->vortices[v];
+        if (!V.x || !V.y || !V.winding || V.component < 1 || V.component > c->ncomp)
+            return fail(c, MEPGL_ERR_INVALID_ARG, "mepgl_generate_string: incomplete vortex track");
+        for (int n = 0; n < F; ++n) {
+            double *t = &tr[((size_t)v * F + n) * 4];
+            t[0] = V.x[n];
+            t[1] = V.y[n];
+            t[2] = (double)V.winding[n];
+            t[3] = (double)V.component;
+        }
+    }
+    // domains and tracks travel in one temporary device buffer
+    const size_t M = (size_t)s.M(), bytes = 2 * M * sizeof(int32_t) + tr.size() * sizeof(double) + 64;
+    char *buf = nullptr;
+    CK(c, cudaMalloc(&buf, bytes));
+    int32_t *dcomp = (int32_t *)buf, *dsc = dcomp + M;
+    double *dtr = (double *)(buf + ((2 * M * sizeof(int32_t) + 15) & ~(size_t)15));
+    cudaError_t e = cudaMemcpyAsync(dcomp, s.comp.data(), M * sizeof(int32_t), cudaMemcpyHostToDevice, c->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(dsc, s.sc.data(), M * sizeof(int32_t), cudaMemcpyHostToDevice, c->stream);
+    if (e == cudaSuccess && !tr.empty())
+        e = cudaMemcpyAsync(dtr, tr.data(), tr.size() * sizeof(double), cudaMemcpyHostToDevice, c->stream);
+    GuessParams p;
+    p.x0 = g->x0;
+    p.y0 = g->y0;
+    p.dx = s.dx;
+    p.psi_abs_1 = g->psi_abs_1;
+    p.psi_abs_2 = g->psi_abs_2;
+    p.noise = g->noise;
+    p.b_z = g->b_z;
+    p.gauge = g->gauge;
+    p.profile = g->profile;
+    p.seed = g->seed;
+    if (e == cudaSuccess)
+        e = launch_generate(c->precision, s.x[c->xi][0], s.x[c->xi][1], s.x[c->xi][2], s.nx, s.ny, F, c->ncomp, dcomp,
+                            dsc, dtr, g->n_vortices, p, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    cudaFree(buf);
+    CK(c, e);
+    c->launches += 1;
+    return reset_history(c);
+}
+
 mepgl_status mepgl_get_state(mepgl_ctx *c, void *a, void *psi_1, void *psi_2, int memory)
 {
     return mepgl_batch_get_state(c, 0, a, psi_1, psi_2, memory);

@@ -908,6 +908,92 @@ __global__ void __launch_bounds__(NT) k_arc_partial(const T *f0, const T *f1, co
     }
 }
 
+// ------------------------------------------------------- initial strings
+// Counter-based Gaussian noise: Philox4x32-10 (Salmon, Moraes, Dror and
+// Shaw, "Parallel random numbers: as easy as 1, 2, 3", SC 2011) keyed by the
+// seed and counted by (image, site, component), then Box-Muller.  Each site
+// draws the same numbers whatever the launch shape.
+__device__ __forceinline__ void philox_round(uint32_t (&c)[4], uint32_t (&k)[2])
+{
+    const uint64_t p0 = (uint64_t)0xD2511F53u * c[0], p1 = (uint64_t)0xCD9E8D57u * c[2];
+    const uint32_t h0 = (uint32_t)(p0 >> 32), l0 = (uint32_t)p0, h1 = (uint32_t)(p1 >> 32), l1 = (uint32_t)p1;
+    c[0] = h1 ^ c[1] ^ k[0];
+    c[1] = l1;
+    c[2] = h0 ^ c[3] ^ k[1];
+    c[3] = l0;
+    k[0] += 0x9E3779B9u;
+    k[1] += 0xBB67AE85u;
+}
+
+__device__ __forceinline__ void philox4x32_10(uint32_t (&c)[4], uint64_t seed)
+{
+    uint32_t k[2] = {(uint32_t)seed, (uint32_t)(seed >> 32)};
+#pragma unroll
+    for (int r = 0; r < 10; ++r) philox_round(c, k);
+}
+
+// two standard normals from the counter (n, s, component)
+__device__ __forceinline__ void normal_pair(uint64_t seed, int n, long s, int comp, double &z0, double &z1)
+{
+    uint32_t c[4] = {(uint32_t)s, (uint32_t)((unsigned long long)s >> 32), (uint32_t)n, (uint32_t)comp};
+    philox4x32_10(c, seed);
+    // 53-bit uniforms in (0, 1]
+    const double u1 = ((double)(((uint64_t)c[0] << 21) ^ (c[1] >> 11)) + 1.0) * 0x1.0p-53;
+    const double u2 = (double)(((uint64_t)c[2] << 21) ^ (c[3] >> 11)) * 0x1.0p-53;
+    const double r = sqrt(-2.0 * log(u1));
+    double sn, cs;
+    sincospi(2.0 * u2, &sn, &cs);
+    z0 = r * cs;
+    z1 = r * sn;
+}
+
+// The initial guess of the reference's StringBuilder (builder.py:107-189)
+// for every image at once: per component |psi| = psi_abs * prod_v f(r_v),
+// theta = sum_v w_v atan2(y - y_v, x - x_v) over the vortex tracks with a
+// nonzero winding in that image, plus N(0, noise^2) on Re and Im, times the
+// superconducting domain; A from the gauge of B_z times the computational
+// domain.  f = tanh(-r^2) (the builder's profile) or tanh(r / sqrt 2).
+// tracks: n_tracks x F x {x, y, winding, component} doubles.
+template <class T>
+__global__ void k_generate(vec2_t<T> *a, vec2_t<T> *p1, vec2_t<T> *p2, int nx, int ny, int F, int ncomp,
+                           const int32_t *comp, const int32_t *sc, const double *tracks, int n_tracks, GuessParams g)
+{
+    const long M = (long)nx * ny;
+    for (long e = blockIdx.x * (long)NT + threadIdx.x; e < M * F; e += (long)gridDim.x * NT) {
+        const int n = (int)(e / M);
+        const long s = e - (long)n * M;
+        const int i = (int)(s % nx), j = (int)(s / nx);
+        const double x = g.x0 + i * g.dx, y = g.y0 + j * g.dx;
+        const double cm = comp[s] ? 1.0 : 0.0, scm = sc[s] ? 1.0 : 0.0;
+        vec2_t<T> av;
+        double ax = 0.0, ay = 0.0;
+        if (g.gauge == 1) ax = -g.b_z * y;
+        else if (g.gauge == 2) ay = g.b_z * x;
+        else if (g.gauge == 3) { ax = -0.5 * g.b_z * y; ay = 0.5 * g.b_z * x; }
+        av.x = (T)(ax * cm);
+        av.y = (T)(ay * cm);
+        a[e] = av;
+        for (int c = 0; c < ncomp; ++c) {
+            double mag = c == 0 ? g.psi_abs_1 : g.psi_abs_2, th = 0.0;
+            for (int v = 0; v < n_tracks; ++v) {
+                const double *t = tracks + ((size_t)v * F + n) * 4;
+                if ((int)t[3] != c + 1 || t[2] == 0.0) continue;
+                const double dxv = x - t[0], dyv = y - t[1], r2 = dxv * dxv + dyv * dyv;
+                mag *= g.profile == 0 ? tanh(-r2) : tanh(sqrt(r2) * 0.70710678118654752440);
+                th += t[2] * atan2(dyv, dxv);
+            }
+            double z0 = 0.0, z1 = 0.0;
+            if (g.noise != 0.0) normal_pair(g.seed, n, s, c, z0, z1);
+            double sn, cs;
+            sincos(th, &sn, &cs);
+            vec2_t<T> pv;
+            pv.x = (T)((mag * cs + g.noise * z0) * scm);
+            pv.y = (T)((mag * sn + g.noise * z1) * scm);
+            (c == 0 ? p1 : p2)[e] = pv;
+        }
+    }
+}
+
 // Magnetic flux of every image: Phi_n = dx^2 sum_sites B (post.py:131-133);
 // one block per image, double sums in a fixed order.
 template <class T>
@@ -1242,6 +1328,22 @@ cudaError_t launch_arc_length(int precision, const void *const *fields, const in
         k_arc_partial<float><<<nb, NT, 0, st>>>((const float *)f[0], (const float *)f[1], (const float *)f[2], w[0],
                                                 w[1], w[2], sites, F, part);
     k_arc_finish<<<1, NT, 0, st>>>(part, nb, F, s);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_generate(int precision, void *a, void *p1, void *p2, int nx, int ny, int F, int ncomp,
+                            const int32_t *comp, const int32_t *sc, const double *tracks, int n_tracks,
+                            const GuessParams &g, cudaStream_t st)
+{
+    const long n = (long)nx * ny * F;
+    long b = (n + NT - 1) / NT;
+    const int grid = (int)(b < 1 ? 1 : (b > 152 * 32 ? 152 * 32 : b));
+    if (precision == 1)
+        k_generate<double><<<grid, NT, 0, st>>>((double2 *)a, (double2 *)p1, (double2 *)p2, nx, ny, F, ncomp, comp, sc,
+                                                tracks, n_tracks, g);
+    else
+        k_generate<float><<<grid, NT, 0, st>>>((float2 *)a, (float2 *)p1, (float2 *)p2, nx, ny, F, ncomp, comp, sc,
+                                               tracks, n_tracks, g);
     return cudaGetLastError();
 }
 

@@ -56,6 +56,18 @@ cudaError_t launch_jb(const Launch &L, const Scalars &sc, int xbuf, void *const 
 // part (>= tiles_per_image * F doubles) as scratch.
 cudaError_t launch_arc_length(int precision, const void *const *fields, const int *width, int nf, long sites, int F,
                               double *part, double *s, cudaStream_t st);
+// Initial-guess parameters of launch_generate (see mepgl_guess).
+struct GuessParams {
+    double x0, y0, dx, psi_abs_1, psi_abs_2, noise, b_z;
+    int gauge, profile;
+    unsigned long long seed;
+};
+// Fill a, psi_1[, psi_2] (F images of nx*ny pairs) with the builder's initial
+// guess; comp / sc: int32 domains on the device; tracks: n_tracks*F*4 doubles
+// (x, y, winding, component) on the device.
+cudaError_t launch_generate(int precision, void *a, void *p1, void *p2, int nx, int ny, int F, int ncomp,
+                            const int32_t *comp, const int32_t *sc, const double *tracks, int n_tracks,
+                            const GuessParams &g, cudaStream_t st);
 // out[n] = dx2 * sum of b over image n (M reals per image, context precision).
 cudaError_t launch_flux(int precision, const void *b, long M, int F, double dx2, double *out, cudaStream_t st);
 // out[n] = winding sum of psi (pairs) of image n around the rectangle `inset`

@@ -55,6 +55,19 @@ class MepglOptions(C.Structure):
                 ("discretization", C.c_int32), ("fp64_arith", C.c_int32)]
 
 
+class MepglVortex(C.Structure):
+    _fields_ = [("component", C.c_int32), ("pad", C.c_int32), ("x", C.c_void_p), ("y", C.c_void_p),
+                ("winding", C.c_void_p)]
+
+
+class MepglGuess(C.Structure):
+    _fields_ = [("x0", C.c_double), ("y0", C.c_double), ("psi_abs_1", C.c_double), ("psi_abs_2", C.c_double),
+                ("noise", C.c_double), ("b_z", C.c_double), ("gauge", C.c_int32), ("profile", C.c_int32),
+                ("seed", C.c_uint64), ("vortices", C.c_void_p), ("n_vortices", C.c_int32), ("pad", C.c_int32)]
+
+
+GAUGES = {None: 0, "none": 0, "Landau_x": 1, "Landau_y": 2, "symmetric": 3}
+
 _lib = None
 _lock = threading.Lock()
 
@@ -93,6 +106,8 @@ _SIGS = {
     "mepgl_batch_arc_length": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_void_p]),
     "mepgl_param_adjoint": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     "mepgl_observables": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "mepgl_generate_string": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "mepgl_batch_generate_string": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p]),
     "mepgl_batch_observables": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]),
     "mepgl_batch_param_adjoint": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]),
 }
@@ -258,6 +273,32 @@ class StringContext:
         h, e, g = np.zeros(self.F), np.zeros(self.F), np.zeros(self.F)
         self._check(self.L.mepgl_param_adjoint(self.h, _ptr(h), _ptr(e), _ptr(g)))
         return np.stack([h, e, g], axis=1)
+
+    def generate_string(self, vortices=(), x0=0.0, y0=0.0, psi_abs_1=1.0, psi_abs_2=1.0, noise=0.0, b_z=0.0,
+                        gauge=None, profile="builder", seed=0):
+        """Build the initial string on the device (mepgl_generate_string).
+
+        vortices: (component, x[F], y[F], winding[F]) tracks in physical
+        coordinates; site (i, j) is at (x0 + i dx, y0 + j dx).  profile
+        "builder" is the reference builder's tanh(-r^2) envelope, "tanh"
+        is tanh(r / sqrt 2); gauge None / "Landau_x" / "Landau_y" /
+        "symmetric" sets A from b_z."""
+        keep = []
+        vs = (MepglVortex * max(1, len(vortices)))()
+        for k, (comp, xv, yv, wv) in enumerate(vortices):
+            xa = np.ascontiguousarray(np.broadcast_to(xv, (self.F,)), np.float64)
+            ya = np.ascontiguousarray(np.broadcast_to(yv, (self.F,)), np.float64)
+            wa = np.ascontiguousarray(np.broadcast_to(wv, (self.F,)), np.int32)
+            keep += [xa, ya, wa]
+            vs[k].component, vs[k].x, vs[k].y, vs[k].winding = int(comp), xa.ctypes.data, ya.ctypes.data, wa.ctypes.data
+        g = MepglGuess()
+        g.x0, g.y0, g.psi_abs_1, g.psi_abs_2, g.noise, g.b_z = x0, y0, psi_abs_1, psi_abs_2, noise, b_z
+        g.gauge = GAUGES[gauge]
+        g.profile = {"builder": 0, "tanh": 1}[profile]
+        g.seed = int(seed)
+        g.vortices = C.cast(vs, C.c_void_p)
+        g.n_vortices = len(vortices)
+        self._check(self.L.mepgl_generate_string(self.h, C.byref(g)))
 
     def observables(self, inset: int = 0):
         """Per-image flux dx^2 sum B and winding sums of psi_1 (and psi_2) around
