@@ -24,7 +24,8 @@ def native():
 
 
 def _setup(mc=True, F=5, Nx=40, Ny=33):
-    sb = StringBuilder(F, Nx, Ny, (-10.0, 10.0), (-8.0, 8.0), mc, B_z=0.6)
+    dx = 20.0 / (Nx - 1)                     # one lattice spacing on both axes
+    sb = StringBuilder(F, Nx, Ny, (-10.0, 10.0), (-8.0, -8.0 + dx * (Ny - 1)), mc, B_z=0.6)
     sb.set_sc_domain(lambda x, y: x * x / 81 + y * y / 49 <= 1.0)
     xv = np.linspace(-9.0, 2.0, F)
     wv = np.array([0] + [1] * (F - 1))
@@ -33,7 +34,6 @@ def _setup(mc=True, F=5, Nx=40, Ny=33):
         sb.add_vortex(xv + 0.5, -0.2 + 0 * xv, wv, 2)
         sb.add_vortex(3.0 + 0 * xv, 2.0 + 0 * xv, -wv, 2)
     comp, sc = sb.get_domain_matrices()
-    dx = 20.0 / (Nx - 1)
     prob = Problem.uniform(Nx, Ny, dx, multicomponent=mc, comp_domain=comp.T.copy(), sc_domain=sc.T.copy())
     tracks = [(c, np.asarray(x), np.asarray(y), np.asarray(w)) for c, vs in ((1, sb.vortices_1), (2, sb.vortices_2))
               for x, y, w in vs]
