@@ -1,9 +1,11 @@
 """Autotuner for the tile shape and residency of the two NLCG passes.
 
 The stencil tile is 32 sites wide with a one-site halo; its height (rows per
-tile, hence the halo-to-interior ratio and the shared memory per block) and
-the minimum resident blocks per SM requested from ptxas (hence the register
-budget) are compile-time template parameters.  The tuner builds one library
+tile, hence the halo-to-interior ratio) and the minimum resident blocks per
+SM requested from ptxas (hence the register budget) are compile-time
+template parameters, and the FP32 passes exist in two designs: warp strips
+(one warp per tile walking down its rows, neighbours by shuffles) and
+shared-memory tiles (eight warps per tile, with variants of the halo copy).  The tuner builds one library
 per candidate (in parallel, into a scratch directory), times the FP32 NLCG
 step of a workload with each (CUDA events on the context's stream, after
 warm-up), and writes the fastest candidate's definitions to
@@ -29,23 +31,29 @@ PKG = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(PKG)
 TUNING = os.path.join(PKG, "tuning.json")
 
-# (rows per FP32 tile, min blocks per SM for the gradient pass, for the
-# direction pass, gradient-pass halo copy: 0 through registers, 1 cp.async,
-# direction pass: 0 fused, 1 split into a pointwise update + polynomial pass,
-# fused direction pass halo copy: 0 x by cp.async and g, d through
-# registers, 1 all three by cp.async)
-CANDIDATES = [(16, 4, 4, 0, 0, 0), (16, 4, 4, 0, 0, 1), (16, 4, 3, 0, 0, 1), (16, 5, 4, 0, 0, 1),
-              (16, 4, 5, 0, 0, 1), (16, 4, 4, 1, 0, 1), (16, 4, 3, 0, 0, 0), (16, 4, 4, 0, 1, 0)]
+# Strip candidates: rows per tile, single-warp blocks per SM (register
+# budget 65536 / (32 x blocks)), row loop unrolled by the window period,
+# unit-weight path for interior sites.
+STRIP = [(16, 16, 0, 0), (32, 16, 0, 0), (32, 16, 1, 0), (32, 16, 0, 1), (32, 16, 1, 1), (16, 16, 0, 1),
+         (32, 12, 0, 1)]
+# Tile candidates: rows per FP32 tile, min blocks per SM for the gradient
+# pass, for the direction pass, gradient-pass halo copy (0 through
+# registers, 1 cp.async), direction pass (0 fused, 1 split into a pointwise
+# update + polynomial pass), fused direction pass halo copy (0 x by cp.async
+# and g, d through registers, 1 all three by cp.async).
+TILE = [(16, 4, 4, 0, 0, 0)]
+CANDIDATES = [dict(MEPGL_STRIP=1, MEPGL_ROWS_F32=r, MEPGL_MINB_STRIP=m, MEPGL_STRIP_UNROLL=u, MEPGL_STRIP_INTERIOR=i)
+              for r, m, u, i in STRIP] + [
+    dict(MEPGL_STRIP=0, MEPGL_ROWS_F32=r, MEPGL_MINB_GRAD=g, MEPGL_MINB_DIR=d, MEPGL_GRAD_ASYNC=a,
+         MEPGL_SPLIT_DIR=sp, MEPGL_DIR_ASYNC=da) for r, g, d, a, sp, da in TILE]
 
 
 def defines(c):
-    rows, g, d, a, sp, da = c
-    return {"MEPGL_ROWS_F32": rows, "MEPGL_MINB_GRAD": g, "MEPGL_MINB_DIR": d, "MEPGL_GRAD_ASYNC": a,
-            "MEPGL_SPLIT_DIR": sp, "MEPGL_DIR_ASYNC": da}
+    return dict(c)
 
 
 def _build(c, base):
-    d = os.path.join(base, "r%d_g%d_d%d_a%d_s%d_da%d" % c)
+    d = os.path.join(base, "_".join("%s%d" % (k.replace("MEPGL_", "").lower(), v) for k, v in sorted(c.items())))
     env = dict(os.environ, MEPGL_LIB_DIR=d,
                MEPGL_NVCC_FLAGS=" ".join("-D%s=%d" % kv for kv in defines(c).items()), MEPGL_NO_TUNING="1")
     r = subprocess.run([sys.executable, "-c", "from mepgl_gb300 import build; build.build(force=True)"], cwd=ROOT,

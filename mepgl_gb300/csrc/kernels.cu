@@ -62,6 +62,23 @@ namespace mepgl {
 #endif
 
 // the float-float passes hold twice the registers of FP32 ones
+// FP32 NLCG passes as warp strips (strip.cuh) instead of shared-memory tiles
+#ifndef MEPGL_STRIP
+#define MEPGL_STRIP 1
+#endif
+#ifndef MEPGL_MINB_STRIP
+#define MEPGL_MINB_STRIP 16   // single-warp blocks per SM: 128 registers
+#endif
+// strip row loop unrolled by the window period; interior sites with unit weights
+#ifndef MEPGL_STRIP_UNROLL
+#define MEPGL_STRIP_UNROLL 0
+#endif
+#ifndef MEPGL_STRIP_INTERIOR
+#define MEPGL_STRIP_INTERIOR 0
+#endif
+#if MEPGL_STRIP && MEPGL_SPLIT_DIR
+#error "MEPGL_SPLIT_DIR applies to the tile kernels; build it with MEPGL_STRIP=0"
+#endif
 #ifndef MEPGL_MINB_GRAD_FF
 #define MEPGL_MINB_GRAD_FF 4
 #endif
@@ -607,6 +624,8 @@ __global__ void __launch_bounds__(NT, MinBlocks<T>::dir) k_dir_poly(const __grid
         __syncthreads();
     }
 }
+
+#include "strip.cuh"
 
 // d[dout] = -g + beta d[din] at every site of the launch's tiles (the
 // pointwise half of computeStepDirection, nlcg.cu:955-994, when the
@@ -1232,9 +1251,33 @@ inline int grid_for(long n, int cap = 152 * 16)
         }                                                                                           \
     } while (0)
 
+// FP64 and float-float NLCG passes (tile kernels).
+#define DISPATCH_WIDE(L, KERNEL, ...)                                                               \
+    do {                                                                                            \
+        if ((L).paired) {                                                                           \
+            if ((L).ncomp == 2) KERNEL<ff, 2><<<(L).grid, NT, 0, (L).stream>>>(__VA_ARGS__);        \
+            else KERNEL<ff, 1><<<(L).grid, NT, 0, (L).stream>>>(__VA_ARGS__);                       \
+        } else {                                                                                    \
+            if ((L).ncomp == 2) KERNEL<double, 2><<<(L).grid, NT, 0, (L).stream>>>(__VA_ARGS__);    \
+            else KERNEL<double, 1><<<(L).grid, NT, 0, (L).stream>>>(__VA_ARGS__);                   \
+        }                                                                                           \
+    } while (0)
+
+// FP32 NLCG passes: one single-warp block per tile.
+#define DISPATCH_STRIP(L, KERNEL, ...)                                                              \
+    do {                                                                                            \
+        if ((L).ncomp == 2) KERNEL<float, 2><<<(L).n_tiles, NTS, 0, (L).stream>>>(__VA_ARGS__);     \
+        else KERNEL<float, 1><<<(L).n_tiles, NTS, 0, (L).stream>>>(__VA_ARGS__);                    \
+    } while (0)
+
 cudaError_t launch_grad(const Launch &L, const Scalars &sc, const StepFlags &f)
 {
+#if MEPGL_STRIP
+    if (L.precision == 0) DISPATCH_STRIP(L, k_grad_s, *L.batch, L.tiles, sc, f);
+    else DISPATCH_WIDE(L, k_grad, *L.batch, L.tiles, L.n_tiles, sc, f);
+#else
     DISPATCH_NLCG(L, k_grad, *L.batch, L.tiles, L.n_tiles, sc, f);
+#endif
     return cudaGetLastError();
 }
 
@@ -1249,7 +1292,12 @@ cudaError_t launch_dir_poly(const Launch &L, const Scalars &sc, const StepFlags 
         if (e != cudaSuccess) return e;
     }
 #endif
+#if MEPGL_STRIP
+    if (L.precision == 0) DISPATCH_STRIP(L, k_dir_poly_s, *L.batch, L.tiles, sc, f);
+    else DISPATCH_WIDE(L, k_dir_poly, *L.batch, L.tiles, L.n_tiles, sc, f);
+#else
     DISPATCH_NLCG(L, k_dir_poly, *L.batch, L.tiles, L.n_tiles, sc, f);
+#endif
     return cudaGetLastError();
 }
 

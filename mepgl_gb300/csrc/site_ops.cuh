@@ -56,6 +56,13 @@ struct Wts {
         lfx = M.sc[s][5]; lbx = M.sc[s][6]; lfy = M.sc[s][7]; lby = M.sc[s][8];
         vUR = M.cc[c][0]; vUL = M.cc[c][1]; vLL = M.cc[c][2]; vLR = M.cc[c][3];
     }
+    // weights of a site whose eight neighbours are all inside both domains
+    // (codes 0xff | 0xff << 8): every weight is 1
+    __device__ __forceinline__ void interior()
+    {
+        area = wfx = wbx = wfy = wby = lfx = lbx = lfy = lby = (T)1;
+        vUR = vUL = vLL = vLR = (T)1;
+    }
 };
 
 // Host-side construction of the tables (same arithmetic as nlcg.cu:522-525,
@@ -93,6 +100,17 @@ struct TileF {
 template <class T, int NC, int TYT>
 struct Tile : TileF<T, NC, TYT> {
     uint16_t m[TYT + 2][TX + 2];
+};
+
+// Neighbourhood of one site read from a shared-memory tile: A(dx, dy) and
+// P(c, dx, dy) for |dx|, |dy| <= 1.  The stencil functions below that take a
+// view also run on register windows (the strip kernels).
+template <class T, int NC, int TYT>
+struct TileView {
+    const TileF<T, NC, TYT> &t;
+    int lx, ly;
+    __device__ __forceinline__ vec2_t<T> A(int dx, int dy) const { return t.A[ly + dy][lx + dx]; }
+    __device__ __forceinline__ vec2_t<T> P(int c, int dx, int dy) const { return t.P[c][ly + dy][lx + dx]; }
 };
 
 // Parameters of one site (uniform strings read the descriptor).
@@ -340,45 +358,46 @@ __device__ __forceinline__ T site_dh_link(const Tile<T, NC, TYT> &t, int lx, int
 // restating gradientPsi (nlcg.cu:504-744) and gradientA (nlcg.cu:746-888).
 // Both link ends use the mass of this site, as the reference does.  hr, hl,
 // hu, hd: applied field at the right, left, upper and lower neighbours.
-template <class T, int NC, int TYT>
-__device__ __forceinline__ void site_gradient(const Tile<T, NC, TYT> &t, int lx, int ly, const SiteParams<T> &p,
-                                              const Wts<T> &w, T hr, T hl, T hu, T hd, int maxwell, int thin_film,
-                                              T *out)
+#define VA(dx_, dy_) (v.A((dx_), (dy_)))
+#define VP(c_, dx_, dy_) (v.P((c_), (dx_), (dy_)))
+template <class T, int NC, class View>
+__device__ __forceinline__ void site_gradient_v(const View &v, const SiteParams<T> &p, const Wts<T> &w, T hr, T hl,
+                                                T hu, T hd, int maxwell, int thin_film, T *out)
 {
-    const vec2_t<T> A0 = TA(0, 0);
-    const vec2_t<T> Ar = TA(1, 0), Al = TA(-1, 0), Au = TA(0, 1), Ad = TA(0, -1);
+    const vec2_t<T> A0 = VA(0, 0);
+    const vec2_t<T> Ar = VA(1, 0), Al = VA(-1, 0), Au = VA(0, 1), Ad = VA(0, -1);
     T gax = 0, gay = 0;
     const T idx = p.idx;
 #pragma unroll
     for (int c = 0; c < NC; ++c) {
-        const vec2_t<T> P0 = TP(c, 0, 0);
+        const vec2_t<T> P0 = VP(c, 0, 0);
         const T x = P0.x, y = P0.y, r2 = x * x + y * y, q = p.q[c];
         T gx = (2 * p.a[c] * x + p.b[c] * 2 * x * r2) * w.area;
         T gy = (2 * p.a[c] * y + p.b[c] * 2 * y * r2) * w.area;
         T u[4];
         {
-            link4(A0.x, Ar.x, P0, TP(c, 1, 0), q, idx, u);
+            link4(A0.x, Ar.x, P0, VP(c, 1, 0), q, idx, u);
             const T f = p.hmx[c] * w.wfx, qa = q * A0.x;
             gx += f * ((u[0] + u[1]) * idx - qa * u[2]);
             gy += f * (-(u[2] + u[3]) * idx - qa * u[0]);
             gax -= f * q * (y * u[0] + x * u[2]);
         }
         {
-            link4(Al.x, A0.x, TP(c, -1, 0), P0, q, idx, u);
+            link4(Al.x, A0.x, VP(c, -1, 0), P0, q, idx, u);
             const T f = p.hmx[c] * w.wbx, qa = q * A0.x;
             gx += f * (-(u[1] + u[0]) * idx - qa * u[3]);
             gy += f * ((u[3] + u[2]) * idx - qa * u[1]);
             gax -= f * q * (y * u[1] + x * u[3]);
         }
         {
-            link4(A0.y, Au.y, P0, TP(c, 0, 1), q, idx, u);
+            link4(A0.y, Au.y, P0, VP(c, 0, 1), q, idx, u);
             const T f = p.hmy[c] * w.wfy, qa = q * A0.y;
             gx += f * ((u[0] + u[1]) * idx - qa * u[2]);
             gy += f * (-(u[2] + u[3]) * idx - qa * u[0]);
             gay -= f * q * (y * u[0] + x * u[2]);
         }
         {
-            link4(Ad.y, A0.y, TP(c, 0, -1), P0, q, idx, u);
+            link4(Ad.y, A0.y, VP(c, 0, -1), P0, q, idx, u);
             const T f = p.hmy[c] * w.wby, qa = q * A0.y;
             gx += f * (-(u[1] + u[0]) * idx - qa * u[3]);
             gy += f * ((u[3] + u[2]) * idx - qa * u[1]);
@@ -388,7 +407,7 @@ __device__ __forceinline__ void site_gradient(const Tile<T, NC, TYT> &t, int lx,
         out[3 + 2 * c] = gy;
     }
     if (NC == 2) {
-        const vec2_t<T> P1 = TP(0, 0, 0), P2 = TP(NC - 1, 0, 0);
+        const vec2_t<T> P1 = VP(0, 0, 0), P2 = VP(NC - 1, 0, 0);
         const T x1 = P1.x, y1 = P1.y, x2 = P2.x, y2 = P2.y;
         const T r1 = x1 * x1 + y1 * y1, r2 = x2 * x2 + y2 * y2;
         const T R = x1 * x2 + y1 * y2, I = x1 * y2 - y1 * x2;
@@ -404,10 +423,10 @@ __device__ __forceinline__ void site_gradient(const Tile<T, NC, TYT> &t, int lx,
         // link differences ex(i,j) = d_x A_y on the x-link i -> i+1, ey(i,j) = d_y A_x
         const T ex0 = (Ar.y - A0.y) * idx, exm = (A0.y - Al.y) * idx;
         const T ey0 = (Au.x - A0.x) * idx, eym = (A0.x - Ad.x) * idx;
-        const T exu = (TA(1, 1).y - Au.y) * idx, exmu = (Au.y - TA(-1, 1).y) * idx;
-        const T exd = (TA(1, -1).y - Ad.y) * idx, exmd = (Ad.y - TA(-1, -1).y) * idx;
-        const T eyr = (TA(1, 1).x - Ar.x) * idx, eyrm = (Ar.x - TA(1, -1).x) * idx;
-        const T eyl = (TA(-1, 1).x - Al.x) * idx, eylm = (Al.x - TA(-1, -1).x) * idx;
+        const T exu = (VA(1, 1).y - Au.y) * idx, exmu = (Au.y - VA(-1, 1).y) * idx;
+        const T exd = (VA(1, -1).y - Ad.y) * idx, exmd = (Ad.y - VA(-1, -1).y) * idx;
+        const T eyr = (VA(1, 1).x - Ar.x) * idx, eyrm = (Ar.x - VA(1, -1).x) * idx;
+        const T eyl = (VA(-1, 1).x - Al.x) * idx, eylm = (Al.x - VA(-1, -1).x) * idx;
         const T h = p.h;
         // residuals of the collocated views of this site and of the
         // neighbours' views of the same plaquettes (nlcg.cu:852-883)
@@ -425,17 +444,25 @@ __device__ __forceinline__ void site_gradient(const Tile<T, NC, TYT> &t, int lx,
     }
 }
 
+template <class T, int NC, int TYT>
+__device__ __forceinline__ void site_gradient(const Tile<T, NC, TYT> &t, int lx, int ly, const SiteParams<T> &p,
+                                              const Wts<T> &w, T hr, T hl, T hu, T hd, int maxwell, int thin_film,
+                                              T *out)
+{
+    site_gradient_v<T, NC>(TileView<T, NC, TYT>{t, lx, ly}, p, w, hr, hl, hu, hd, maxwell, thin_film, out);
+}
+
 // Quartic coefficients of F(x + a d) at one site (polynomialExpansion,
 // nlcg.cu:997-1370): out = {A, B, C, D, E}.  compat keeps the reference's
 // x-link first-order slip and y-link halved cubic coefficient.
-template <class T, int NC, int TYT>
-__device__ __forceinline__ void site_poly(const Tile<T, NC, TYT> &t, const TileF<T, NC, TYT> &dt, int lx, int ly,
-                                          const SiteParams<T> &p, const Wts<T> &w, int compat, int thin_film, T *out)
+template <class T, int NC, class View, class DView>
+__device__ __forceinline__ void site_poly_v(const View &v, const DView &dv, const SiteParams<T> &p, const Wts<T> &w,
+                                            int compat, int thin_film, T *out)
 {
     T e = 0, b1 = 0, c2 = 0, d3 = 0, e4 = 0;
 #pragma unroll
     for (int c = 0; c < NC; ++c) {
-        const vec2_t<T> P0 = TP(c, 0, 0), D0 = dt.P[c][ly][lx];
+        const vec2_t<T> P0 = VP(c, 0, 0), D0 = dv.P(c, 0, 0);
         const T n0 = p.aob[c] + P0.x * P0.x + P0.y * P0.y;
         const T n1 = 2 * (P0.x * D0.x + P0.y * D0.y);
         const T n2 = D0.x * D0.x + D0.y * D0.y;
@@ -447,8 +474,8 @@ __device__ __forceinline__ void site_poly(const Tile<T, NC, TYT> &t, const TileF
         e4 += bb * ((T)0.5 * n2 * n2);
     }
     if (NC == 2) {
-        const vec2_t<T> P1 = TP(0, 0, 0), P2 = TP(NC - 1, 0, 0);
-        const vec2_t<T> D1 = dt.P[0][ly][lx], D2 = dt.P[NC - 1][ly][lx];
+        const vec2_t<T> P1 = VP(0, 0, 0), P2 = VP(NC - 1, 0, 0);
+        const vec2_t<T> D1 = dv.P(0, 0, 0), D2 = dv.P(NC - 1, 0, 0);
         const T x1 = P1.x, y1 = P1.y, x2 = P2.x, y2 = P2.y;
         const T u1 = D1.x, v1 = D1.y, u2 = D2.x, v2 = D2.y;
         const T R0 = x1 * x2 + y1 * y2, R1 = u1 * x2 + v1 * y2 + x1 * u2 + y1 * v2, R2 = u1 * u2 + v1 * v2;
@@ -465,12 +492,12 @@ __device__ __forceinline__ void site_poly(const Tile<T, NC, TYT> &t, const TileF
     }
     e *= w.area; b1 *= w.area; c2 *= w.area; d3 *= w.area; e4 *= w.area;
     if (!thin_film) {
-        const vec2_t<T> A0 = TA(0, 0), a0 = dt.A[ly][lx];
+        const vec2_t<T> A0 = VA(0, 0), a0 = dv.A(0, 0);
         const T idx = p.idx;
-        const T ayp = (TA(1, 0).y - A0.y) * idx, aym = (A0.y - TA(-1, 0).y) * idx;
-        const T axp = (TA(0, 1).x - A0.x) * idx, axm = (A0.x - TA(0, -1).x) * idx;
-        const T dyp = (dt.A[ly][lx + 1].y - a0.y) * idx, dym = (a0.y - dt.A[ly][lx - 1].y) * idx;
-        const T dxp = (dt.A[ly + 1][lx].x - a0.x) * idx, dxm = (a0.x - dt.A[ly - 1][lx].x) * idx;
+        const T ayp = (VA(1, 0).y - A0.y) * idx, aym = (A0.y - VA(-1, 0).y) * idx;
+        const T axp = (VA(0, 1).x - A0.x) * idx, axm = (A0.x - VA(0, -1).x) * idx;
+        const T dyp = (dv.A(1, 0).y - a0.y) * idx, dym = (a0.y - dv.A(-1, 0).y) * idx;
+        const T dxp = (dv.A(0, 1).x - a0.x) * idx, dxm = (a0.x - dv.A(0, -1).x) * idx;
         T em0 = 0, em1 = 0, em2 = 0, m0, m1;
 #define EMV(wv, yy, xx, dyy, dxx)        \
         m0 = yy - xx - p.h;              \
@@ -490,17 +517,17 @@ __device__ __forceinline__ void site_poly(const Tile<T, NC, TYT> &t, const TileF
 #pragma unroll
     for (int dir = 0; dir < 2; ++dir) {
         const int ox = dir == 0 ? 1 : 0, oy = dir == 0 ? 0 : 1;
-        const T Ai = dir == 0 ? TA(0, 0).x : TA(0, 0).y;
-        const T Aj = dir == 0 ? TA(ox, oy).x : TA(ox, oy).y;
-        const T ai = dir == 0 ? dt.A[ly][lx].x : dt.A[ly][lx].y;
-        const T aj = dir == 0 ? dt.A[ly + oy][lx + ox].x : dt.A[ly + oy][lx + ox].y;
+        const T Ai = dir == 0 ? VA(0, 0).x : VA(0, 0).y;
+        const T Aj = dir == 0 ? VA(ox, oy).x : VA(ox, oy).y;
+        const T ai = dir == 0 ? dv.A(0, 0).x : dv.A(0, 0).y;
+        const T aj = dir == 0 ? dv.A(ox, oy).x : dv.A(ox, oy).y;
         const T wl = dir == 0 ? w.wfx : w.wfy;
 #pragma unroll
         for (int c = 0; c < NC; ++c) {
             const T q = p.q[c];
             const T qd = (compat && dir == 0) ? (T)-1 : q;
-            const vec2_t<T> pi = TP(c, 0, 0), pj = TP(c, ox, oy);
-            const vec2_t<T> di = dt.P[c][ly][lx], dj = dt.P[c][ly + oy][lx + ox];
+            const vec2_t<T> pi = VP(c, 0, 0), pj = VP(c, ox, oy);
+            const vec2_t<T> di = dv.P(c, 0, 0), dj = dv.P(c, ox, oy);
             T t0[4];
             link4(Ai, Aj, pi, pj, q, p.idx, t0);
             const T ddre = (dj.x - di.x) * p.idx, ddim = (dj.y - di.y) * p.idx;
@@ -538,6 +565,15 @@ __device__ __forceinline__ void site_poly(const Tile<T, NC, TYT> &t, const TileF
     out[3] = d3 * p.dx2;
     out[4] = e4 * p.dx2;
 }
+
+template <class T, int NC, int TYT>
+__device__ __forceinline__ void site_poly(const Tile<T, NC, TYT> &t, const TileF<T, NC, TYT> &dt, int lx, int ly,
+                                          const SiteParams<T> &p, const Wts<T> &w, int compat, int thin_film, T *out)
+{
+    site_poly_v<T, NC>(TileView<T, NC, TYT>{t, lx, ly}, TileView<T, NC, TYT>{dt, lx, ly}, p, w, compat, thin_film, out);
+}
+#undef VA
+#undef VP
 
 // B and J at one site (computeJBKernel, nlcg.cu:243-364).
 template <class T, int NC, int TYT>
