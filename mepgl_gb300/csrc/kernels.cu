@@ -25,6 +25,7 @@
 
 #include "kernels.cuh"
 #include "site_ops.cuh"
+#include "site_pair.cuh"
 
 namespace mepgl {
 
@@ -75,6 +76,10 @@ namespace mepgl {
 #endif
 #ifndef MEPGL_STRIP_INTERIOR
 #define MEPGL_STRIP_INTERIOR 0
+#endif
+// two-component FP32 strips in packed FP32x2 arithmetic (site_pair.cuh)
+#ifndef MEPGL_STRIP_PAIR
+#define MEPGL_STRIP_PAIR 1
 #endif
 #if MEPGL_STRIP && MEPGL_SPLIT_DIR
 #error "MEPGL_SPLIT_DIR applies to the tile kernels; build it with MEPGL_STRIP=0"

@@ -18,6 +18,26 @@
 
 constexpr int NTS = 32;   // threads per block of the strip kernels
 
+// Two-component FP32 strings run the packed stencils (site_pair.cuh): the
+// window then holds psi as (Re psi_1, Re psi_2), (Im psi_1, Im psi_2) in the
+// two pair slots of the components.
+template <class T, int NC>
+struct StripPacked {
+    static constexpr bool v = MEPGL_STRIP_PAIR && NC == 2 && std::is_same<T, float>::value;
+};
+
+// (re, im) of two components <-> (Re 1, Re 2), (Im 1, Im 2): a 2 x 2 transpose.
+template <class V>
+__device__ __forceinline__ void transpose_pair(V &a, V &b)
+{
+    const V p = a, q = b;
+    a.x = p.x;
+    a.y = q.x;
+    b.x = p.y;
+    b.y = q.y;
+}
+
+
 constexpr unsigned FULL_MASK = 0xffffffffu;
 
 // Register window of one site: A(dx, dy), P(c, dx, dy); the strip kernels
@@ -40,6 +60,23 @@ struct RegView {
             }
     }
 };
+
+// Packed view of a register window (PairView) from a RegView of the same
+// site whose psi slots already hold the packed pairs.
+template <class T, int NC>
+__device__ __forceinline__ PairView pair_view(const RegView<T, NC> &r)
+{
+    PairView v;
+#pragma unroll
+    for (int y = 0; y < 3; ++y)
+#pragma unroll
+        for (int x = 0; x < 3; ++x) {
+            v.a[y][x] = r.a[y][x];
+            v.px[y][x] = r.p[0][y][x];
+            v.py[y][x] = r.p[NC - 1][y][x];
+        }
+    return v;
+}
 
 template <class T>
 __device__ __forceinline__ vec2_t<T> zero2()
@@ -244,6 +281,10 @@ __global__ void __launch_bounds__(NTS, MEPGL_MINB_STRIP) k_grad_s(const __grid_c
             hx[c].y = hv.y + alpha * hd.y;
             R.gold[c] = rc[2][c];
         }
+        if constexpr (StripPacked<T, NC>::v) {
+            transpose_pair(R.x[1], R.x[NC]);
+            transpose_pair(hx[1], hx[NC]);
+        }
         R.al = from_left2<T>(R.x[0], hx[0], L.lane);
         R.ar = from_right<T>(R.x[0], hx[0], L.lane);
 #pragma unroll
@@ -274,9 +315,14 @@ __global__ void __launch_bounds__(NTS, MEPGL_MINB_STRIP) k_grad_s(const __grid_c
         take(Rp, j + 1, hp1);
         if (r + 1 < rows) load(j + 2, true);
         const int s = L.gi + S.nx * j;
-        if (L.cok)
+        if (L.cok) {
+            V o[1 + NC];
 #pragma unroll
-            for (int c = 0; c < 1 + NC; ++c) xout[c][s] = R0.x[c];
+            for (int c = 0; c < 1 + NC; ++c) o[c] = R0.x[c];
+            if constexpr (StripPacked<T, NC>::v) transpose_pair(o[1], o[NC]);
+#pragma unroll
+            for (int c = 0; c < 1 + NC; ++c) xout[c][s] = o[c];
+        }
         RegView<T, NC> w3;
         w3.clear();
         w3.a[0][0] = Rm.al; w3.a[0][1] = Rm.x[0]; w3.a[0][2] = Rm.ar;
@@ -301,7 +347,12 @@ __global__ void __launch_bounds__(NTS, MEPGL_MINB_STRIP) k_grad_s(const __grid_c
             }
             T g[2 + 2 * NC];
             Wts<T> w;
-            if (MEPGL_STRIP_INTERIOR && R0.m == 0xffffu) {   // interior site: unit weights, folded in
+            if constexpr (StripPacked<T, NC>::v) {
+                w.load(R0.m);
+                PairParams pp;
+                pp.set(p);
+                site_gradient_pair(pair_view(w3), p, pp, w, hr, hl, hu, hd, f.maxwell, S.thin_film, g);
+            } else if (MEPGL_STRIP_INTERIOR && R0.m == 0xffffu) {   // interior site: unit weights, folded in
                 w.interior();
                 site_gradient_v<T, NC>(w3, p, w, hr, hl, hu, hd, f.maxwell, S.thin_film, g);
             } else {
@@ -385,6 +436,10 @@ __global__ void __launch_bounds__(NTS, MEPGL_MINB_STRIP) k_dir_poly_s(const __gr
             R.d[c].x = -rc[1][c].x + beta * rc[2][c].x;
             R.d[c].y = -rc[1][c].y + beta * rc[2][c].y;
         }
+        if constexpr (StripPacked<T, NC>::v) {
+            transpose_pair(R.x[1], R.x[NC]);
+            transpose_pair(R.d[1], R.d[NC]);
+        }
         R.m = rm;
     };
     auto load = [&](int j, bool issue) {
@@ -415,9 +470,14 @@ __global__ void __launch_bounds__(NTS, MEPGL_MINB_STRIP) k_dir_poly_s(const __gr
         else strip_halo<T, NC, 3, 3>(ring[0], src, S, L, j + 2, 0u, false);
         cp_async_wait_groups<2>();   // groups of rows j + 1 and j + 2 may still be pending
         const int s = L.gi + S.nx * j;
-        if (L.cok)
+        if (L.cok) {
+            V o[1 + NC];
 #pragma unroll
-            for (int c = 0; c < 1 + NC; ++c) dout[c][s] = R0.d[c];
+            for (int c = 0; c < 1 + NC; ++c) o[c] = R0.d[c];
+            if constexpr (StripPacked<T, NC>::v) transpose_pair(o[1], o[NC]);
+#pragma unroll
+            for (int c = 0; c < 1 + NC; ++c) dout[c][s] = o[c];
+        }
         // halo column of row j (this lane's side), new direction formed here
         const V(&h)[3][1 + NC] = ring[j % 3][L.lane == 0 ? 0 : 1];
         V hx[1 + NC], hd[1 + NC];
@@ -427,6 +487,10 @@ __global__ void __launch_bounds__(NTS, MEPGL_MINB_STRIP) k_dir_poly_s(const __gr
             const V hg = h[1][c], hdd = h[2][c];
             hd[c].x = -hg.x + beta * hdd.x;
             hd[c].y = -hg.y + beta * hdd.y;
+        }
+        if constexpr (StripPacked<T, NC>::v) {
+            transpose_pair(hx[1], hx[NC]);
+            transpose_pair(hd[1], hd[NC]);
         }
         RegView<T, NC> vx, vd;
         vx.clear();
@@ -454,7 +518,12 @@ __global__ void __launch_bounds__(NTS, MEPGL_MINB_STRIP) k_dir_poly_s(const __gr
             if (S.per_site) p.load_site(S, s, NC);
             T o[5];
             Wts<T> w;
-            if (MEPGL_STRIP_INTERIOR && R0.m == 0xffffu) {   // interior site: unit weights, folded in
+            if constexpr (StripPacked<T, NC>::v) {
+                w.load(R0.m);
+                PairParams pp;
+                pp.set(p);
+                site_poly_pair(pair_view(vx), pair_view(vd), p, pp, w, f.poly_compat, S.thin_film, o);
+            } else if (MEPGL_STRIP_INTERIOR && R0.m == 0xffffu) {   // interior site: unit weights, folded in
                 w.interior();
                 site_poly_v<T, NC>(vx, vd, p, w, f.poly_compat, S.thin_film, o);
             } else {
