@@ -237,12 +237,13 @@ def run_ours(args):
 
     # ---- per-pass timing on the launching stream (roofline) --------------------
     ms_grad, ms_dir = ctx.profile_passes(10)
+    k_grad, k_dir = ctx.pass_kernels()
     S = (2 + 2 * 2) * 4                    # bytes of state per site-image (A, psi_1, psi_2 in FP32)
     bytes_grad = (5 * S + 2) * units_per_step  # read x, d, g_prev; write x, g; masks
     bytes_dir = (4 * S + 2) * units_per_step   # read x, g, d; write d; masks
     peak, peak_kind = peaks()
-    kern = {"k_grad": {"ms": ms_grad, "bytes": bytes_grad, "gbs": bytes_grad / ms_grad / 1e6},
-            "k_dir_poly": {"ms": ms_dir, "bytes": bytes_dir, "gbs": bytes_dir / ms_dir / 1e6}}
+    kern = {k_grad: {"ms": ms_grad, "bytes": bytes_grad, "gbs": bytes_grad / ms_grad / 1e6},
+            k_dir: {"ms": ms_dir, "bytes": bytes_dir, "gbs": bytes_dir / ms_dir / 1e6}}
     dom = max(kern, key=lambda k: kern[k]["ms"])
     traffic = None
     tfile = os.path.join(ROOT, "profiles", "traffic_config2_fp32.json")

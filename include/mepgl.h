@@ -266,6 +266,13 @@ mepgl_status mepgl_info(const mepgl_ctx *ctx, int *n_images, int *precision, int
  * reference has no timing facility); used by the benchmark's roofline. */
 mepgl_status mepgl_profile_passes(mepgl_ctx *ctx, int steps, int use_cg, double *ms_grad, double *ms_dir_poly);
 
+/* Names of the kernels that run the two NLCG passes of this context in its
+ * current precision and FP64 arithmetic (FP32 passes are warp-strip or
+ * shared-memory-tile kernels, chosen when the library is built).  The
+ * strings are static.  No reference counterpart; labels timings and
+ * profiler captures. */
+mepgl_status mepgl_pass_kernels(const mepgl_ctx *ctx, const char **grad, const char **dir_poly);
+
 /* Allocation-free free energy.  No counterpart in the reference.  For callers
  * that cannot allocate device memory -- code running inside someone else's
  * CUDA-graph capture or memory pool, or an embedding that owns a fixed

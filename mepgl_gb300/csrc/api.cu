@@ -379,6 +379,7 @@ Launch make_launch(mepgl_ctx *c, int batch, int si = -1)
     L.batch = &c->batches[batch];
     const int t0 = si >= 0 ? c->string_tile0[si] : c->batch_tile0[batch];
     L.tiles = c->dtiles + t0;
+    L.tile0 = t0;
     L.n_tiles = si >= 0 ? c->string_ntiles[si] : c->batch_ntiles[batch];
     L.grid = L.n_tiles;
     L.precision = c->precision;
@@ -1164,6 +1165,13 @@ mepgl_status mepgl_info(const mepgl_ctx *c, int *n_images, int *precision, int64
     if (n_images) *n_images = c->strings[0].F;
     if (precision) *precision = c->precision;
     if (kernel_launches) *kernel_launches = c->launches;
+    return MEPGL_OK;
+}
+
+mepgl_status mepgl_pass_kernels(const mepgl_ctx *c, const char **grad, const char **dir_poly)
+{
+    if (!c || !grad || !dir_poly) return MEPGL_ERR_INVALID_ARG;
+    nlcg_pass_kernels(c->precision, c->opt.fp64_arith == MEPGL_FP64_PAIRED, grad, dir_poly);
     return MEPGL_OK;
 }
 

@@ -70,6 +70,12 @@ namespace mepgl {
 #ifndef MEPGL_MINB_STRIP
 #define MEPGL_MINB_STRIP 16   // single-warp blocks per SM: 128 registers
 #endif
+#ifndef MEPGL_MINB_STRIP_GRAD
+#define MEPGL_MINB_STRIP_GRAD MEPGL_MINB_STRIP
+#endif
+#ifndef MEPGL_MINB_STRIP_DIR
+#define MEPGL_MINB_STRIP_DIR MEPGL_MINB_STRIP
+#endif
 // strip row loop unrolled by the window period; interior sites with unit weights
 #ifndef MEPGL_STRIP_UNROLL
 #define MEPGL_STRIP_UNROLL 0
@@ -97,6 +103,14 @@ template <class T> struct TileRows { static constexpr int v = sizeof(T) == 4 ? M
 template <> struct TileRows<ff> { static constexpr int v = MEPGL_ROWS_F64; };
 
 int nlcg_step_launches() { return 2 + MEPGL_SPLIT_DIR; }
+
+void nlcg_pass_kernels(int precision, int paired, const char **grad, const char **dir_poly)
+{
+    (void)paired;
+    const bool strip = MEPGL_STRIP && precision == 0;
+    *grad = strip ? "k_grad_s" : "k_grad";
+    *dir_poly = strip ? "k_dir_poly_s" : "k_dir_poly";
+}
 
 int tile_rows(int precision) { return precision == 1 ? TileRows<double>::v : TileRows<float>::v; }
 
@@ -1278,7 +1292,7 @@ inline int grid_for(long n, int cap = 152 * 16)
 cudaError_t launch_grad(const Launch &L, const Scalars &sc, const StepFlags &f)
 {
 #if MEPGL_STRIP
-    if (L.precision == 0) DISPATCH_STRIP(L, k_grad_s, *L.batch, L.tiles, sc, f);
+    if (L.precision == 0) DISPATCH_STRIP(L, k_grad_s, *L.batch, L.tile0, sc, f);
     else DISPATCH_WIDE(L, k_grad, *L.batch, L.tiles, L.n_tiles, sc, f);
 #else
     DISPATCH_NLCG(L, k_grad, *L.batch, L.tiles, L.n_tiles, sc, f);
@@ -1298,7 +1312,7 @@ cudaError_t launch_dir_poly(const Launch &L, const Scalars &sc, const StepFlags 
     }
 #endif
 #if MEPGL_STRIP
-    if (L.precision == 0) DISPATCH_STRIP(L, k_dir_poly_s, *L.batch, L.tiles, sc, f);
+    if (L.precision == 0) DISPATCH_STRIP(L, k_dir_poly_s, *L.batch, L.tile0, sc, f);
     else DISPATCH_WIDE(L, k_dir_poly, *L.batch, L.tiles, L.n_tiles, sc, f);
 #else
     DISPATCH_NLCG(L, k_dir_poly, *L.batch, L.tiles, L.n_tiles, sc, f);

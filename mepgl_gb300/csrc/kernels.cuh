@@ -11,12 +11,15 @@ constexpr int LS_GRID = 2001;         // line-search grid points x_0 .. x_2000
 int tile_rows(int precision);
 // Kernel launches per NLCG step and launch group (2, or 3 with the split direction pass).
 int nlcg_step_launches();
+// Kernel names of the two NLCG passes for a precision (0 float, 1 double) and arithmetic.
+void nlcg_pass_kernels(int precision, int paired, const char **grad, const char **dir_poly);
 // Copy the neighbour-code weight tables to constant memory (idempotent).
 cudaError_t upload_mask_tables();
 
 struct Launch {
     const Batch *batch;          // host copy; passed by value to the kernels
     const TileRef *tiles;        // device
+    int tile0;                   // global index of tiles[0] (tiles are in (string, image, row, column) order)
     int n_tiles;
     int grid;                    // blocks launched (grid-stride over tiles)
     int precision;               // 0 float, 1 double

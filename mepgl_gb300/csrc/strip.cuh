@@ -174,6 +174,19 @@ __device__ __forceinline__ void strip_halo(vec2_t<T> (&slot)[2][NR][1 + NC], con
 template <int N>
 __device__ __forceinline__ void cp_async_wait_groups() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
 
+// Tile g of the global tile order (strings in order, each from its
+// tile_base: image, tile row, tile column), derived from the block index and
+// the descriptors alone so that it is uniform over the block.
+__device__ __forceinline__ TileRef strip_tile(const Batch &bt, int g)
+{
+    int s = 0;
+    for (int k = 1; k < bt.n; ++k)
+        if (g >= bt.s[k].tile_base) s = k;
+    TileRef t = flat_tile(bt.s[s], g - bt.s[s].tile_base);
+    t.s = (int16_t)s;
+    return t;
+}
+
 // Packed neighbour codes of the lane's site in row j (0 outside the lattice).
 __device__ __forceinline__ uint16_t strip_code(const StringDesc &S, const StripLane &L, int j)
 {
@@ -238,14 +251,13 @@ struct GradRow {
 // gradient of every site, |g|^2 and g . (g - g_prev); the last tile of an
 // image computes beta.  Same semantics as k_grad.
 template <class T, int NC>
-__global__ void __launch_bounds__(NTS, MEPGL_MINB_STRIP) k_grad_s(const __grid_constant__ Batch bt,
-                                                                  const TileRef *__restrict__ tiles, Scalars sc,
-                                                                  StepFlags f)
+__global__ void __launch_bounds__(NTS, MEPGL_MINB_STRIP_GRAD) k_grad_s(const __grid_constant__ Batch bt,
+                                                                  int tile0, Scalars sc, StepFlags f)
 {
     constexpr int TYT = TileRows<T>::v;
     using V = vec2_t<T>;
     __shared__ __align__(16) V ring[3][2][2][1 + NC];   // [row % 3][side][x, d][field]
-    const TileRef tr = tiles[blockIdx.x];
+    const TileRef tr = strip_tile(bt, tile0 + (int)blockIdx.x);
     const StringDesc &S = bt.s[tr.s];
     const int img = S.img_base + tr.n;
     const int i0 = tr.tx * TX, j0 = tr.ty * TYT;
@@ -401,15 +413,14 @@ struct DirRow {
 // quartic coefficients of F(x + a d); the last tile of an image runs the
 // line search.  Same semantics as k_dir_poly.
 template <class T, int NC>
-__global__ void __launch_bounds__(NTS, MEPGL_MINB_STRIP) k_dir_poly_s(const __grid_constant__ Batch bt,
-                                                                      const TileRef *__restrict__ tiles, Scalars sc,
-                                                                      StepFlags f)
+__global__ void __launch_bounds__(NTS, MEPGL_MINB_STRIP_DIR) k_dir_poly_s(const __grid_constant__ Batch bt,
+                                                                      int tile0, Scalars sc, StepFlags f)
 {
     constexpr int TYT = TileRows<T>::v;
     using V = vec2_t<T>;
     __shared__ __align__(16) V ring[3][2][3][1 + NC];   // [row % 3][side][x, g, d][field]
     __shared__ double coef[5];
-    const TileRef tr = tiles[blockIdx.x];
+    const TileRef tr = strip_tile(bt, tile0 + (int)blockIdx.x);
     const StringDesc &S = bt.s[tr.s];
     const int img = S.img_base + tr.n;
     const int i0 = tr.tx * TX, j0 = tr.ty * TYT;
