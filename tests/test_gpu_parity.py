@@ -163,6 +163,34 @@ def test_nlcg_steps_vs_oracle(i, opts):
     assert relmax(fin.psi_1, r["psi_1"]) < 1e-9
 
 
+@pytest.mark.parametrize("i", range(len(CASES) - 1))   # the 2 x 2 case converges to round-off: its step is arbitrary
+@pytest.mark.parametrize("maxwell", [False, True])
+def test_fp32_nlcg_steps_vs_oracle_fp32(i, maxwell):
+    """The FP32 NLCG passes (the warp-strip kernels, with the packed stencils
+    for two components) against the FP32 oracle, on the ragged, thin-film,
+    and per-site cases.  Exact line polynomial and exact line search
+    keep the step continuous in the data, so rounding differences stay
+    small: energies 2e-5 relative, steps 1e-3, fields 1e-4 of their max-norm
+    after six steps; Maxwell-only steps leave psi untouched."""
+    prob, st = _case(i)
+    o = cref.Oracle(prob, np.float32)
+    scale = np.max(np.abs(o.energy(st.a, st.psi_1, st.psi_2)))   # energies may converge to round-off
+    sv = o.solver(st, ls_mode=1, poly_compat=False)
+    c = make(prob, st, precision="fp32", line_search=1, line_polynomial=1)
+    for k in range(3):
+        sv.nlcg_steps(2, maxwell=maxwell)
+        c.nlcg_steps(2, maxwell=maxwell)
+        r = sv.get()
+        sc = c.image_scalars()
+        np.testing.assert_allclose(sc["fenergy"], r["fenergy"], rtol=2e-5, atol=2e-5 * scale)
+        np.testing.assert_allclose(sc["alpha"], r["alpha"], rtol=1e-3)
+    fin = c.get_state()
+    assert relmax(fin.a, r["a"]) < 1e-4
+    assert relmax(fin.psi_1, r["psi_1"]) < 1e-4
+    if maxwell:
+        np.testing.assert_array_equal(fin.psi_1, st.psi_1.astype(np.float32))
+
+
 def test_graph_and_direct_launches_agree():
     prob, st = _case(0)
     a = make(prob, st, use_graphs=1)
