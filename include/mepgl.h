@@ -268,10 +268,12 @@ mepgl_status mepgl_profile_passes(mepgl_ctx *ctx, int steps, int use_cg, double 
 
 /* Names of the kernels that run the two NLCG passes of this context in its
  * current precision and FP64 arithmetic (FP32 passes are warp-strip or
- * shared-memory-tile kernels, chosen when the library is built).  The
- * strings are static.  No reference counterpart; labels timings and
- * profiler captures. */
-mepgl_status mepgl_pass_kernels(const mepgl_ctx *ctx, const char **grad, const char **dir_poly);
+ * shared-memory-tile kernels, chosen when the library is built), and of the
+ * kernel that runs whole mepgl_nlcg_steps calls as one persistent launch
+ * ("" when the passes are launched separately; mepgl_profile_passes always
+ * times the separate pass kernels).  The strings are static.  No reference
+ * counterpart; labels timings and profiler captures. */
+mepgl_status mepgl_pass_kernels(const mepgl_ctx *ctx, const char **grad, const char **dir_poly, const char **fused);
 
 /* Allocation-free free energy.  No counterpart in the reference.  For callers
  * that cannot allocate device memory -- code running inside someone else's

@@ -34,9 +34,10 @@ TUNING = os.path.join(PKG, "tuning.json")
 # Strip candidates: rows per tile, single-warp blocks per SM for the
 # gradient and the direction pass (register budget 65536 / (32 x blocks)),
 # row loop unrolled by the window period, unit-weight path for interior
-# sites, packed FP32x2 stencils for two components.
-STRIP = [(32, 16, 16, 0, 0, 1), (32, 20, 20, 0, 0, 1), (32, 24, 24, 0, 0, 1), (32, 20, 16, 0, 0, 1),
-         (32, 16, 20, 0, 0, 1), (16, 20, 20, 0, 0, 1), (32, 16, 16, 0, 0, 0)]
+# sites, packed FP32x2 stencils for two components, all steps of a call in
+# one fused persistent launch, and its blocks per SM.
+STRIP = [(32, 16, 16, 0, 0, 1, 0, 16), (32, 16, 16, 0, 0, 1, 1, 12), (32, 16, 16, 0, 0, 1, 1, 16),
+         (16, 16, 16, 0, 0, 1, 1, 12), (32, 16, 16, 0, 0, 1, 1, 10)]
 # Tile candidates: rows per FP32 tile, min blocks per SM for the gradient
 # pass, for the direction pass, gradient-pass halo copy (0 through
 # registers, 1 cp.async), direction pass (0 fused, 1 split into a pointwise
@@ -44,7 +45,8 @@ STRIP = [(32, 16, 16, 0, 0, 1), (32, 20, 20, 0, 0, 1), (32, 24, 24, 0, 0, 1), (3
 # and g, d through registers, 1 all three by cp.async).
 TILE = [(16, 4, 4, 0, 0, 0)]
 CANDIDATES = [dict(MEPGL_STRIP=1, MEPGL_ROWS_F32=r, MEPGL_MINB_STRIP_GRAD=mg, MEPGL_MINB_STRIP_DIR=md,
-                   MEPGL_STRIP_UNROLL=u, MEPGL_STRIP_INTERIOR=i, MEPGL_STRIP_PAIR=pk) for r, mg, md, u, i, pk in STRIP] + [
+                   MEPGL_STRIP_UNROLL=u, MEPGL_STRIP_INTERIOR=i, MEPGL_STRIP_PAIR=pk, MEPGL_STRIP_FUSED=fu,
+                   MEPGL_MINB_STRIP_FUSED=mf) for r, mg, md, u, i, pk, fu, mf in STRIP] + [
     dict(MEPGL_STRIP=0, MEPGL_ROWS_F32=r, MEPGL_MINB_GRAD=g, MEPGL_MINB_DIR=d, MEPGL_GRAD_ASYNC=a,
          MEPGL_SPLIT_DIR=sp, MEPGL_DIR_ASYNC=da) for r, g, d, a, sp, da in TILE]
 

@@ -52,6 +52,8 @@ struct mepgl_ctx {
     std::vector<int> batch_tile0, batch_ntiles, string_batch;
     TileRef *dtiles = nullptr;
     int n_tiles = 0, total_images = 0;
+    unsigned long long *fqueue = nullptr;   // work counter of the fused NLCG launch
+    unsigned *fstage = nullptr;             // per-image stage counters of the fused NLCG launch
     std::vector<int> string_tile0, string_ntiles;
     Scalars sc{};
     double *dscratch = nullptr;   // per-image temporaries (energies, 3 adjoints)
@@ -259,6 +261,8 @@ void free_scalars(mepgl_ctx *c)
     cudaFree(S.alpha_pend); cudaFree(S.fenergy); cudaFree(S.poly); cudaFree(S.part); cudaFree(S.ticket);
     cudaFree(S.xtab_f); cudaFree(S.xtab_d); cudaFree(S.status);
     memset(&S, 0, sizeof(S));
+    cudaFree(c->fqueue); c->fqueue = nullptr;
+    cudaFree(c->fstage); c->fstage = nullptr;
     cudaFree(c->dscratch); c->dscratch = nullptr;
     cudaFree(c->ds); cudaFree(c->ds_jb); c->ds = c->ds_jb = nullptr;
     cudaFree(c->dtiles); c->dtiles = nullptr;
@@ -322,6 +326,8 @@ mepgl_status build_layout(mepgl_ctx *c)
     CK(c, cudaMemset(S.ticket, 0, I * sizeof(unsigned)));
     CK(c, cudaMalloc(&S.status, 16 * sizeof(int)));
     CK(c, cudaMemset(S.status, 0, 16 * sizeof(int)));
+    CK(c, cudaMalloc(&c->fqueue, sizeof(unsigned long long)));
+    CK(c, cudaMalloc(&c->fstage, I * sizeof(unsigned)));
     // line-search grid x_p = x_0 * m^p rounded to float / double at every step
     std::vector<double> xf(LS_GRID), xd(LS_GRID);
     float fx = 1e-10f;
@@ -460,6 +466,18 @@ mepgl_status two_step_graph(mepgl_ctx *c, int use_cg, int maxwell, cudaGraphExec
 
 mepgl_status nlcg_steps(mepgl_ctx *c, int iters, int use_cg, int maxwell)
 {
+    if (iters > 0 && nlcg_fused(c->precision)) {
+        // all steps of a batch in one persistent launch (per-image stages instead of kernel boundaries)
+        const StepFlags f0 = step_flags(c, 1, use_cg, maxwell);
+        for (size_t b = 0; b < c->batches.size(); ++b)
+            CK(c, launch_nlcg_fused(make_launch(c, (int)b), c->sc, f0, 1, iters, c->fqueue, c->fstage,
+                                    c->total_images));
+        c->xi ^= iters & 1;
+        c->di ^= iters & 1;
+        c->launches += (int64_t)c->batches.size();
+        c->pending = true;
+        return MEPGL_OK;
+    }
     int it = 1;
     if (c->opt.use_graphs && iters >= 2) {
         cudaGraphExec_t ex;
@@ -474,6 +492,21 @@ mepgl_status nlcg_steps(mepgl_ctx *c, int iters, int use_cg, int maxwell)
     for (; it <= iters; ++it) {
         mepgl_status st = one_step(c, it, use_cg, maxwell);
         if (st != MEPGL_OK) return st;
+    }
+    return MEPGL_OK;
+}
+
+// Device-side error flags: status[0] is set when a stage wait of the fused
+// NLCG launch ran out (the launch then stopped early).  Read on the stream
+// after the work before it, then cleared.
+mepgl_status check_device_status(mepgl_ctx *c)
+{
+    int st = 0;
+    CK(c, cudaMemcpyAsync(&st, c->sc.status, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+    CK(c, cudaStreamSynchronize(c->stream));
+    if (st) {
+        CK(c, cudaMemsetAsync(c->sc.status, 0, sizeof(int), c->stream));
+        return fail(c, MEPGL_ERR_CUDA, "fused NLCG launch: a per-image stage wait ran out; the steps are incomplete");
     }
     return MEPGL_OK;
 }
@@ -886,7 +919,9 @@ mepgl_status mepgl_batch_get_state(mepgl_ctx *c, int string, void *a, void *psi_
     StringHost &s = c->strings[string];
     void *dst[3] = {a, psi_1, psi_2};
     const void *src[3] = {s.x[c->xi][0], s.x[c->xi][1], s.x[c->xi][2]};
-    return copy_fields(c, s, dst, src, memory, false);
+    st = copy_fields(c, s, dst, src, memory, false);
+    if (st == MEPGL_OK && nlcg_fused(c->precision)) st = check_device_status(c);
+    return st;
 }
 
 mepgl_status mepgl_free_energy(mepgl_ctx *c, double *fenergy) { return mepgl_batch_free_energy(c, 0, fenergy); }
@@ -1001,7 +1036,7 @@ mepgl_status mepgl_batch_image_scalars(mepgl_ctx *c, int string, double *fenergy
     if (g_norm2) CK(c, cudaMemcpyAsync(g_norm2, c->sc.gn0 + o, F * 8, cudaMemcpyDeviceToHost, c->stream));
     if (alpha) CK(c, cudaMemcpyAsync(alpha, c->sc.alpha + o, F * 8, cudaMemcpyDeviceToHost, c->stream));
     CK(c, cudaStreamSynchronize(c->stream));
-    return MEPGL_OK;
+    return nlcg_fused(c->precision) ? check_device_status(c) : MEPGL_OK;
 }
 
 mepgl_status mepgl_compute_jb(mepgl_ctx *c, void *b, void *j_1, void *j_2, int memory)
@@ -1168,10 +1203,11 @@ mepgl_status mepgl_info(const mepgl_ctx *c, int *n_images, int *precision, int64
     return MEPGL_OK;
 }
 
-mepgl_status mepgl_pass_kernels(const mepgl_ctx *c, const char **grad, const char **dir_poly)
+mepgl_status mepgl_pass_kernels(const mepgl_ctx *c, const char **grad, const char **dir_poly, const char **fused)
 {
-    if (!c || !grad || !dir_poly) return MEPGL_ERR_INVALID_ARG;
+    if (!c || !grad || !dir_poly || !fused) return MEPGL_ERR_INVALID_ARG;
     nlcg_pass_kernels(c->precision, c->opt.fp64_arith == MEPGL_FP64_PAIRED, grad, dir_poly);
+    *fused = nlcg_fused(c->precision) ? "k_nlcg_s" : "";
     return MEPGL_OK;
 }
 
@@ -1214,7 +1250,7 @@ mepgl_status mepgl_synchronize(mepgl_ctx *c)
 {
     if (!c) return MEPGL_ERR_INVALID_ARG;
     CK(c, cudaStreamSynchronize(c->stream));
-    return MEPGL_OK;
+    return nlcg_fused(c->precision) ? check_device_status(c) : MEPGL_OK;
 }
 
 }  // extern "C"

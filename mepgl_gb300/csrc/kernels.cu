@@ -87,6 +87,13 @@ namespace mepgl {
 #ifndef MEPGL_STRIP_PAIR
 #define MEPGL_STRIP_PAIR 1
 #endif
+// FP32 NLCG steps as one persistent launch with per-image stage counters (strip.cuh)
+#ifndef MEPGL_STRIP_FUSED
+#define MEPGL_STRIP_FUSED 0
+#endif
+#ifndef MEPGL_MINB_STRIP_FUSED
+#define MEPGL_MINB_STRIP_FUSED MEPGL_MINB_STRIP
+#endif
 #if MEPGL_STRIP && MEPGL_SPLIT_DIR
 #error "MEPGL_SPLIT_DIR applies to the tile kernels; build it with MEPGL_STRIP=0"
 #endif
@@ -103,6 +110,8 @@ template <class T> struct TileRows { static constexpr int v = sizeof(T) == 4 ? M
 template <> struct TileRows<ff> { static constexpr int v = MEPGL_ROWS_F64; };
 
 int nlcg_step_launches() { return 2 + MEPGL_SPLIT_DIR; }
+
+bool nlcg_fused(int precision) { return MEPGL_STRIP && MEPGL_STRIP_FUSED && precision == 0; }
 
 void nlcg_pass_kernels(int precision, int paired, const char **grad, const char **dir_poly)
 {
@@ -1318,6 +1327,41 @@ cudaError_t launch_dir_poly(const Launch &L, const Scalars &sc, const StepFlags 
     DISPATCH_NLCG(L, k_dir_poly, *L.batch, L.tiles, L.n_tiles, sc, f);
 #endif
     return cudaGetLastError();
+}
+
+cudaError_t launch_nlcg_fused(const Launch &L, const Scalars &sc, const StepFlags &f0, int it0, int steps,
+                              unsigned long long *queue, unsigned *stage, int n_stage)
+{
+#if MEPGL_STRIP
+    static int slots[2] = {0, 0};
+    const int ci = L.ncomp == 2 ? 1 : 0;
+    if (slots[ci] == 0) {
+        int dev = 0, sms = 0, nb = 0;
+        cudaError_t e = cudaGetDevice(&dev);
+        if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        if (e == cudaSuccess)
+            e = ci ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_nlcg_s<float, 2>, NTS, 0)
+                   : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_nlcg_s<float, 1>, NTS, 0);
+        if (e != cudaSuccess) return e;
+        slots[ci] = nb * sms > 0 ? nb * sms : 1;
+    }
+    StepPlan plan;
+    plan.xi0 = f0.xin;
+    plan.di0 = f0.din;
+    plan.it0 = it0;
+    plan.base = f0;
+    cudaError_t e = cudaMemsetAsync(queue, 0, sizeof(unsigned long long), L.stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(stage, 0, sizeof(unsigned) * (size_t)n_stage, L.stream);
+    if (e != cudaSuccess) return e;
+    const long long items = 2LL * L.n_tiles * steps;
+    const int grid = items < slots[ci] ? (int)items : slots[ci];
+    if (ci) k_nlcg_s<float, 2><<<grid, NTS, 0, L.stream>>>(*L.batch, L.tile0, L.n_tiles, steps, plan, sc, queue, stage);
+    else k_nlcg_s<float, 1><<<grid, NTS, 0, L.stream>>>(*L.batch, L.tile0, L.n_tiles, steps, plan, sc, queue, stage);
+    return cudaGetLastError();
+#else
+    (void)L; (void)sc; (void)f0; (void)it0; (void)steps; (void)queue; (void)stage; (void)n_stage;
+    return cudaErrorNotSupported;
+#endif
 }
 
 cudaError_t launch_energy(const Launch &L, const Scalars &sc, int xbuf, double *out)

@@ -36,6 +36,13 @@ struct StepFlags {
     int poly_compat, ls_exact;
 };
 
+// True when the NLCG steps of this precision run as one fused persistent launch.
+bool nlcg_fused(int precision);
+// `steps` NLCG steps (iterations it0, it0 + 1, ...; step 0 with the buffers
+// of f0) of the launch's tiles in one persistent launch; queue (one counter)
+// and stage (one per global image, n_stage) are reset on the stream first.
+cudaError_t launch_nlcg_fused(const Launch &L, const Scalars &sc, const StepFlags &f0, int it0, int steps,
+                              unsigned long long *queue, unsigned *stage, int n_stage);
 // Pass 1: x <- x + alpha_pend d (into x[xout]); g = dF/dx; |g|^2, g.(g - g_prev);
 // the last tile of each image sets beta.
 cudaError_t launch_grad(const Launch &L, const Scalars &sc, const StepFlags &f);

@@ -247,17 +247,22 @@ struct GradRow {
     uint16_t m;
 };
 
-// Pass A as a warp strip: x <- x + alpha_pend d over the tile (+ halo), the
-// gradient of every site, |g|^2 and g . (g - g_prev); the last tile of an
-// image computes beta.  Same semantics as k_grad.
+// Halo ring of the gradient pass: [row % 3][side][x, d][field].
 template <class T, int NC>
-__global__ void __launch_bounds__(NTS, MEPGL_MINB_STRIP_GRAD) k_grad_s(const __grid_constant__ Batch bt,
-                                                                  int tile0, Scalars sc, StepFlags f)
+using GradRing = vec2_t<T>[3][2][2][1 + NC];
+
+// Pass A on one tile as a warp strip: x <- x + alpha_pend d over the tile
+// (+ halo), the gradient of every site, |g|^2 and g . (g - g_prev); the last
+// tile of an image computes beta.  Same semantics as k_grad.  Returns true
+// (in every lane) when this tile finished its image.  Before the tile's
+// partials are counted every lane fences its field stores, so that a
+// consumer that has seen the image finished (same launch) reads them.
+template <class T, int NC>
+__device__ __forceinline__ bool grad_tile(const Batch &bt, const TileRef tr, const Scalars &sc, const StepFlags &f,
+                                          GradRing<T, NC> &ring)
 {
     constexpr int TYT = TileRows<T>::v;
     using V = vec2_t<T>;
-    __shared__ __align__(16) V ring[3][2][2][1 + NC];   // [row % 3][side][x, d][field]
-    const TileRef tr = strip_tile(bt, tile0 + (int)blockIdx.x);
     const StringDesc &S = bt.s[tr.s];
     const int img = S.img_base + tr.n;
     const int i0 = tr.tx * TX, j0 = tr.ty * TYT;
@@ -273,7 +278,7 @@ __global__ void __launch_bounds__(NTS, MEPGL_MINB_STRIP_GRAD) k_grad_s(const __g
         xout[c] = static_cast<V *>(S.x[f.xout][c]) + off;
         gcur[c] = static_cast<V *>(S.g[f.gcur][c]) + off;
     }
-    const T alpha = (T)sc.alpha_pend[img];
+    const T alpha = (T)__ldcg(sc.alpha_pend + img);
     const unsigned fields = alpha != (T)0 ? 3u : 1u;   // d is not read when nothing is pending
     SiteParams<T> p;
     p.load_uniform(S);
@@ -389,16 +394,28 @@ __global__ void __launch_bounds__(NTS, MEPGL_MINB_STRIP_GRAD) k_grad_s(const __g
     }
     const int tpi = S.tiles_x * S.tiles_y;
     double tot[2];
-    if (finish_image_warp<2>(v, sc, part_slot(S, tr), S.tile_base + tr.n * tpi, tpi, img, tot) && L.lane == 0) {
+    __threadfence();
+    __syncwarp();
+    const bool fin = finish_image_warp<2>(v, sc, part_slot(S, tr), S.tile_base + tr.n * tpi, tpi, img, tot);
+    if (fin && L.lane == 0) {
         (f.gcur ? sc.gn1 : sc.gn0)[img] = tot[0];
         sc.gdg[img] = tot[1];
         double beta = 0.0;
         if (f.use_cg) {
-            beta = tot[1] / (f.gprev ? sc.gn1 : sc.gn0)[img];
+            beta = tot[1] / __ldcg((f.gprev ? sc.gn1 : sc.gn0) + img);
             beta = beta > 0.0 ? beta : 0.0;   // Polak-Ribiere clipped at 0; NaN -> 0
         }
         sc.beta[img] = beta;
     }
+    return fin;
+}
+
+template <class T, int NC>
+__global__ void __launch_bounds__(NTS, MEPGL_MINB_STRIP_GRAD) k_grad_s(const __grid_constant__ Batch bt,
+                                                                  int tile0, Scalars sc, StepFlags f)
+{
+    __shared__ __align__(16) GradRing<T, NC> ring;
+    grad_tile<T, NC>(bt, strip_tile(bt, tile0 + (int)blockIdx.x), sc, f, ring);
 }
 
 // One row of the polynomial window: fields and new direction of the lane's
@@ -409,18 +426,21 @@ struct DirRow {
     uint16_t m;
 };
 
-// Pass B as a warp strip: d <- -g + beta d over the tile (+ halo), the
-// quartic coefficients of F(x + a d); the last tile of an image runs the
-// line search.  Same semantics as k_dir_poly.
+// Halo ring of the direction pass: [row % 3][side][x, g, d][field].
 template <class T, int NC>
-__global__ void __launch_bounds__(NTS, MEPGL_MINB_STRIP_DIR) k_dir_poly_s(const __grid_constant__ Batch bt,
-                                                                      int tile0, Scalars sc, StepFlags f)
+using DirRing = vec2_t<T>[3][2][3][1 + NC];
+
+// Pass B on one tile as a warp strip: d <- -g + beta d over the tile
+// (+ halo), the quartic coefficients of F(x + a d); the last tile of an
+// image runs the line search.  Same semantics as k_dir_poly.  Returns true
+// (in every lane) when this tile finished its image; field stores are
+// fenced as in grad_tile.
+template <class T, int NC>
+__device__ __forceinline__ bool dir_tile(const Batch &bt, const TileRef tr, const Scalars &sc, const StepFlags &f,
+                                         DirRing<T, NC> &ring, double (&coef)[5])
 {
     constexpr int TYT = TileRows<T>::v;
     using V = vec2_t<T>;
-    __shared__ __align__(16) V ring[3][2][3][1 + NC];   // [row % 3][side][x, g, d][field]
-    __shared__ double coef[5];
-    const TileRef tr = strip_tile(bt, tile0 + (int)blockIdx.x);
     const StringDesc &S = bt.s[tr.s];
     const int img = S.img_base + tr.n;
     const int i0 = tr.tx * TX, j0 = tr.ty * TYT;
@@ -435,7 +455,7 @@ __global__ void __launch_bounds__(NTS, MEPGL_MINB_STRIP_DIR) k_dir_poly_s(const 
         src[2][c] = static_cast<const V *>(S.d[f.din][c]) + off;
         dout[c] = static_cast<V *>(S.d[f.dout][c]) + off;
     }
-    const T beta = (T)sc.beta[img];
+    const T beta = (T)__ldcg(sc.beta + img);
     SiteParams<T> p;
     p.load_uniform(S);
     V rc[3][1 + NC];
@@ -550,7 +570,10 @@ __global__ void __launch_bounds__(NTS, MEPGL_MINB_STRIP_DIR) k_dir_poly_s(const 
     }
     const int tpi = S.tiles_x * S.tiles_y;
     double tot[5];
-    if (finish_image_warp<5>(v, sc, part_slot(S, tr), S.tile_base + tr.n * tpi, tpi, img, tot)) {
+    __threadfence();
+    __syncwarp();
+    const bool fin = finish_image_warp<5>(v, sc, part_slot(S, tr), S.tile_base + tr.n * tpi, tpi, img, tot);
+    if (fin) {
         if (L.lane == 0) {
 #pragma unroll
             for (int k = 0; k < 5; ++k) coef[k] = tot[k];
@@ -566,6 +589,116 @@ __global__ void __launch_bounds__(NTS, MEPGL_MINB_STRIP_DIR) k_dir_poly_s(const 
         if (L.lane == 0) {
             sc.alpha[img] = alpha;
             sc.alpha_pend[img] = alpha;
+        }
+        __syncwarp();
+    }
+    return fin;
+}
+
+template <class T, int NC>
+__global__ void __launch_bounds__(NTS, MEPGL_MINB_STRIP_DIR) k_dir_poly_s(const __grid_constant__ Batch bt,
+                                                                      int tile0, Scalars sc, StepFlags f)
+{
+    __shared__ __align__(16) DirRing<T, NC> ring;
+    __shared__ double coef[5];
+    dir_tile<T, NC>(bt, strip_tile(bt, tile0 + (int)blockIdx.x), sc, f, ring, coef);
+}
+
+// ------------------------------------------------------------ fused steps
+// `steps` NLCG steps of one launch's tiles in a single persistent launch.
+// Work items are (step, pass, tile) in that order, handed out by a global
+// counter.  The direction pass of an image needs only that image's
+// gradient pass of the same step, and the next gradient pass of an image
+// needs only its direction pass (the step alpha), so an item waits on a
+// per-image stage counter instead of a kernel boundary: stage = 2k + 1 once
+// the gradient pass of step k finished the image, 2k + 2 once its
+// direction pass did.  An item depends only on items handed out before it,
+// and an item is only taken by a running block, so the waits always end;
+// each is still bounded, and a wait that runs out sets status[0] and
+// ends its block.
+
+// Step plan of a fused launch: the buffers and gradient slot of step k
+// follow from those of step 0 as the separate launches toggle them.
+struct StepPlan {
+    int xi0, di0, it0;   // x and d buffers read by step 0; iteration number of step 0
+    StepFlags base;      // use_cg, maxwell and the line-search options
+    __device__ __forceinline__ StepFlags step(int k) const
+    {
+        StepFlags f = base;
+        f.gcur = (it0 + k) & 1;
+        f.gprev = f.gcur ^ 1;
+        f.xin = xi0 ^ (k & 1);
+        f.xout = f.xin ^ 1;
+        f.din = di0 ^ (k & 1);
+        f.dout = f.din ^ 1;
+        return f;
+    }
+};
+
+constexpr unsigned STAGE_WAIT_POLLS = 1u << 22;   // x about 100 ns per poll
+
+// Lane 0 waits until stage >= need (acquire, then a fence so that the whole
+// warp's later loads see what the finishing block wrote); false if the
+// wait ran out.
+__device__ __forceinline__ bool wait_stage(const unsigned *stage, unsigned need, int *status)
+{
+    int ok = 1;
+    if ((threadIdx.x & 31) == 0) {
+        unsigned polls = 0, v;
+        for (;;) {
+            asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(stage) : "memory");
+            if (v >= need) break;
+            if (++polls > STAGE_WAIT_POLLS) {
+                atomicExch(status, 1);
+                ok = 0;
+                break;
+            }
+            __nanosleep(64);
+        }
+        __threadfence();
+    }
+    ok = __shfl_sync(FULL_MASK, ok, 0);
+    __syncwarp();
+    return ok != 0;
+}
+
+__device__ __forceinline__ void publish_stage(unsigned *stage, unsigned value)
+{
+    if ((threadIdx.x & 31) == 0) {
+        __threadfence();
+        asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(stage), "r"(value) : "memory");
+    }
+    __syncwarp();
+}
+
+template <class T, int NC>
+__global__ void __launch_bounds__(NTS, MEPGL_MINB_STRIP_FUSED) k_nlcg_s(const __grid_constant__ Batch bt, int tile0,
+                                                                        int n_tiles, int steps, StepPlan plan,
+                                                                        Scalars sc, unsigned long long *queue,
+                                                                        unsigned *stage)
+{
+    __shared__ __align__(16) GradRing<T, NC> gring;
+    __shared__ __align__(16) DirRing<T, NC> dring;
+    __shared__ double coef[5];
+    const unsigned long long per_step = 2ull * (unsigned long long)n_tiles;
+    const unsigned long long total = per_step * (unsigned long long)steps;
+    for (;;) {
+        unsigned long long item = 0;
+        if ((threadIdx.x & 31) == 0) item = atomicAdd(queue, 1ull);
+        item = __shfl_sync(FULL_MASK, item, 0);
+        if (item >= total) return;
+        const int k = (int)(item / per_step);
+        const int r = (int)(item - (unsigned long long)k * per_step);
+        const int pass = r >= n_tiles ? 1 : 0, u = r - pass * n_tiles;
+        const TileRef tr = strip_tile(bt, tile0 + u);
+        const int img = bt.s[tr.s].img_base + tr.n;
+        const unsigned need = 2u * (unsigned)k + (unsigned)pass;
+        if (need > 0 && !wait_stage(stage + img, need, sc.status)) return;
+        const StepFlags f = plan.step(k);
+        if (pass == 0) {
+            if (grad_tile<T, NC>(bt, tr, sc, f, gring)) publish_stage(stage + img, need + 1);
+        } else {
+            if (dir_tile<T, NC>(bt, tr, sc, f, dring, coef)) publish_stage(stage + img, need + 1);
         }
     }
 }

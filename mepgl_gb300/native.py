@@ -92,7 +92,7 @@ _SIGS = {
     "mepgl_info": (C.c_int, [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int64)]),
     "mepgl_synchronize": (C.c_int, [C.c_void_p]),
     "mepgl_profile_passes": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_void_p]),
-    "mepgl_pass_kernels": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
+    "mepgl_pass_kernels": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     "mepgl_free_energy_noalloc": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_double]
                                   + [C.c_void_p] * 11 + [C.c_double] * 5 + [C.c_void_p] * 5),
     "mepgl_noalloc_last_error": (C.c_char_p, []),
@@ -350,10 +350,11 @@ class StringContext:
         return dict(n_images=n.value, precision="fp64" if p.value else "fp32", kernel_launches=k.value)
 
     def pass_kernels(self):
-        """(gradient pass, direction/line pass) kernel names for the current precision."""
-        g, d = C.c_char_p(), C.c_char_p()
-        self._check(self.L.mepgl_pass_kernels(self.h, C.byref(g), C.byref(d)))
-        return g.value.decode(), d.value.decode()
+        """(gradient pass, direction/line pass, fused steps or "") kernel names
+        for the current precision."""
+        g, d, f = C.c_char_p(), C.c_char_p(), C.c_char_p()
+        self._check(self.L.mepgl_pass_kernels(self.h, C.byref(g), C.byref(d), C.byref(f)))
+        return g.value.decode(), d.value.decode(), f.value.decode()
 
     def profile_passes(self, steps: int, nlcg: bool = True):
         """Mean milliseconds of (gradient pass, direction/line pass) over `steps` real steps."""
