@@ -61,6 +61,13 @@ enum { MEPGL_DISC_REFERENCE = 0, MEPGL_DISC_LINK = 1 };
  * reductions, line search and every other kernel stay double.  No
  * reference counterpart. */
 enum { MEPGL_FP64_NATIVE = 0, MEPGL_FP64_PAIRED = 1 };
+/* How the FP32 NLCG steps of a mepgl_nlcg_steps call are launched: two pass
+ * kernels per step, or every step of the call in one persistent launch whose
+ * tiles wait on per-image stage counters instead of kernel boundaries.  AUTO
+ * fuses the batches of at most a few waves of tiles, where the boundaries
+ * idle much of the GPU.  Both give the same results bit for bit.  No
+ * reference counterpart. */
+enum { MEPGL_FP32_STEPS_AUTO = 0, MEPGL_FP32_STEPS_PASSES = 1, MEPGL_FP32_STEPS_FUSED = 2 };
 
 /* The physical problem.  Replaces the generated headers config.cuh/real.cuh
  * (N, dx, MULTICOMPONENT, NO_SELF_FIELD, DOUBLE_PRECISION) and the lattice
@@ -93,6 +100,7 @@ typedef struct mepgl_options {
     int32_t tile_rows;         /* rows per stencil tile: 0 = auto, 4, 8 or 16   */
     int32_t discretization;    /* MEPGL_DISC_*                                  */
     int32_t fp64_arith;        /* MEPGL_FP64_*                                  */
+    int32_t fp32_steps;        /* MEPGL_FP32_STEPS_*                            */
 } mepgl_options;
 
 typedef struct mepgl_ctx mepgl_ctx;

@@ -464,9 +464,22 @@ mepgl_status two_step_graph(mepgl_ctx *c, int use_cg, int maxwell, cudaGraphExec
     return MEPGL_OK;
 }
 
+// Fused FP32 steps pay where a batch is a few waves of the pass kernels
+// (the kernel boundaries then idle much of the GPU); on larger batches the
+// pass kernels, which hold more warps per SM, are faster.
+bool use_fused(const mepgl_ctx *c)
+{
+    if (!nlcg_fused(c->precision) || c->opt.fp32_steps == MEPGL_FP32_STEPS_PASSES) return false;
+    if (c->opt.fp32_steps == MEPGL_FP32_STEPS_FUSED) return true;
+    const long long cap = (long long)fuse_waves() * strip_pass_slots(c->ncomp);
+    for (int n : c->batch_ntiles)
+        if (n > cap) return false;
+    return true;
+}
+
 mepgl_status nlcg_steps(mepgl_ctx *c, int iters, int use_cg, int maxwell)
 {
-    if (iters > 0 && nlcg_fused(c->precision)) {
+    if (iters > 0 && use_fused(c)) {
         // all steps of a batch in one persistent launch (per-image stages instead of kernel boundaries)
         const StepFlags f0 = step_flags(c, 1, use_cg, maxwell);
         for (size_t b = 0; b < c->batches.size(); ++b)
@@ -706,6 +719,7 @@ void mepgl_default_options(mepgl_options *o)
     o->tile_rows = 0;
     o->discretization = MEPGL_DISC_REFERENCE;
     o->fp64_arith = MEPGL_FP64_NATIVE;
+    o->fp32_steps = MEPGL_FP32_STEPS_AUTO;
 }
 
 const char *mepgl_version(void) { return "mepgl_gb300 0.1 (sm_103a)"; }
@@ -748,9 +762,10 @@ mepgl_status mepgl_create_batch(const mepgl_problem *probs, int n_strings, const
     if (opt) c->opt = *opt;
     else mepgl_default_options(&c->opt);
     if ((c->opt.discretization != MEPGL_DISC_REFERENCE && c->opt.discretization != MEPGL_DISC_LINK) ||
-        (c->opt.fp64_arith != MEPGL_FP64_NATIVE && c->opt.fp64_arith != MEPGL_FP64_PAIRED)) {
+        (c->opt.fp64_arith != MEPGL_FP64_NATIVE && c->opt.fp64_arith != MEPGL_FP64_PAIRED) ||
+        c->opt.fp32_steps < MEPGL_FP32_STEPS_AUTO || c->opt.fp32_steps > MEPGL_FP32_STEPS_FUSED) {
         delete c;
-        return fail(nullptr, MEPGL_ERR_INVALID_ARG, "mepgl_create: unknown discretization or fp64_arith");
+        return fail(nullptr, MEPGL_ERR_INVALID_ARG, "mepgl_create: unknown discretization, fp64_arith or fp32_steps");
     }
     c->ncomp = p->multicomponent ? 2 : 1;
     c->thin_film = p->thin_film ? 1 : 0;
@@ -1207,7 +1222,7 @@ mepgl_status mepgl_pass_kernels(const mepgl_ctx *c, const char **grad, const cha
 {
     if (!c || !grad || !dir_poly || !fused) return MEPGL_ERR_INVALID_ARG;
     nlcg_pass_kernels(c->precision, c->opt.fp64_arith == MEPGL_FP64_PAIRED, grad, dir_poly);
-    *fused = nlcg_fused(c->precision) ? "k_nlcg_s" : "";
+    *fused = use_fused(c) ? "k_nlcg_s" : "";
     return MEPGL_OK;
 }
 

@@ -94,6 +94,11 @@ namespace mepgl {
 #ifndef MEPGL_MINB_STRIP_FUSED
 #define MEPGL_MINB_STRIP_FUSED MEPGL_MINB_STRIP
 #endif
+// fused steps only for batches of at most this many waves of the pass kernels
+// (beyond that the boundaries cost little and the pass kernels hold more warps)
+#ifndef MEPGL_FUSE_WAVES
+#define MEPGL_FUSE_WAVES 4
+#endif
 #if MEPGL_STRIP && MEPGL_SPLIT_DIR
 #error "MEPGL_SPLIT_DIR applies to the tile kernels; build it with MEPGL_STRIP=0"
 #endif
@@ -112,6 +117,8 @@ template <> struct TileRows<ff> { static constexpr int v = MEPGL_ROWS_F64; };
 int nlcg_step_launches() { return 2 + MEPGL_SPLIT_DIR; }
 
 bool nlcg_fused(int precision) { return MEPGL_STRIP && MEPGL_STRIP_FUSED && precision == 0; }
+
+int fuse_waves() { return MEPGL_FUSE_WAVES; }
 
 void nlcg_pass_kernels(int precision, int paired, const char **grad, const char **dir_poly)
 {
@@ -1327,6 +1334,28 @@ cudaError_t launch_dir_poly(const Launch &L, const Scalars &sc, const StepFlags 
     DISPATCH_NLCG(L, k_dir_poly, *L.batch, L.tiles, L.n_tiles, sc, f);
 #endif
     return cudaGetLastError();
+}
+
+int strip_pass_slots(int ncomp)
+{
+#if MEPGL_STRIP
+    static int slots[2] = {0, 0};
+    const int ci = ncomp == 2 ? 1 : 0;
+    if (slots[ci] == 0) {
+        int dev = 0, sms = 0, nb = 0;
+        if (cudaGetDevice(&dev) != cudaSuccess ||
+            cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+            return 0;
+        const cudaError_t e = ci ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_dir_poly_s<float, 2>, NTS, 0)
+                                 : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_dir_poly_s<float, 1>, NTS, 0);
+        if (e != cudaSuccess) return 0;
+        slots[ci] = nb * sms;
+    }
+    return slots[ci];
+#else
+    (void)ncomp;
+    return 0;
+#endif
 }
 
 cudaError_t launch_nlcg_fused(const Launch &L, const Scalars &sc, const StepFlags &f0, int it0, int steps,

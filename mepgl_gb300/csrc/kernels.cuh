@@ -36,8 +36,12 @@ struct StepFlags {
     int poly_compat, ls_exact;
 };
 
-// True when the NLCG steps of this precision run as one fused persistent launch.
+// True when this build has fused FP32 NLCG steps (one persistent launch per call).
 bool nlcg_fused(int precision);
+// Fused steps are used for batches of at most fuse_waves() x strip_pass_slots()
+// tiles: resident blocks of the FP32 pass kernels on the current device.
+int fuse_waves();
+int strip_pass_slots(int ncomp);
 // `steps` NLCG steps (iterations it0, it0 + 1, ...; step 0 with the buffers
 // of f0) of the launch's tiles in one persistent launch; queue (one counter)
 // and stage (one per global image, n_stage) are reset on the stream first.

@@ -31,6 +31,7 @@ METRIC_FIELDS, METRIC_JB = 0, 1
 REDIST_LINEAR, REDIST_CUBIC = 0, 1
 DISC_REFERENCE, DISC_LINK = 0, 1
 FP64_NATIVE, FP64_PAIRED = 0, 1
+FP32_STEPS_AUTO, FP32_STEPS_PASSES, FP32_STEPS_FUSED = 0, 1, 2
 
 _STATUS = {0: "OK", 1: "INVALID_ARG", 2: "CUDA", 3: "NAN", 4: "IO", 5: "UNSUPPORTED", 6: "STATE"}
 
@@ -52,7 +53,7 @@ class MepglProblem(C.Structure):
 class MepglOptions(C.Structure):
     _fields_ = [("line_search", C.c_int32), ("line_polynomial", C.c_int32), ("spline", C.c_int32),
                 ("metric", C.c_int32), ("use_graphs", C.c_int32), ("tile_rows", C.c_int32),
-                ("discretization", C.c_int32), ("fp64_arith", C.c_int32)]
+                ("discretization", C.c_int32), ("fp64_arith", C.c_int32), ("fp32_steps", C.c_int32)]
 
 
 class MepglVortex(C.Structure):

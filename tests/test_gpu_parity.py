@@ -191,6 +191,34 @@ def test_fp32_nlcg_steps_vs_oracle_fp32(i, maxwell):
         np.testing.assert_array_equal(fin.psi_1, st.psi_1.astype(np.float32))
 
 
+@pytest.mark.parametrize("mc", [True, False])
+def test_fused_fp32_steps_equal_pass_kernels(mc):
+    """The fused persistent launch runs the same tile code with the same
+    partial-sum order as the two pass kernels: identical results, bit for
+    bit, over calls of odd and even step counts (ragged lattice, several
+    tiles per image, two strings in one batch)."""
+    from mepgl_gb300.native import StringBatch, FP32_STEPS_FUSED, FP32_STEPS_PASSES
+    rng = np.random.default_rng(77)
+    probs, sts = [], []
+    for n in (70, 45):
+        prob = W.random_problem(rng, n=n, multicomponent=mc)
+        probs.append(prob)
+        sts.append(W.random_state(rng, prob, images=5))
+    out = []
+    for mode in (FP32_STEPS_FUSED, FP32_STEPS_PASSES):
+        b = StringBatch(probs, [5, 5], "fp32", line_polynomial=1, fp32_steps=mode)
+        for i, st in enumerate(sts):
+            b.set_string_state(i, st)
+        for k in (3, 4, 1):
+            b.nlcg_steps(k)
+        out.append([(b.string_scalars(i)["fenergy"], b.get_string_state(i).psi_1, b.get_string_state(i).a)
+                    for i in range(2)])
+    for (e0, p0, a0), (e1, p1, a1) in zip(*out):
+        np.testing.assert_array_equal(e0, e1)
+        np.testing.assert_array_equal(p0, p1)
+        np.testing.assert_array_equal(a0, a1)
+
+
 def test_graph_and_direct_launches_agree():
     prob, st = _case(0)
     a = make(prob, st, use_graphs=1)
