@@ -35,9 +35,9 @@ TUNING = os.path.join(PKG, "tuning.json")
 # gradient and the direction pass (register budget 65536 / (32 x blocks)),
 # row loop unrolled by the window period, unit-weight path for interior
 # sites, packed FP32x2 stencils for two components, all steps of a call in
-# one fused persistent launch, and its blocks per SM.
-STRIP = [(32, 16, 16, 0, 0, 1, 0, 16), (32, 16, 16, 0, 0, 1, 1, 12), (32, 16, 16, 0, 0, 1, 1, 16),
-         (16, 16, 16, 0, 0, 1, 1, 12), (32, 16, 16, 0, 0, 1, 1, 10)]
+# one fused persistent launch, and its blocks per SM or explicit register cap.
+STRIP = [(32, 16, 16, 0, 0, 1, 1, 12, 0), (32, 16, 16, 0, 0, 1, 1, 16, 152), (32, 16, 16, 0, 0, 1, 1, 16, 144),
+         (32, 16, 16, 0, 0, 1, 1, 16, 128), (32, 16, 16, 0, 0, 1, 0, 16, 0)]
 # Tile candidates: rows per FP32 tile, min blocks per SM for the gradient
 # pass, for the direction pass, gradient-pass halo copy (0 through
 # registers, 1 cp.async), direction pass (0 fused, 1 split into a pointwise
@@ -46,7 +46,7 @@ STRIP = [(32, 16, 16, 0, 0, 1, 0, 16), (32, 16, 16, 0, 0, 1, 1, 12), (32, 16, 16
 TILE = [(16, 4, 4, 0, 0, 0)]
 CANDIDATES = [dict(MEPGL_STRIP=1, MEPGL_ROWS_F32=r, MEPGL_MINB_STRIP_GRAD=mg, MEPGL_MINB_STRIP_DIR=md,
                    MEPGL_STRIP_UNROLL=u, MEPGL_STRIP_INTERIOR=i, MEPGL_STRIP_PAIR=pk, MEPGL_STRIP_FUSED=fu,
-                   MEPGL_MINB_STRIP_FUSED=mf) for r, mg, md, u, i, pk, fu, mf in STRIP] + [
+                   MEPGL_MINB_STRIP_FUSED=mf, MEPGL_MAXREG_FUSED=mr) for r, mg, md, u, i, pk, fu, mf, mr in STRIP] + [
     dict(MEPGL_STRIP=0, MEPGL_ROWS_F32=r, MEPGL_MINB_GRAD=g, MEPGL_MINB_DIR=d, MEPGL_GRAD_ASYNC=a,
          MEPGL_SPLIT_DIR=sp, MEPGL_DIR_ASYNC=da) for r, g, d, a, sp, da in TILE]
 

@@ -94,6 +94,10 @@ namespace mepgl {
 #ifndef MEPGL_MINB_STRIP_FUSED
 #define MEPGL_MINB_STRIP_FUSED MEPGL_MINB_STRIP
 #endif
+// explicit register cap of the fused kernel (0: from MEPGL_MINB_STRIP_FUSED)
+#ifndef MEPGL_MAXREG_FUSED
+#define MEPGL_MAXREG_FUSED 0
+#endif
 // fused steps only for batches of at most this many waves of the pass kernels
 // (beyond that the boundaries cost little and the pass kernels hold more warps)
 #ifndef MEPGL_FUSE_WAVES

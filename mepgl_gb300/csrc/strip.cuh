@@ -671,8 +671,16 @@ __device__ __forceinline__ void publish_stage(unsigned *stage, unsigned value)
     __syncwarp();
 }
 
+// Register budget of the fused kernel: an explicit cap, or the one
+// resident-block target implies.
+#if MEPGL_MAXREG_FUSED
+#define MEPGL_FUSED_BOUNDS __maxnreg__(MEPGL_MAXREG_FUSED)
+#else
+#define MEPGL_FUSED_BOUNDS __launch_bounds__(NTS, MEPGL_MINB_STRIP_FUSED)
+#endif
+
 template <class T, int NC>
-__global__ void __launch_bounds__(NTS, MEPGL_MINB_STRIP_FUSED) k_nlcg_s(const __grid_constant__ Batch bt, int tile0,
+__global__ void MEPGL_FUSED_BOUNDS k_nlcg_s(const __grid_constant__ Batch bt, int tile0,
                                                                         int n_tiles, int steps, StepPlan plan,
                                                                         Scalars sc, unsigned long long *queue,
                                                                         unsigned *stage)
