@@ -1,11 +1,13 @@
-// strip.cuh -- the two NLCG passes as warp strips (FP32 fields).  Included
-// by kernels.cu inside its anonymous namespace, after the tile kernels,
-// whose helpers (part_slot, h_site, line search) it uses.
+// strip.cuh -- the two NLCG passes as warp strips (FP32 fields), launched
+// as two pass kernels per step or as one fused persistent launch per call
+// (end of file).  Included by kernels.cu inside its anonymous namespace,
+// after the tile kernels, whose helpers (part_slot, h_site, line search) it
+// uses.
 //
-// A block is one warp and owns one tile of the usual tiling (TX = 32
-// columns x TYT rows of one image), so everything that depends on the tile
-// (pointers, parameters, row numbers) is uniform over the block and can live
-// in uniform registers.  Lane l holds column i0 + l and walks down the
+// A block is one warp.  In the pass kernels it owns one tile of the usual
+// tiling (TX = 32 columns x TYT rows of one image); in the fused kernel it
+// takes tiles from a work queue.  Everything that depends on the tile
+// (pointers, parameters, row numbers) is uniform over the block.  Lane l holds column i0 + l and walks down the
 // tile's rows with a three-row window of its column in registers; the
 // x-neighbours come from the adjacent lanes by shuffles.  Lanes 0 and 31
 // copy the halo column next to them (i0 - 1, i0 + 32) into a three-row ring
@@ -36,7 +38,6 @@ __device__ __forceinline__ void transpose_pair(V &a, V &b)
     b.x = p.y;
     b.y = q.y;
 }
-
 
 constexpr unsigned FULL_MASK = 0xffffffffu;
 
@@ -680,10 +681,8 @@ __device__ __forceinline__ void publish_stage(unsigned *stage, unsigned value)
 #endif
 
 template <class T, int NC>
-__global__ void MEPGL_FUSED_BOUNDS k_nlcg_s(const __grid_constant__ Batch bt, int tile0,
-                                                                        int n_tiles, int steps, StepPlan plan,
-                                                                        Scalars sc, unsigned long long *queue,
-                                                                        unsigned *stage)
+__global__ void MEPGL_FUSED_BOUNDS k_nlcg_s(const __grid_constant__ Batch bt, int tile0, int n_tiles, int steps,
+                                            StepPlan plan, Scalars sc, unsigned long long *queue, unsigned *stage)
 {
     __shared__ __align__(16) GradRing<T, NC> gring;
     __shared__ __align__(16) DirRing<T, NC> dring;
