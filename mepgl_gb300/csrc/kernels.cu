@@ -106,16 +106,24 @@ namespace mepgl {
 #if MEPGL_STRIP && MEPGL_SPLIT_DIR
 #error "MEPGL_SPLIT_DIR applies to the tile kernels; build it with MEPGL_STRIP=0"
 #endif
+// paired FP64 passes of two-component strings in packed float-float arithmetic
+#ifndef MEPGL_FF_PAIR
+#define MEPGL_FF_PAIR 1
+#endif
 #ifndef MEPGL_MINB_GRAD_FF
 #define MEPGL_MINB_GRAD_FF 4
 #endif
 #ifndef MEPGL_MINB_DIR_FF
-#define MEPGL_MINB_DIR_FF 4
+#define MEPGL_MINB_DIR_FF 2
 #endif
 template <class T> struct MinBlocks { static constexpr int grad = MEPGL_MINB_GRAD, dir = MEPGL_MINB_DIR; };
 template <> struct MinBlocks<ff> { static constexpr int grad = MEPGL_MINB_GRAD_FF, dir = MEPGL_MINB_DIR_FF; };
 
 template <class T> struct TileRows { static constexpr int v = sizeof(T) == 4 ? MEPGL_ROWS_F32 : MEPGL_ROWS_F64; };
+// Two-component float-float NLCG passes run the packed stencils (site_pair.cuh).
+template <class T, int NC> struct FFPacked {
+    static constexpr bool v = MEPGL_FF_PAIR && NC == 2 && std::is_same<T, ff>::value;
+};
 template <> struct TileRows<ff> { static constexpr int v = MEPGL_ROWS_F64; };
 
 int nlcg_step_launches() { return 2 + MEPGL_SPLIT_DIR; }
@@ -508,7 +516,14 @@ __global__ void __launch_bounds__(NT, MinBlocks<T>::grad) k_grad(const __grid_co
                     hd = h_site(S, p, gj > 0 ? s - S.nx : s);
                 }
                 T g[2 + 2 * NC];
-                site_gradient<T, NC, TYT>(t, lx + 1, ly + 1, p, w, hr, hl, hu, hd, f.maxwell, S.thin_film, g);
+                if constexpr (FFPacked<T, NC>::v) {
+                    PairParams<T> pp;
+                    pp.set(p);
+                    site_gradient_pair<T>(pair_view_tile(t, lx + 1, ly + 1), p, pp, w, hr, hl, hu, hd, f.maxwell,
+                                          S.thin_film, g);
+                } else {
+                    site_gradient<T, NC, TYT>(t, lx + 1, ly + 1, p, w, hr, hl, hu, hd, f.maxwell, S.thin_film, g);
+                }
 #pragma unroll
                 for (int c = 0; c < 1 + NC; ++c) {
                     V gv;
@@ -633,7 +648,14 @@ __global__ void __launch_bounds__(NT, MinBlocks<T>::dir) k_dir_poly(const __grid
                 w.load(tx.m[ly + 1][lx + 1]);
                 if (S.per_site) p.load_site(S, gi + S.nx * gj, NC);
                 T o[5];
-                site_poly<T, NC, TYT>(tx, td, lx + 1, ly + 1, p, w, f.poly_compat, S.thin_film, o);
+                if constexpr (FFPacked<T, NC>::v) {
+                    PairParams<T> pp;
+                    pp.set(p);
+                    site_poly_pair<T>(pair_view_tile(tx, lx + 1, ly + 1), pair_view_tile(td, lx + 1, ly + 1), p, pp,
+                                      w, f.poly_compat, S.thin_film, o);
+                } else {
+                    site_poly<T, NC, TYT>(tx, td, lx + 1, ly + 1, p, w, f.poly_compat, S.thin_film, o);
+                }
 #pragma unroll
                 for (int k = 0; k < 5; ++k) v[k] += o[k];
             }

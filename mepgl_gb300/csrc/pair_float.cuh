@@ -100,6 +100,56 @@ __device__ __forceinline__ ff shfl_down(ff v, int o)
     return ff(__shfl_down_sync(0xffffffffu, v.hi, o), __shfl_down_sync(0xffffffffu, v.lo, o));
 }
 
+// ------------------------------------------------ packed pairs of float-floats
+// Two independent float-float numbers (one per lane of an FP32x2 register
+// pair: the two components of a two-component string), hi = (hi_0, hi_1),
+// lo = (lo_0, lo_1).  Every operation is the scalar one above, lane by lane,
+// on the packed FP32x2 instructions (same rounding, half the instructions).
+struct ffp {
+    float2 hi, lo;
+};
+
+__device__ __forceinline__ float2 neg2f(float2 a) { return make_float2(-a.x, -a.y); }
+__device__ __forceinline__ float2 addf2(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 subf2(float2 a, float2 b) { return __fadd2_rn(a, neg2f(b)); }
+
+__device__ __forceinline__ ffp two_sum(float2 a, float2 b)
+{
+    const float2 s = addf2(a, b);
+    const float2 bb = subf2(s, a);
+    return ffp{s, addf2(subf2(a, subf2(s, bb)), subf2(b, bb))};
+}
+
+__device__ __forceinline__ ffp fast_two_sum(float2 a, float2 b)
+{
+    const float2 s = addf2(a, b);
+    return ffp{s, subf2(b, subf2(s, a))};
+}
+
+__device__ __forceinline__ ffp operator+(ffp a, ffp b)
+{
+    const ffp s = two_sum(a.hi, b.hi);
+#if MEPGL_FF_ACCURATE_ADD
+    const ffp t = two_sum(a.lo, b.lo);
+    const ffp u = fast_two_sum(s.hi, addf2(s.lo, t.hi));
+    return fast_two_sum(u.hi, addf2(u.lo, t.lo));
+#else
+    return fast_two_sum(s.hi, addf2(s.lo, addf2(a.lo, b.lo)));
+#endif
+}
+
+__device__ __forceinline__ ffp operator-(ffp a) { return ffp{neg2f(a.hi), neg2f(a.lo)}; }
+__device__ __forceinline__ ffp operator-(ffp a, ffp b) { return a + (-b); }
+
+__device__ __forceinline__ ffp operator*(ffp a, ffp b)
+{
+    const float2 p = __fmul2_rn(a.hi, b.hi);
+    float2 e = __ffma2_rn(a.hi, b.hi, neg2f(p));   // exact error of the products
+    e = __ffma2_rn(a.hi, b.lo, e);
+    e = __ffma2_rn(a.lo, b.hi, e);
+    return fast_two_sum(p, e);
+}
+
 // double <-> float-float at the memory boundary (two and three FP64-pipe
 // operations; integer-only splitting was measured slower on GB300, where
 // these kernels are bound by instruction issue rather than by the FP64 pipe)

@@ -65,9 +65,9 @@ struct RegView {
 // Packed view of a register window (PairView) from a RegView of the same
 // site whose psi slots already hold the packed pairs.
 template <class T, int NC>
-__device__ __forceinline__ PairView pair_view(const RegView<T, NC> &r)
+__device__ __forceinline__ PairView<T> pair_view(const RegView<T, NC> &r)
 {
-    PairView v;
+    PairView<T> v;
 #pragma unroll
     for (int y = 0; y < 3; ++y)
 #pragma unroll
@@ -367,9 +367,9 @@ __device__ __forceinline__ bool grad_tile(const Batch &bt, const TileRef tr, con
             Wts<T> w;
             if constexpr (StripPacked<T, NC>::v) {
                 w.load(R0.m);
-                PairParams pp;
+                PairParams<T> pp;
                 pp.set(p);
-                site_gradient_pair(pair_view(w3), p, pp, w, hr, hl, hu, hd, f.maxwell, S.thin_film, g);
+                site_gradient_pair<T>(pair_view(w3), p, pp, w, hr, hl, hu, hd, f.maxwell, S.thin_film, g);
             } else if (MEPGL_STRIP_INTERIOR && R0.m == 0xffffu) {   // interior site: unit weights, folded in
                 w.interior();
                 site_gradient_v<T, NC>(w3, p, w, hr, hl, hu, hd, f.maxwell, S.thin_film, g);
@@ -552,9 +552,9 @@ __device__ __forceinline__ bool dir_tile(const Batch &bt, const TileRef tr, cons
             Wts<T> w;
             if constexpr (StripPacked<T, NC>::v) {
                 w.load(R0.m);
-                PairParams pp;
+                PairParams<T> pp;
                 pp.set(p);
-                site_poly_pair(pair_view(vx), pair_view(vd), p, pp, w, f.poly_compat, S.thin_film, o);
+                site_poly_pair<T>(pair_view(vx), pair_view(vd), p, pp, w, f.poly_compat, S.thin_film, o);
             } else if (MEPGL_STRIP_INTERIOR && R0.m == 0xffffu) {   // interior site: unit weights, folded in
                 w.interior();
                 site_poly_v<T, NC>(vx, vd, p, w, f.poly_compat, S.thin_film, o);
