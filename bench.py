@@ -154,6 +154,30 @@ def cpu_oracle_step_rate(prob, st, images: int, steps: int, dtype, budget_s: flo
     return units / dt, dict(steps=done, images=images, seconds=dt, threads=cref.threads())
 
 
+def host_cpu():
+    """CPU model and logical core count of this host (for the CPU baseline)."""
+    model = None
+    try:
+        with open("/proc/cpuinfo") as f:
+            for line in f:
+                key = line.split(":")[0].strip().lower()
+                if key in ("model name", "cpu model", "hardware") and ":" in line:
+                    model = line.split(":", 1)[1].strip()
+                    break
+    except OSError:
+        pass
+    if not model:
+        try:
+            out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+            model = next((l.split(":", 1)[1].strip() for l in out.splitlines() if l.startswith("Model name")), None)
+        except (OSError, subprocess.SubprocessError):
+            model = None
+    if not model:
+        import platform
+        model = platform.machine()
+    return {"model": model, "logical_cores": os.cpu_count()}
+
+
 def run_reference(args):
     """--impl reference: the CPU implementation (C oracle, all host threads)."""
     world, rank, _ = dist_env()
@@ -183,7 +207,8 @@ def run_reference(args):
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": WORKLOAD, "sites": prob.nx * prob.ny, "images": 64, "components": 2,
                    "cache": "inputs larger than L2"},
-        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cref.threads(), "kind": "port", "sample": sample},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cref.threads(), "kind": "port", "sample": sample,
+                         "host": host_cpu()},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -316,21 +341,30 @@ def run_ours(args):
     # The barrier estimate of the string method does not converge to 1e-6 on
     # these workloads (its value drifts with the reparametrization cadence), so
     # this reports the time until the end-state energy difference F_{F-1} - F_0
-    # (which does converge) stays within 1e-6 of the FP64 run's final value, on
-    # the small single-component string (64x64, 16 images, 50 steps per
-    # reparametrization).  The 256x256 timings are in barrier.py runs.
+    # (which does converge) stays within 1e-6 of the FP64 run's final value.
+    # Default: the small single-component string (64x64, 16 images, 50 steps per
+    # reparametrization; latency-bound, seconds).  --ttb-config 2: the 256x256
+    # two-component string (100 steps per reparametrization; several minutes),
+    # against the value its long FP64 run converges to, with paired-FP64 polish.
     ttb = None
     if rank == 0 and not args.no_ttb:
         from mepgl_gb300 import barrier as B
-        r64, _ = B.run(1, 50, 150, "fp64")
-        rmx, _ = B.run(1, 50, 150, "mixed", -1)
-        target = r64[-1][3]
+        if args.ttb_config == 2:
+            target = 1.00779044   # F_{F-1} - F_0 after 600 outer iterations of FP64 (IEEE) relaxation
+            r64, _ = B.run(2, 100, 160, "fp64")
+            rmx, _ = B.run(2, 100, 250, "mixed", -1, fp64_arith="paired")
+            work = "two-component GL 256x256 dx=0.4, 64 images, mode L, 100 NLCG steps per iteration"
+        else:
+            r64, _ = B.run(1, 50, 150, "fp64")
+            rmx, _ = B.run(1, 50, 150, "mixed", -1)
+            target = r64[-1][3]
+            work = "single-component GL 64x64 dx=0.5, 16 images, mode L, 50 NLCG steps per iteration"
 
         def t_to(rec):
             return B.time_within([x[0] for x in rec], [x[3] for x in rec], target, 1e-6)
-        ttb = {"quantity": "F_end - F_0 within 1e-6 of the FP64 run's final value",
-               "workload": "single-component GL 64x64 dx=0.5, 16 images, mode L, 50 NLCG steps per iteration",
-               "fp64_s": t_to(r64), "mixed_s": t_to(rmx),
+        ttb = {"quantity": "F_end - F_0 within 1e-6 of the converged FP64 value",
+               "workload": work, "target": target, "fp64_s": t_to(r64), "mixed_s": t_to(rmx),
+               "mixed_polish": "paired FP64" if args.ttb_config == 2 else "IEEE FP64",
                "mixed_fp32_iterations": sum(1 for x in rmx if x[4] == "fp32"),
                "barrier_fp64": r64[-1][1], "barrier_mixed": rmx[-1][1]}
 
@@ -338,7 +372,7 @@ def run_ours(args):
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
         rate, info = cpu_oracle_step_rate(prob, st, images=16, steps=2, dtype=np.float32)
-        cpu = {"value": rate, "unit": UNIT, "cores": info["threads"], "kind": "port",
+        cpu = {"value": rate, "unit": UNIT, "cores": info["threads"], "kind": "port", "host": host_cpu(),
                "sample": f"{info['steps']} NLCG steps on {info['images']} of 64 images of the workload "
                          f"({info['seconds']:.1f} s), C oracle in FP32, OpenMP over images"}
 
@@ -368,6 +402,8 @@ def main(argv=None):
     ap.add_argument("--impl", choices=("ours", "reference"), default="ours")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-ttb", action="store_true", help="skip the time-to-converged-end-state leg")
+    ap.add_argument("--ttb-config", type=int, choices=(1, 2), default=1,
+                    help="workload of that leg: 1 (64x64, seconds) or 2 (256x256, several minutes)")
     args = ap.parse_args(argv)
     if args.impl == "reference":
         return run_reference(args)
