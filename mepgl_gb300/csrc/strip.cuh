@@ -286,18 +286,18 @@ __device__ __forceinline__ bool grad_tile(const Batch &bt, const TileRef tr, con
     V rc[3][1 + NC];
     uint16_t rm;
     // raw row j -> window row (x + alpha d; left / right A by shuffles)
-    auto take = [&](GradRow<T, NC> &R, int j, V (&hp)[NC]) {
-        cp_async_wait_groups<0>();   // row j's halo is the newest group
+    auto take = [&](GradRow<T, NC> &R, int j, V (&hp)[NC], const V (&raw)[3][1 + NC], uint16_t m) {
+        cp_async_wait_groups<0>();   // row j's halo is in the newest groups
         const V(&h)[2][1 + NC] = ring[(j + 3) % 3][L.lane == 0 ? 0 : 1];
         V hx[1 + NC];
 #pragma unroll
         for (int c = 0; c < 1 + NC; ++c) {
-            R.x[c].x = rc[0][c].x + alpha * rc[1][c].x;
-            R.x[c].y = rc[0][c].y + alpha * rc[1][c].y;
+            R.x[c].x = raw[0][c].x + alpha * raw[1][c].x;
+            R.x[c].y = raw[0][c].y + alpha * raw[1][c].y;
             const V hv = h[0][c], hd = fields & 2u ? h[1][c] : zero2<T>();
             hx[c].x = hv.x + alpha * hd.x;
             hx[c].y = hv.y + alpha * hd.y;
-            R.gold[c] = rc[2][c];
+            R.gold[c] = raw[2][c];
         }
         if constexpr (StripPacked<T, NC>::v) {
             transpose_pair(R.x[1], R.x[NC]);
@@ -307,20 +307,24 @@ __device__ __forceinline__ bool grad_tile(const Batch &bt, const TileRef tr, con
         R.ar = from_right<T>(R.x[0], hx[0], L.lane);
 #pragma unroll
         for (int c = 0; c < NC; ++c) hp[c] = hx[1 + c];
-        R.m = rm;
+        R.m = m;
     };
-    auto load = [&](int j, bool gold) {
-        strip_load<T, NC, 3>(rc, src, S, L, j, gold ? fields | 4u : fields);
+    auto load = [&](V (&raw)[3][1 + NC], uint16_t &m, int j, bool gold) {
+        strip_load<T, NC, 3>(raw, src, S, L, j, gold ? fields | 4u : fields);
         strip_halo<T, NC, 2, 3>(ring[(j + 3) % 3], src, S, L, j, fields, true);
-        rm = strip_code(S, L, j);
+        m = strip_code(S, L, j);
     };
     GradRow<T, NC> Rm, R0, Rp;
     V hp0[NC], hp1[NC];
-    load(j0 - 1, false);
-    take(Rm, j0 - 1, hp0);
-    load(j0, true);
-    take(R0, j0, hp0);
-    load(j0 + 1, true);
+    {   // the first three rows are loaded together: one memory latency, not three
+        V ra[3][1 + NC], rb[3][1 + NC];
+        uint16_t ma, mb;
+        load(ra, ma, j0 - 1, false);
+        load(rb, mb, j0, true);
+        load(rc, rm, j0 + 1, true);
+        take(Rm, j0 - 1, hp0, ra, ma);
+        take(R0, j0, hp0, rb, mb);
+    }
     const int rows = S.ny - j0 < TYT ? S.ny - j0 : TYT;
     T v[2] = {(T)0, (T)0};
 #if MEPGL_STRIP_UNROLL
@@ -330,8 +334,8 @@ __device__ __forceinline__ bool grad_tile(const Batch &bt, const TileRef tr, con
 #endif
     for (int r = 0; r < rows; ++r) {
         const int j = j0 + r;
-        take(Rp, j + 1, hp1);
-        if (r + 1 < rows) load(j + 2, true);
+        take(Rp, j + 1, hp1, rc, rm);
+        if (r + 1 < rows) load(rc, rm, j + 2, true);
         const int s = L.gi + S.nx * j;
         if (L.cok) {
             V o[1 + NC];
@@ -461,33 +465,37 @@ __device__ __forceinline__ bool dir_tile(const Batch &bt, const TileRef tr, cons
     p.load_uniform(S);
     V rc[3][1 + NC];
     uint16_t rm;
-    auto take = [&](DirRow<T, NC> &R) {
+    auto take = [&](DirRow<T, NC> &R, const V (&raw)[3][1 + NC], uint16_t m) {
 #pragma unroll
         for (int c = 0; c < 1 + NC; ++c) {
-            R.x[c] = rc[0][c];
-            R.d[c].x = -rc[1][c].x + beta * rc[2][c].x;
-            R.d[c].y = -rc[1][c].y + beta * rc[2][c].y;
+            R.x[c] = raw[0][c];
+            R.d[c].x = -raw[1][c].x + beta * raw[2][c].x;
+            R.d[c].y = -raw[1][c].y + beta * raw[2][c].y;
         }
         if constexpr (StripPacked<T, NC>::v) {
             transpose_pair(R.x[1], R.x[NC]);
             transpose_pair(R.d[1], R.d[NC]);
         }
-        R.m = rm;
+        R.m = m;
     };
-    auto load = [&](int j, bool issue) {
-        strip_load<T, NC, 3>(rc, src, S, L, j, issue ? 7u : 0u);
+    auto load = [&](V (&raw)[3][1 + NC], uint16_t &m, int j, bool issue) {
+        strip_load<T, NC, 3>(raw, src, S, L, j, issue ? 7u : 0u);
         strip_halo<T, NC, 3, 3>(ring[(j + 3) % 3], src, S, L, j, 7u, issue);
-        rm = strip_code(S, L, j);
+        m = strip_code(S, L, j);
     };
     DirRow<T, NC> R0, Rp;
     T xm_ax, dm_ax;   // row j - 1: only A_x of x and of d is read
-    load(j0 - 1, true);
-    take(R0);
-    xm_ax = R0.x[0].x;
-    dm_ax = R0.d[0].x;
-    load(j0, true);
-    take(R0);
-    load(j0 + 1, true);
+    {   // the first three rows are loaded together: one memory latency, not three
+        V ra[3][1 + NC], rb[3][1 + NC];
+        uint16_t ma, mb;
+        load(ra, ma, j0 - 1, true);
+        load(rb, mb, j0, true);
+        load(rc, rm, j0 + 1, true);
+        take(R0, ra, ma);
+        xm_ax = R0.x[0].x;
+        dm_ax = R0.d[0].x;
+        take(R0, rb, mb);
+    }
     const int rows = S.ny - j0 < TYT ? S.ny - j0 : TYT;
     T v[5] = {(T)0, (T)0, (T)0, (T)0, (T)0};
 #if MEPGL_STRIP_UNROLL
@@ -497,8 +505,8 @@ __device__ __forceinline__ bool dir_tile(const Batch &bt, const TileRef tr, cons
 #endif
     for (int r = 0; r < rows; ++r) {
         const int j = j0 + r;
-        take(Rp);
-        if (r + 1 < rows) load(j + 2, true);
+        take(Rp, rc, rm);
+        if (r + 1 < rows) load(rc, rm, j + 2, true);
         else strip_halo<T, NC, 3, 3>(ring[0], src, S, L, j + 2, 0u, false);
         cp_async_wait_groups<2>();   // groups of rows j + 1 and j + 2 may still be pending
         const int s = L.gi + S.nx * j;
@@ -569,6 +577,9 @@ __device__ __forceinline__ bool dir_tile(const Batch &bt, const TileRef tr, cons
         dm_ax = R0.d[0].x;
         R0 = Rp;
     }
+    // the halo copy of the row below the tile may still be in flight: complete it before the
+    // ring can be reused (the fused kernel runs more tiles in the same block)
+    cp_async_wait_groups<0>();
     const int tpi = S.tiles_x * S.tiles_y;
     double tot[5];
     __threadfence();
