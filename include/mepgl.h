@@ -283,6 +283,15 @@ mepgl_status mepgl_profile_passes(mepgl_ctx *ctx, int steps, int use_cg, double 
  * counterpart; labels timings and profiler captures. */
 mepgl_status mepgl_pass_kernels(const mepgl_ctx *ctx, const char **grad, const char **dir_poly, const char **fused);
 
+/* Self-test of the fused launch's bounded waits: one fused launch whose work
+ * queue starts after the gradient items of its step, so every direction item
+ * waits for an image stage that nothing sets, gives up after a short poll
+ * limit and sets the device status flag.  *timed_out = 1 when the flag was
+ * set (then cleared).  The launch writes no field or scalar, so the context
+ * continues as before.  FP32 contexts of a build with fused steps; no
+ * reference counterpart. */
+mepgl_status mepgl_fused_wait_selftest(mepgl_ctx *ctx, int *timed_out);
+
 /* Allocation-free free energy.  No counterpart in the reference.  For callers
  * that cannot allocate device memory -- code running inside someone else's
  * CUDA-graph capture or memory pool, or an embedding that owns a fixed

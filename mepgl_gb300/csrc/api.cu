@@ -1226,6 +1226,25 @@ mepgl_status mepgl_pass_kernels(const mepgl_ctx *c, const char **grad, const cha
     return MEPGL_OK;
 }
 
+mepgl_status mepgl_fused_wait_selftest(mepgl_ctx *c, int *timed_out)
+{
+    if (!c || !timed_out) return MEPGL_ERR_INVALID_ARG;
+    if (!nlcg_fused(c->precision))
+        return fail(c, MEPGL_ERR_UNSUPPORTED, "mepgl_fused_wait_selftest: needs an FP32 context and fused steps");
+    mepgl_status st = flush(c);
+    if (st != MEPGL_OK) return st;
+    const Launch L = make_launch(c, 0);
+    CK(c, launch_nlcg_fused(L, c->sc, step_flags(c, 1, 1, 0), 1, 1, c->fqueue, c->fstage, c->total_images,
+                            (unsigned long long)L.n_tiles, 4096u));
+    c->launches += 1;
+    int flag = 0;
+    CK(c, cudaMemcpyAsync(&flag, c->sc.status, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+    CK(c, cudaStreamSynchronize(c->stream));
+    if (flag) CK(c, cudaMemsetAsync(c->sc.status, 0, sizeof(int), c->stream));
+    *timed_out = flag ? 1 : 0;
+    return MEPGL_OK;
+}
+
 mepgl_status mepgl_profile_passes(mepgl_ctx *c, int steps, int use_cg, double *ms_grad, double *ms_dir_poly)
 {
     if (c && c->opt.discretization == MEPGL_DISC_LINK)

@@ -1385,7 +1385,8 @@ int strip_pass_slots(int ncomp)
 }
 
 cudaError_t launch_nlcg_fused(const Launch &L, const Scalars &sc, const StepFlags &f0, int it0, int steps,
-                              unsigned long long *queue, unsigned *stage, int n_stage)
+                              unsigned long long *queue, unsigned *stage, int n_stage, unsigned long long first_item,
+                              unsigned max_polls)
 {
 #if MEPGL_STRIP
     static int slots[2] = {0, 0};
@@ -1405,16 +1406,23 @@ cudaError_t launch_nlcg_fused(const Launch &L, const Scalars &sc, const StepFlag
     plan.di0 = f0.din;
     plan.it0 = it0;
     plan.base = f0;
-    cudaError_t e = cudaMemsetAsync(queue, 0, sizeof(unsigned long long), L.stream);
+    cudaError_t e = first_item ? cudaMemcpyAsync(queue, &first_item, sizeof(first_item), cudaMemcpyHostToDevice, L.stream)
+                               : cudaMemsetAsync(queue, 0, sizeof(unsigned long long), L.stream);
+    if (e == cudaSuccess && first_item) e = cudaStreamSynchronize(L.stream);   // first_item is a host local
     if (e == cudaSuccess) e = cudaMemsetAsync(stage, 0, sizeof(unsigned) * (size_t)n_stage, L.stream);
     if (e != cudaSuccess) return e;
     const long long items = 2LL * L.n_tiles * steps;
     const int grid = items < slots[ci] ? (int)items : slots[ci];
-    if (ci) k_nlcg_s<float, 2><<<grid, NTS, 0, L.stream>>>(*L.batch, L.tile0, L.n_tiles, steps, plan, sc, queue, stage);
-    else k_nlcg_s<float, 1><<<grid, NTS, 0, L.stream>>>(*L.batch, L.tile0, L.n_tiles, steps, plan, sc, queue, stage);
+    if (ci)
+        k_nlcg_s<float, 2><<<grid, NTS, 0, L.stream>>>(*L.batch, L.tile0, L.n_tiles, steps, plan, sc, queue, stage,
+                                                         max_polls);
+    else
+        k_nlcg_s<float, 1><<<grid, NTS, 0, L.stream>>>(*L.batch, L.tile0, L.n_tiles, steps, plan, sc, queue, stage,
+                                                         max_polls);
     return cudaGetLastError();
 #else
     (void)L; (void)sc; (void)f0; (void)it0; (void)steps; (void)queue; (void)stage; (void)n_stage;
+    (void)first_item; (void)max_polls;
     return cudaErrorNotSupported;
 #endif
 }

@@ -45,8 +45,12 @@ int strip_pass_slots(int ncomp);
 // `steps` NLCG steps (iterations it0, it0 + 1, ...; step 0 with the buffers
 // of f0) of the launch's tiles in one persistent launch; queue (one counter)
 // and stage (one per global image, n_stage) are reset on the stream first.
+// first_item > 0 starts the queue there (the wait self-test); each per-image
+// wait polls at most max_polls times.
+constexpr unsigned STAGE_WAIT_POLLS = 1u << 22;   // about 100 ns to 1 us per poll
 cudaError_t launch_nlcg_fused(const Launch &L, const Scalars &sc, const StepFlags &f0, int it0, int steps,
-                              unsigned long long *queue, unsigned *stage, int n_stage);
+                              unsigned long long *queue, unsigned *stage, int n_stage,
+                              unsigned long long first_item = 0, unsigned max_polls = STAGE_WAIT_POLLS);
 // Pass 1: x <- x + alpha_pend d (into x[xout]); g = dF/dx; |g|^2, g.(g - g_prev);
 // the last tile of each image sets beta.
 cudaError_t launch_grad(const Launch &L, const Scalars &sc, const StepFlags &f);

@@ -647,12 +647,10 @@ struct StepPlan {
     }
 };
 
-constexpr unsigned STAGE_WAIT_POLLS = 1u << 22;   // x about 100 ns per poll
-
 // Lane 0 waits until stage >= need (acquire, then a fence so that the whole
-// warp's later loads see what the finishing block wrote); false if the
-// wait ran out.
-__device__ __forceinline__ bool wait_stage(const unsigned *stage, unsigned need, int *status)
+// warp's later loads see what the finishing block wrote), polling at most
+// max_polls times; false if the wait ran out.
+__device__ __forceinline__ bool wait_stage(const unsigned *stage, unsigned need, unsigned max_polls, int *status)
 {
     int ok = 1;
     if ((threadIdx.x & 31) == 0) {
@@ -660,7 +658,7 @@ __device__ __forceinline__ bool wait_stage(const unsigned *stage, unsigned need,
         for (;;) {
             asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(stage) : "memory");
             if (v >= need) break;
-            if (++polls > STAGE_WAIT_POLLS) {
+            if (++polls > max_polls) {
                 atomicExch(status, 1);
                 ok = 0;
                 break;
@@ -693,7 +691,8 @@ __device__ __forceinline__ void publish_stage(unsigned *stage, unsigned value)
 
 template <class T, int NC>
 __global__ void MEPGL_FUSED_BOUNDS k_nlcg_s(const __grid_constant__ Batch bt, int tile0, int n_tiles, int steps,
-                                            StepPlan plan, Scalars sc, unsigned long long *queue, unsigned *stage)
+                                            StepPlan plan, Scalars sc, unsigned long long *queue, unsigned *stage,
+                                            unsigned max_polls)
 {
     __shared__ __align__(16) GradRing<T, NC> gring;
     __shared__ __align__(16) DirRing<T, NC> dring;
@@ -711,7 +710,7 @@ __global__ void MEPGL_FUSED_BOUNDS k_nlcg_s(const __grid_constant__ Batch bt, in
         const TileRef tr = strip_tile(bt, tile0 + u);
         const int img = bt.s[tr.s].img_base + tr.n;
         const unsigned need = 2u * (unsigned)k + (unsigned)pass;
-        if (need > 0 && !wait_stage(stage + img, need, sc.status)) return;
+        if (need > 0 && !wait_stage(stage + img, need, max_polls, sc.status)) return;
         const StepFlags f = plan.step(k);
         if (pass == 0) {
             if (grad_tile<T, NC>(bt, tr, sc, f, gring)) publish_stage(stage + img, need + 1);

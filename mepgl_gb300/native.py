@@ -94,6 +94,7 @@ _SIGS = {
     "mepgl_synchronize": (C.c_int, [C.c_void_p]),
     "mepgl_profile_passes": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_void_p]),
     "mepgl_pass_kernels": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "mepgl_fused_wait_selftest": (C.c_int, [C.c_void_p, C.c_void_p]),
     "mepgl_free_energy_noalloc": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_double]
                                   + [C.c_void_p] * 11 + [C.c_double] * 5 + [C.c_void_p] * 5),
     "mepgl_noalloc_last_error": (C.c_char_p, []),
@@ -356,6 +357,13 @@ class StringContext:
         g, d, f = C.c_char_p(), C.c_char_p(), C.c_char_p()
         self._check(self.L.mepgl_pass_kernels(self.h, C.byref(g), C.byref(d), C.byref(f)))
         return g.value.decode(), d.value.decode(), f.value.decode()
+
+    def fused_wait_selftest(self) -> bool:
+        """Run the fused launch's bounded-wait self-test; True when its waits
+        ran out and were reported (the expected outcome)."""
+        t = C.c_int()
+        self._check(self.L.mepgl_fused_wait_selftest(self.h, C.byref(t)))
+        return bool(t.value)
 
     def profile_passes(self, steps: int, nlcg: bool = True):
         """Mean milliseconds of (gradient pass, direction/line pass) over `steps` real steps."""

@@ -219,6 +219,25 @@ def test_fused_fp32_steps_equal_pass_kernels(mc):
         np.testing.assert_array_equal(a0, a1)
 
 
+def test_fused_waits_are_bounded_and_reported():
+    """A fused launch whose queue skips the gradient items: every direction
+    item waits for an image stage that nothing sets, gives up after its poll
+    limit and raises the device status flag, which the host reads back.  The
+    context is unharmed: its next steps equal those of a fresh context."""
+    import time
+    from mepgl_gb300.native import FP32_STEPS_FUSED
+    prob, st = W.config2(n=40, images=4)
+    a = make(prob, st, precision="fp32", line_polynomial=1, fp32_steps=FP32_STEPS_FUSED)
+    t0 = time.perf_counter()
+    assert a.fused_wait_selftest()
+    assert time.perf_counter() - t0 < 30.0
+    b = make(prob, st, precision="fp32", line_polynomial=1, fp32_steps=FP32_STEPS_FUSED)
+    a.nlcg_steps(3)
+    b.nlcg_steps(3)
+    np.testing.assert_array_equal(a.image_scalars()["fenergy"], b.image_scalars()["fenergy"])
+    np.testing.assert_array_equal(a.get_state().psi_1, b.get_state().psi_1)
+
+
 def test_graph_and_direct_launches_agree():
     prob, st = _case(0)
     a = make(prob, st, use_graphs=1)
