@@ -58,6 +58,27 @@ template <> __device__ __forceinline__ void store2<ff>(double2 *p, ff2 v)
     *p = make_double2(to_double(v.x), to_double(v.y));
 }
 
+// Storage of the NLCG work arrays (gradient g and direction d): the compute
+// type itself for float and double; float-float pairs in the paired FP64 mode
+// (ff2 fills the same 16 bytes as double2), so the paired passes move them
+// without conversions.  The arrays are internal to the NLCG passes and the
+// pending-step update, and are zeroed (a valid value in every format)
+// whenever the history is reset.
+template <class T> __device__ __forceinline__ vec2_t<T> loadw(const vec2_t<store_t<T>> *p) { return load2<T>(p); }
+template <> __device__ __forceinline__ ff2 loadw<ff>(const double2 *p)
+{
+    const float4 q = *reinterpret_cast<const float4 *>(p);
+    ff2 r;
+    r.x = ff(q.x, q.y);
+    r.y = ff(q.z, q.w);
+    return r;
+}
+template <class T> __device__ __forceinline__ void storew(vec2_t<store_t<T>> *p, vec2_t<T> v) { store2<T>(p, v); }
+template <> __device__ __forceinline__ void storew<ff>(double2 *p, ff2 v)
+{
+    *reinterpret_cast<float4 *>(p) = make_float4(v.x.hi, v.x.lo, v.y.hi, v.y.lo);
+}
+
 // Uniform GL parameters in one precision (hm* = 0.5 / m, aob = a / b).
 template <class T>
 struct Uniform {

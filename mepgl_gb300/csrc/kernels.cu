@@ -170,7 +170,9 @@ struct ImagePtrs {                  // storage type (double for float-float)
 // stores them.  Out-of-lattice elements are zero.
 // mode 0: x = in;  mode 1: x = in + alpha * aux (and interior x -> out);
 // mode 2: x = -aux + beta * in, i.e. the new direction (interior -> out).
-template <class T, int NC, int TYT, int MODE>
+// IN_WORK / AUX_WORK: in (and out) / aux are NLCG work arrays (g, d) rather
+// than fields.
+template <class T, int NC, int TYT, int MODE, bool IN_WORK = false, bool AUX_WORK = false>
 __device__ __forceinline__ void stage(Tile<T, NC, TYT> &t, const StringDesc &S, const ImagePtrs<T, NC> &ip, int i0,
                                       int j0, T coef, bool write_out, bool masks)
 {
@@ -197,10 +199,11 @@ __device__ __forceinline__ void stage(Tile<T, NC, TYT> &t, const StringDesc &S, 
         if (ok[k]) {
             const int s = sidx[k];
 #pragma unroll
-            for (int c = 0; c < 1 + NC; ++c) f[k][c] = load2<T>(ip.in[c] + s);
+            for (int c = 0; c < 1 + NC; ++c) f[k][c] = IN_WORK ? loadw<T>(ip.in[c] + s) : load2<T>(ip.in[c] + s);
             if (aux)
 #pragma unroll
-                for (int c = 0; c < 1 + NC; ++c) a[k][c] = load2<T>(ip.aux[c] + s);
+                for (int c = 0; c < 1 + NC; ++c)
+                    a[k][c] = AUX_WORK ? loadw<T>(ip.aux[c] + s) : load2<T>(ip.aux[c] + s);
             if (masks)
                 m[k] = S.mask ? S.mask[s]
                               : (uint16_t)((S.code_comp[s] & 0xff) | ((S.code_sc[s] & 0xff) << 8));
@@ -226,7 +229,10 @@ __device__ __forceinline__ void stage(Tile<T, NC, TYT> &t, const StringDesc &S, 
         }
         if (write_out && ok[k] && hx >= 1 && hx <= TX && hy >= 1 && hy <= TYT)
 #pragma unroll
-            for (int c = 0; c < 1 + NC; ++c) store2<T>(ip.out[c] + sidx[k], v[c]);
+            for (int c = 0; c < 1 + NC; ++c) {
+                if (IN_WORK) storew<T>(ip.out[c] + sidx[k], v[c]);
+                else store2<T>(ip.out[c] + sidx[k], v[c]);
+            }
         t.A[hy][hx] = v[0];
 #pragma unroll
         for (int c = 0; c < NC; ++c) t.P[c][hy][hx] = v[1 + c];
@@ -434,7 +440,7 @@ __global__ void __launch_bounds__(NT, MinBlocks<T>::grad) k_grad(const __grid_co
         image_ptrs<T, NC>(ip, S.x[f.xin], S.d[f.din], S.x[f.xout], off);
 #if MEPGL_GRAD_ASYNC
         if constexpr (std::is_same<T, ff>::value) {
-            stage<T, NC, TYT, 1>(t, S, ip, i0, j0, (T)sc.alpha_pend[img], true, true);
+            stage<T, NC, TYT, 1, false, true>(t, S, ip, i0, j0, (T)sc.alpha_pend[img], true, true);
         } else {
             constexpr int HW = TX + 2, HE = (TYT + 2) * HW, NI = (HE + NT - 1) / NT;
             const T alpha = (T)sc.alpha_pend[img];
@@ -474,7 +480,7 @@ __global__ void __launch_bounds__(NT, MinBlocks<T>::grad) k_grad(const __grid_co
             }
         }
 #else
-        stage<T, NC, TYT, 1>(t, S, ip, i0, j0, (T)sc.alpha_pend[img], true, true);
+        stage<T, NC, TYT, 1, false, true>(t, S, ip, i0, j0, (T)sc.alpha_pend[img], true, true);
 #endif
         using W = vec2_t<store_t<T>>;
         W *gcur[1 + NC];
@@ -497,7 +503,7 @@ __global__ void __launch_bounds__(NT, MinBlocks<T>::grad) k_grad(const __grid_co
 #pragma unroll
             for (int c = 0; c < 1 + NC; ++c) {
                 gold[r][c].x = gold[r][c].y = (T)0;
-                if (gi < S.nx && gj < S.ny) gold[r][c] = load2<T>(gprev[c] + gi + S.nx * gj);
+                if (gi < S.nx && gj < S.ny) gold[r][c] = loadw<T>(gprev[c] + gi + S.nx * gj);
             }
         }
 #pragma unroll
@@ -529,7 +535,7 @@ __global__ void __launch_bounds__(NT, MinBlocks<T>::grad) k_grad(const __grid_co
                     V gv;
                     gv.x = g[2 * c];
                     gv.y = g[2 * c + 1];
-                    store2<T>(gcur[c] + s, gv);
+                    storew<T>(gcur[c] + s, gv);
                     const V go = gold[r][c];
                     v[0] += gv.x * gv.x + gv.y * gv.y;
                     v[1] += gv.x * (gv.x - go.x) + gv.y * (gv.y - go.y);
@@ -580,9 +586,9 @@ __global__ void __launch_bounds__(NT, MinBlocks<T>::dir) k_dir_poly(const __grid
 #if MEPGL_SPLIT_DIR
             ImagePtrs<T, NC> ipn;
             image_ptrs<T, NC>(ipn, S.d[f.dout], nullptr, nullptr, off);
-            stage<T, NC, TYT, 0>(td, S, ipn, i0, j0, (T)0, false, false);
+            stage<T, NC, TYT, 0, true>(td, S, ipn, i0, j0, (T)0, false, false);
 #else
-            stage<T, NC, TYT, 2>(td, S, ipd, i0, j0, (T)sc.beta[img], true, false);
+            stage<T, NC, TYT, 2, true, true>(td, S, ipd, i0, j0, (T)sc.beta[img], true, false);
 #endif
         } else {
             uint16_t codes[((TYT + 2) * (TX + 2) + NT - 1) / NT];
@@ -629,7 +635,7 @@ __global__ void __launch_bounds__(NT, MinBlocks<T>::dir) k_dir_poly(const __grid
             for (int c = 0; c < 1 + NC; ++c) dsrc[c] = ipd.out[c];
             stage_async<T, NC, TYT>(td, S, dsrc, i0, j0, nullptr);
 #else
-            stage<T, NC, TYT, 2>(td, S, ipd, i0, j0, (T)sc.beta[img], true, false);
+            stage<T, NC, TYT, 2, true, true>(td, S, ipd, i0, j0, (T)sc.beta[img], true, false);
 #endif
             store_codes<T, NC, TYT>(tx, codes);
             cp_async_wait_all();
@@ -713,8 +719,8 @@ __global__ void __launch_bounds__(NT) k_dir_update(const __grid_constant__ Batch
                 for (int c = 0; c < 1 + NC; ++c) {
                     const int s = gi + S.nx * gj;
                     using W = vec2_t<store_t<T>>;
-                    gv[r][c] = load2<T>(static_cast<const W *>(S.g[f.gcur][c]) + off + s);
-                    dv[r][c] = load2<T>(static_cast<const W *>(S.d[f.din][c]) + off + s);
+                    gv[r][c] = loadw<T>(static_cast<const W *>(S.g[f.gcur][c]) + off + s);
+                    dv[r][c] = loadw<T>(static_cast<const W *>(S.d[f.din][c]) + off + s);
                 }
         }
 #pragma unroll
@@ -726,7 +732,7 @@ __global__ void __launch_bounds__(NT) k_dir_update(const __grid_constant__ Batch
                     V v;
                     v.x = -gv[r][c].x + beta * dv[r][c].x;
                     v.y = -gv[r][c].y + beta * dv[r][c].y;
-                    store2<T>(static_cast<vec2_t<store_t<T>> *>(S.d[f.dout][c]) + off + gi + S.nx * gj, v);
+                    storew<T>(static_cast<vec2_t<store_t<T>> *>(S.d[f.dout][c]) + off + gi + S.nx * gj, v);
                 }
         }
     }
@@ -930,8 +936,10 @@ __global__ void __launch_bounds__(NT) k_jb(const __grid_constant__ Batch bt, con
     }
 }
 
-// x += alpha_pend[image] d over one image per blockIdx.y.
-template <class T>
+// x += alpha_pend[image] d over one image per blockIdx.y.  W: the compute
+// type of the NLCG passes that wrote d (ff: d holds float-float pairs, the
+// update runs in double on their values).
+template <class T, class W = T>
 __global__ void __launch_bounds__(NT) k_apply_update(vec2_t<T> *x, const vec2_t<T> *d, const double *alpha_pend,
                                                      long M)
 {
@@ -940,7 +948,14 @@ __global__ void __launch_bounds__(NT) k_apply_update(vec2_t<T> *x, const vec2_t<
     const long off = (long)blockIdx.y * M;
     for (long p = blockIdx.x * (long)NT + threadIdx.x; p < M; p += (long)gridDim.x * NT) {
         vec2_t<T> v = x[off + p];
-        const vec2_t<T> dd = d[off + p];
+        vec2_t<T> dd;
+        if constexpr (std::is_same<W, ff>::value) {
+            const ff2 w = loadw<ff>(d + off + p);
+            dd.x = to_double(w.x);
+            dd.y = to_double(w.y);
+        } else {
+            dd = d[off + p];
+        }
         v.x = v.x + a * dd.x;
         v.y = v.y + a * dd.y;
         x[off + p] = v;
@@ -1474,7 +1489,10 @@ cudaError_t launch_apply_update(const Launch &L, const Scalars &sc, const String
         const long M = (long)S.nx * S.ny;
         for (int c = 0; c < 1 + S.ncomp; ++c) {
             const dim3 grid((unsigned)((M + NT - 1) / NT < 64 ? (M + NT - 1) / NT : 64), (unsigned)S.F);
-            if (L.precision == 1)
+            if (L.precision == 1 && L.paired)   // d holds float-float pairs (paired passes)
+                k_apply_update<double, ff><<<grid, NT, 0, L.stream>>>(
+                    (double2 *)S.x[xbuf][c], (const double2 *)S.d[dbuf][c], sc.alpha_pend + S.img_base, M);
+            else if (L.precision == 1)
                 k_apply_update<double><<<grid, NT, 0, L.stream>>>(
                     (double2 *)S.x[xbuf][c], (const double2 *)S.d[dbuf][c], sc.alpha_pend + S.img_base, M);
             else
