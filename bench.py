@@ -349,24 +349,32 @@ def run_ours(args):
     ttb = None
     if rank == 0 and not args.no_ttb:
         from mepgl_gb300 import barrier as B
+        rmx = r64p = None
         if args.ttb_config == 2:
             target = 1.00779044   # F_{F-1} - F_0 after 600 outer iterations of FP64 (IEEE) relaxation
             r64, _ = B.run(2, 100, 160, "fp64")
-            rmx, _ = B.run(2, 100, 250, "mixed", -1, fp64_arith="paired")
+            rmxp, _ = B.run(2, 100, 250, "mixed", -1, fp64_arith="paired")
             work = "two-component GL 256x256 dx=0.4, 64 images, mode L, 100 NLCG steps per iteration"
         else:
             r64, _ = B.run(1, 50, 150, "fp64")
-            rmx, _ = B.run(1, 50, 150, "mixed", -1)
             target = r64[-1][3]
+            rmx, _ = B.run(1, 50, 150, "mixed", -1)
+            rmxp, _ = B.run(1, 50, 150, "mixed", -1, fp64_arith="paired")
+            r64p, _ = B.run(1, 50, 150, "fp64", fp64_arith="paired")
             work = "single-component GL 64x64 dx=0.5, 16 images, mode L, 50 NLCG steps per iteration"
 
         def t_to(rec):
+            if rec is None:
+                return None
             return B.time_within([x[0] for x in rec], [x[3] for x in rec], target, 1e-6)
         ttb = {"quantity": "F_end - F_0 within 1e-6 of the converged FP64 value",
-               "workload": work, "target": target, "fp64_s": t_to(r64), "mixed_s": t_to(rmx),
-               "mixed_polish": "paired FP64" if args.ttb_config == 2 else "IEEE FP64",
-               "mixed_fp32_iterations": sum(1 for x in rmx if x[4] == "fp32"),
-               "barrier_fp64": r64[-1][1], "barrier_mixed": rmx[-1][1]}
+               "workload": work, "target": target,
+               "fp64_s": t_to(r64),                 # IEEE double throughout
+               "mixed_s": t_to(rmx),                # FP32 until the end states plateau, then IEEE double
+               "mixed_paired_s": t_to(rmxp),        # FP32, then paired (float-float) FP64
+               "fp64_paired_s": t_to(r64p),         # paired FP64 throughout
+               "mixed_fp32_iterations": sum(1 for x in rmxp if x[4] == "fp32"),
+               "barrier_fp64": r64[-1][1], "barrier_mixed": rmxp[-1][1]}
 
     # ---- CPU baseline (rank 0, N = 1 only) ------------------------------------
     cpu = None
