@@ -118,6 +118,16 @@ namespace mepgl {
 #endif
 template <class T> struct MinBlocks { static constexpr int grad = MEPGL_MINB_GRAD, dir = MEPGL_MINB_DIR; };
 template <> struct MinBlocks<ff> { static constexpr int grad = MEPGL_MINB_GRAD_FF, dir = MEPGL_MINB_DIR_FF; };
+// Gradient tile kernels whose stencil spills at their register budget stage
+// one halo element at a time and read the previous gradient after the
+// stencil.  MEPGL_GRAD_LEAN: 0 none, 1 the float-float kernels (default),
+// 2 every precision.
+#ifndef MEPGL_GRAD_LEAN
+#define MEPGL_GRAD_LEAN 1
+#endif
+template <class T> struct GradLean {
+    static constexpr bool v = MEPGL_GRAD_LEAN == 2 || (MEPGL_GRAD_LEAN == 1 && std::is_same<T, ff>::value);
+};
 
 template <class T> struct TileRows { static constexpr int v = sizeof(T) == 4 ? MEPGL_ROWS_F32 : MEPGL_ROWS_F64; };
 // Two-component float-float NLCG passes run the packed stencils (site_pair.cuh).
@@ -172,19 +182,23 @@ struct ImagePtrs {                  // storage type (double for float-float)
 // mode 2: x = -aux + beta * in, i.e. the new direction (interior -> out).
 // IN_WORK / AUX_WORK: in (and out) / aux are NLCG work arrays (g, d) rather
 // than fields.
-template <class T, int NC, int TYT, int MODE, bool IN_WORK = false, bool AUX_WORK = false>
+// CHUNK: one element's loads in flight at a time instead of all of them
+// (fewer registers live, for the kernels whose stencil is near its budget).
+template <class T, int NC, int TYT, int MODE, bool IN_WORK = false, bool AUX_WORK = false, bool CHUNK = false>
 __device__ __forceinline__ void stage(Tile<T, NC, TYT> &t, const StringDesc &S, const ImagePtrs<T, NC> &ip, int i0,
                                       int j0, T coef, bool write_out, bool masks)
 {
     using V = vec2_t<T>;
-    constexpr int HW = TX + 2, HE = (TYT + 2) * HW, NI = (HE + NT - 1) / NT;
+    constexpr int HW = TX + 2, HE = (TYT + 2) * HW, NI = (HE + NT - 1) / NT, KB = CHUNK ? 1 : NI;
     const bool aux = MODE == 2 || (MODE == 1 && coef != (T)0);
     V f[NI][1 + NC], a[NI][1 + NC];
     uint16_t m[NI];
     int sidx[NI];
     bool ok[NI];
 #pragma unroll
-    for (int k = 0; k < NI; ++k) {
+    for (int k0 = 0; k0 < NI; k0 += KB) {
+#pragma unroll
+    for (int k = k0; k < k0 + KB; ++k) {
         const int e = threadIdx.x + k * NT;
         const int hy = e / HW, hx = e - hy * HW;
         const int gi = i0 + hx - 1, gj = j0 + hy - 1;
@@ -210,7 +224,7 @@ __device__ __forceinline__ void stage(Tile<T, NC, TYT> &t, const StringDesc &S, 
         }
     }
 #pragma unroll
-    for (int k = 0; k < NI; ++k) {
+    for (int k = k0; k < k0 + KB; ++k) {
         const int e = threadIdx.x + k * NT;
         if (e >= HE) continue;
         const int hy = e / HW, hx = e - hy * HW;
@@ -237,6 +251,7 @@ __device__ __forceinline__ void stage(Tile<T, NC, TYT> &t, const StringDesc &S, 
 #pragma unroll
         for (int c = 0; c < NC; ++c) t.P[c][hy][hx] = v[1 + c];
         if (masks) t.m[hy][hx] = m[k];
+    }
     }
 }
 
@@ -440,7 +455,7 @@ __global__ void __launch_bounds__(NT, MinBlocks<T>::grad) k_grad(const __grid_co
         image_ptrs<T, NC>(ip, S.x[f.xin], S.d[f.din], S.x[f.xout], off);
 #if MEPGL_GRAD_ASYNC
         if constexpr (std::is_same<T, ff>::value) {
-            stage<T, NC, TYT, 1, false, true>(t, S, ip, i0, j0, (T)sc.alpha_pend[img], true, true);
+            stage<T, NC, TYT, 1, false, true, GradLean<T>::v>(t, S, ip, i0, j0, (T)sc.alpha_pend[img], true, true);
         } else {
             constexpr int HW = TX + 2, HE = (TYT + 2) * HW, NI = (HE + NT - 1) / NT;
             const T alpha = (T)sc.alpha_pend[img];
@@ -480,7 +495,7 @@ __global__ void __launch_bounds__(NT, MinBlocks<T>::grad) k_grad(const __grid_co
             }
         }
 #else
-        stage<T, NC, TYT, 1, false, true>(t, S, ip, i0, j0, (T)sc.alpha_pend[img], true, true);
+        stage<T, NC, TYT, 1, false, true, GradLean<T>::v>(t, S, ip, i0, j0, (T)sc.alpha_pend[img], true, true);
 #endif
         using W = vec2_t<store_t<T>>;
         W *gcur[1 + NC];
@@ -496,7 +511,9 @@ __global__ void __launch_bounds__(NT, MinBlocks<T>::grad) k_grad(const __grid_co
         T v[2] = {(T)0, (T)0};
         const int lx = threadIdx.x & 31, gi = i0 + lx;
         // previous gradient of this thread's sites, loaded before the stencil
+        // (lean kernels: after it, so that it holds no registers meanwhile)
         V gold[TYT / 8][1 + NC];
+        if (!GradLean<T>::v)
 #pragma unroll
         for (int r = 0; r < TYT / 8; ++r) {
             const int gj = j0 + (threadIdx.x >> 5) + 8 * r;
@@ -530,6 +547,9 @@ __global__ void __launch_bounds__(NT, MinBlocks<T>::grad) k_grad(const __grid_co
                 } else {
                     site_gradient<T, NC, TYT>(t, lx + 1, ly + 1, p, w, hr, hl, hu, hd, f.maxwell, S.thin_film, g);
                 }
+                if (GradLean<T>::v)
+#pragma unroll
+                    for (int c = 0; c < 1 + NC; ++c) gold[r][c] = loadw<T>(gprev[c] + s);
 #pragma unroll
                 for (int c = 0; c < 1 + NC; ++c) {
                     V gv;
