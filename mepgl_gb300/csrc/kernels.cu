@@ -91,6 +91,10 @@ namespace mepgl {
 #ifndef MEPGL_STRIP_FUSED
 #define MEPGL_STRIP_FUSED 0
 #endif
+// FP32 strip launches of a single string use kernels specialised for it
+#ifndef MEPGL_STRIP_ONE
+#define MEPGL_STRIP_ONE 1
+#endif
 #ifndef MEPGL_MINB_STRIP_FUSED
 #define MEPGL_MINB_STRIP_FUSED MEPGL_MINB_STRIP
 #endif
@@ -1359,12 +1363,22 @@ inline int grid_for(long n, int cap = 152 * 16)
         }                                                                                           \
     } while (0)
 
-// FP32 NLCG passes: one single-warp block per tile.
+// FP32 NLCG passes: one single-warp block per tile; launches of one string
+// take the kernels that read its descriptor at fixed offsets.
 #define DISPATCH_STRIP(L, KERNEL, ...)                                                              \
     do {                                                                                            \
-        if ((L).ncomp == 2) KERNEL<float, 2><<<(L).n_tiles, NTS, 0, (L).stream>>>(__VA_ARGS__);     \
-        else KERNEL<float, 1><<<(L).n_tiles, NTS, 0, (L).stream>>>(__VA_ARGS__);                    \
+        if (strip_one(L)) {                                                                         \
+            if ((L).ncomp == 2) KERNEL<float, 2, true><<<(L).n_tiles, NTS, 0, (L).stream>>>(__VA_ARGS__); \
+            else KERNEL<float, 1, true><<<(L).n_tiles, NTS, 0, (L).stream>>>(__VA_ARGS__);          \
+        } else {                                                                                    \
+            if ((L).ncomp == 2) KERNEL<float, 2, false><<<(L).n_tiles, NTS, 0, (L).stream>>>(__VA_ARGS__); \
+            else KERNEL<float, 1, false><<<(L).n_tiles, NTS, 0, (L).stream>>>(__VA_ARGS__);         \
+        }                                                                                           \
     } while (0)
+
+// Single-string FP32 launch (MEPGL_STRIP_ONE = 0 sends every launch through
+// the indexed-descriptor kernels).
+static inline bool strip_one(const Launch &L) { return MEPGL_STRIP_ONE && L.batch->n == 1; }
 
 cudaError_t launch_grad(const Launch &L, const Scalars &sc, const StepFlags &f)
 {
@@ -1407,8 +1421,8 @@ int strip_pass_slots(int ncomp)
         if (cudaGetDevice(&dev) != cudaSuccess ||
             cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
             return 0;
-        const cudaError_t e = ci ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_dir_poly_s<float, 2>, NTS, 0)
-                                 : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_dir_poly_s<float, 1>, NTS, 0);
+        const cudaError_t e = ci ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_dir_poly_s<float, 2, false>, NTS, 0)
+                                 : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_dir_poly_s<float, 1, false>, NTS, 0);
         if (e != cudaSuccess) return 0;
         slots[ci] = nb * sms;
     }
@@ -1424,15 +1438,21 @@ cudaError_t launch_nlcg_fused(const Launch &L, const Scalars &sc, const StepFlag
                               unsigned max_polls)
 {
 #if MEPGL_STRIP
-    static int slots[2] = {0, 0};
-    const int ci = L.ncomp == 2 ? 1 : 0;
+    static int slots[4] = {0, 0, 0, 0};
+    const bool one = strip_one(L);
+    const int ci = (L.ncomp == 2 ? 1 : 0) + (one ? 2 : 0);
     if (slots[ci] == 0) {
         int dev = 0, sms = 0, nb = 0;
         cudaError_t e = cudaGetDevice(&dev);
         if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        if (e == cudaSuccess)
-            e = ci ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_nlcg_s<float, 2>, NTS, 0)
-                   : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_nlcg_s<float, 1>, NTS, 0);
+        if (e == cudaSuccess) {
+            switch (ci) {
+            case 0: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_nlcg_s<float, 1, false>, NTS, 0); break;
+            case 1: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_nlcg_s<float, 2, false>, NTS, 0); break;
+            case 2: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_nlcg_s<float, 1, true>, NTS, 0); break;
+            default: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_nlcg_s<float, 2, true>, NTS, 0); break;
+            }
+        }
         if (e != cudaSuccess) return e;
         slots[ci] = nb * sms > 0 ? nb * sms : 1;
     }
@@ -1448,12 +1468,14 @@ cudaError_t launch_nlcg_fused(const Launch &L, const Scalars &sc, const StepFlag
     if (e != cudaSuccess) return e;
     const long long items = 2LL * L.n_tiles * steps;
     const int grid = items < slots[ci] ? (int)items : slots[ci];
-    if (ci)
-        k_nlcg_s<float, 2><<<grid, NTS, 0, L.stream>>>(*L.batch, L.tile0, L.n_tiles, steps, plan, sc, queue, stage,
-                                                         max_polls);
-    else
-        k_nlcg_s<float, 1><<<grid, NTS, 0, L.stream>>>(*L.batch, L.tile0, L.n_tiles, steps, plan, sc, queue, stage,
-                                                         max_polls);
+#define FUSED_ARGS *L.batch, L.tile0, L.n_tiles, steps, plan, sc, queue, stage, max_polls
+    switch (ci) {
+    case 0: k_nlcg_s<float, 1, false><<<grid, NTS, 0, L.stream>>>(FUSED_ARGS); break;
+    case 1: k_nlcg_s<float, 2, false><<<grid, NTS, 0, L.stream>>>(FUSED_ARGS); break;
+    case 2: k_nlcg_s<float, 1, true><<<grid, NTS, 0, L.stream>>>(FUSED_ARGS); break;
+    default: k_nlcg_s<float, 2, true><<<grid, NTS, 0, L.stream>>>(FUSED_ARGS); break;
+    }
+#undef FUSED_ARGS
     return cudaGetLastError();
 #else
     (void)L; (void)sc; (void)f0; (void)it0; (void)steps; (void)queue; (void)stage; (void)n_stage;

@@ -178,11 +178,16 @@ __device__ __forceinline__ void cp_async_wait_groups() { asm volatile("cp.async.
 // Tile g of the global tile order (strings in order, each from its
 // tile_base: image, tile row, tile column), derived from the block index and
 // the descriptors alone so that it is uniform over the block.
+// ONE: the launch covers a single string (bt.n == 1); its descriptor is
+// then read at fixed offsets, i.e. as constant operands, not through
+// indexed constant loads.
+template <bool ONE>
 __device__ __forceinline__ TileRef strip_tile(const Batch &bt, int g)
 {
     int s = 0;
-    for (int k = 1; k < bt.n; ++k)
-        if (g >= bt.s[k].tile_base) s = k;
+    if (!ONE)
+        for (int k = 1; k < bt.n; ++k)
+            if (g >= bt.s[k].tile_base) s = k;
     TileRef t = flat_tile(bt.s[s], g - bt.s[s].tile_base);
     t.s = (int16_t)s;
     return t;
@@ -258,13 +263,13 @@ using GradRing = vec2_t<T>[3][2][2][1 + NC];
 // (in every lane) when this tile finished its image.  Before the tile's
 // partials are counted every lane fences its field stores, so that a
 // consumer that has seen the image finished (same launch) reads them.
-template <class T, int NC>
+template <class T, int NC, bool ONE>
 __device__ __forceinline__ bool grad_tile(const Batch &bt, const TileRef tr, const Scalars &sc, const StepFlags &f,
                                           GradRing<T, NC> &ring)
 {
     constexpr int TYT = TileRows<T>::v;
     using V = vec2_t<T>;
-    const StringDesc &S = bt.s[tr.s];
+    const StringDesc &S = bt.s[ONE ? 0 : tr.s];
     const int img = S.img_base + tr.n;
     const int i0 = tr.tx * TX, j0 = tr.ty * TYT;
     const size_t off = (size_t)tr.n * S.nx * S.ny;
@@ -415,12 +420,12 @@ __device__ __forceinline__ bool grad_tile(const Batch &bt, const TileRef tr, con
     return fin;
 }
 
-template <class T, int NC>
+template <class T, int NC, bool ONE>
 __global__ void __launch_bounds__(NTS, MEPGL_MINB_STRIP_GRAD) k_grad_s(const __grid_constant__ Batch bt,
                                                                   int tile0, Scalars sc, StepFlags f)
 {
     __shared__ __align__(16) GradRing<T, NC> ring;
-    grad_tile<T, NC>(bt, strip_tile(bt, tile0 + (int)blockIdx.x), sc, f, ring);
+    grad_tile<T, NC, ONE>(bt, strip_tile<ONE>(bt, tile0 + (int)blockIdx.x), sc, f, ring);
 }
 
 // One row of the polynomial window: fields and new direction of the lane's
@@ -440,13 +445,13 @@ using DirRing = vec2_t<T>[3][2][3][1 + NC];
 // image runs the line search.  Same semantics as k_dir_poly.  Returns true
 // (in every lane) when this tile finished its image; field stores are
 // fenced as in grad_tile.
-template <class T, int NC>
+template <class T, int NC, bool ONE>
 __device__ __forceinline__ bool dir_tile(const Batch &bt, const TileRef tr, const Scalars &sc, const StepFlags &f,
                                          DirRing<T, NC> &ring, double (&coef)[5])
 {
     constexpr int TYT = TileRows<T>::v;
     using V = vec2_t<T>;
-    const StringDesc &S = bt.s[tr.s];
+    const StringDesc &S = bt.s[ONE ? 0 : tr.s];
     const int img = S.img_base + tr.n;
     const int i0 = tr.tx * TX, j0 = tr.ty * TYT;
     const size_t off = (size_t)tr.n * S.nx * S.ny;
@@ -607,13 +612,13 @@ __device__ __forceinline__ bool dir_tile(const Batch &bt, const TileRef tr, cons
     return fin;
 }
 
-template <class T, int NC>
+template <class T, int NC, bool ONE>
 __global__ void __launch_bounds__(NTS, MEPGL_MINB_STRIP_DIR) k_dir_poly_s(const __grid_constant__ Batch bt,
                                                                       int tile0, Scalars sc, StepFlags f)
 {
     __shared__ __align__(16) DirRing<T, NC> ring;
     __shared__ double coef[5];
-    dir_tile<T, NC>(bt, strip_tile(bt, tile0 + (int)blockIdx.x), sc, f, ring, coef);
+    dir_tile<T, NC, ONE>(bt, strip_tile<ONE>(bt, tile0 + (int)blockIdx.x), sc, f, ring, coef);
 }
 
 // ------------------------------------------------------------ fused steps
@@ -689,7 +694,7 @@ __device__ __forceinline__ void publish_stage(unsigned *stage, unsigned value)
 #define MEPGL_FUSED_BOUNDS __launch_bounds__(NTS, MEPGL_MINB_STRIP_FUSED)
 #endif
 
-template <class T, int NC>
+template <class T, int NC, bool ONE>
 __global__ void MEPGL_FUSED_BOUNDS k_nlcg_s(const __grid_constant__ Batch bt, int tile0, int n_tiles, int steps,
                                             StepPlan plan, Scalars sc, unsigned long long *queue, unsigned *stage,
                                             unsigned max_polls)
@@ -707,15 +712,15 @@ __global__ void MEPGL_FUSED_BOUNDS k_nlcg_s(const __grid_constant__ Batch bt, in
         const int k = (int)(item / per_step);
         const int r = (int)(item - (unsigned long long)k * per_step);
         const int pass = r >= n_tiles ? 1 : 0, u = r - pass * n_tiles;
-        const TileRef tr = strip_tile(bt, tile0 + u);
-        const int img = bt.s[tr.s].img_base + tr.n;
+        const TileRef tr = strip_tile<ONE>(bt, tile0 + u);
+        const int img = bt.s[ONE ? 0 : tr.s].img_base + tr.n;
         const unsigned need = 2u * (unsigned)k + (unsigned)pass;
         if (need > 0 && !wait_stage(stage + img, need, max_polls, sc.status)) return;
         const StepFlags f = plan.step(k);
         if (pass == 0) {
-            if (grad_tile<T, NC>(bt, tr, sc, f, gring)) publish_stage(stage + img, need + 1);
+            if (grad_tile<T, NC, ONE>(bt, tr, sc, f, gring)) publish_stage(stage + img, need + 1);
         } else {
-            if (dir_tile<T, NC>(bt, tr, sc, f, dring, coef)) publish_stage(stage + img, need + 1);
+            if (dir_tile<T, NC, ONE>(bt, tr, sc, f, dring, coef)) publish_stage(stage + img, need + 1);
         }
     }
 }
