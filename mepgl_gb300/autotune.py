@@ -36,7 +36,7 @@ TUNING = os.path.join(PKG, "tuning.json")
 # row loop unrolled by the window period, unit-weight path for interior
 # sites, packed FP32x2 stencils for two components, all steps of a call in
 # one fused persistent launch, and its blocks per SM or explicit register cap.
-STRIP = [(32, 16, 16, 0, 0, 1, 1, 12, 0), (32, 16, 16, 0, 0, 1, 1, 16, 152), (32, 16, 16, 0, 0, 1, 1, 16, 144),
+STRIP = [(40, 16, 16, 0, 0, 1, 1, 12, 0), (32, 16, 16, 0, 0, 1, 1, 12, 0), (32, 16, 16, 0, 0, 1, 1, 16, 152), (32, 16, 16, 0, 0, 1, 1, 16, 144),
          (32, 16, 16, 0, 0, 1, 1, 16, 128), (32, 16, 16, 0, 0, 1, 0, 16, 0)]
 # Tile candidates: rows per FP32 tile, min blocks per SM for the gradient
 # pass, for the direction pass, gradient-pass halo copy (0 through
