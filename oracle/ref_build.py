@@ -10,16 +10,18 @@ the host once the CUDA language extensions are stubbed (``ref_shim.h``) and the
 or cuSPARSE calls -- are left out.  ``ref_driver.cpp`` then emulates each
 launch serially and restates the host-side call sequence.
 
-For every variant (N, dx, components, precision, thin film) this script writes
-under ``oracle/_ref/<tag>/``:
+For every variant (N, dx, components, precision, thin film) this script
+compiles, in a temporary directory that is removed afterwards:
 
 * ``real.cuh`` / ``config.cuh`` -- the two headers the reference generates per
   run, written here from the variant;
 * ``nlcg_kernels.inc`` / ``interp_kernels.inc`` -- the kernels of
   mepgl/src/nlcg.cu and mepgl/src/interpolation.cu with ``#include`` lines and
-  ``__host__`` functions removed (read from the reference tree at build time;
-  nothing is copied into the repository);
-* ``libref.so`` -- ``ref_driver.cpp`` compiled against them.
+  ``__host__`` functions removed, read from the reference tree at build time;
+
+and writes ``oracle/_ref/<tag>/libref.so`` -- ``ref_driver.cpp`` compiled
+against them -- and nothing else: no reference text is kept in or shipped
+with the repository.
 
 The FP64 variants do not define ``DOUBLE_PRECISION``; the reference compiles
 its cubic spline only without that macro (interpolation.cu:359,483), and this
@@ -37,6 +39,7 @@ import os
 import re
 import subprocess
 import sys
+import tempfile
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 REF_ROOT = os.environ.get("MEPGL_REFERENCE", "/root/reference")
@@ -155,15 +158,18 @@ def build(n: int, dx: float, comps: int, prec: str, film: bool, force: bool = Fa
         "nlcg_kernels.inc": _strip_includes(_strip_host_functions(nlcg)),
         "interp_kernels.inc": _strip_includes(_strip_host_functions(interp)),
     }
-    for name, body in files.items():
-        with open(os.path.join(d, name), "w") as f:
-            f.write(body)
-    cmd = [
-        os.environ.get("CXX", "g++"), "-std=c++17", "-O2", "-ffp-contract=off", "-fPIC", "-shared",
-        "-w", "-I", d, "-I", HERE, "-include", os.path.join(HERE, "ref_shim.h"),
-        os.path.join(HERE, "ref_driver.cpp"), "-o", lib + ".tmp",
-    ]
-    subprocess.run(cmd, check=True)
+    # the filtered kernel text lives only in a temporary directory for the
+    # compile; the variant directory keeps the library alone
+    with tempfile.TemporaryDirectory(prefix="mepgl_ref_") as tmp:
+        for name, body in files.items():
+            with open(os.path.join(tmp, name), "w") as f:
+                f.write(body)
+        cmd = [
+            os.environ.get("CXX", "g++"), "-std=c++17", "-O2", "-ffp-contract=off", "-fPIC", "-shared",
+            "-w", "-I", tmp, "-I", HERE, "-include", os.path.join(HERE, "ref_shim.h"),
+            os.path.join(HERE, "ref_driver.cpp"), "-o", lib + ".tmp",
+        ]
+        subprocess.run(cmd, check=True)
     os.replace(lib + ".tmp", lib)
     return lib
 
