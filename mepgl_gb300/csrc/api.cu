@@ -572,7 +572,8 @@ mepgl_status ensure_plan(mepgl_ctx *c, int F, int F_new)
     if (need <= c->plan_cap) return MEPGL_OK;
     RedistPlan &p = c->plan;
     cudaFree(p.k); cudaFree(p.w); cudaFree(p.h); cudaFree(p.dl); cudaFree(p.d); cudaFree(p.du); cudaFree(p.du2);
-    cudaFree(p.ipiv); cudaFree(p.status);
+    cudaFree(p.ipiv); cudaFree(p.status); cudaFree(p.aux);
+    CK(c, cudaMalloc(&p.aux, redist_aux_size(need) * sizeof(double)));
     CK(c, cudaMalloc(&p.k, need * sizeof(int)));
     CK(c, cudaMalloc(&p.ipiv, need * sizeof(int)));
     CK(c, cudaMalloc(&p.status, 4 * sizeof(int)));
@@ -833,7 +834,7 @@ mepgl_status mepgl_destroy(mepgl_ctx *c)
     free_scalars(c);
     RedistPlan &p = c->plan;
     cudaFree(p.k); cudaFree(p.w); cudaFree(p.h); cudaFree(p.dl); cudaFree(p.d); cudaFree(p.du); cudaFree(p.du2);
-    cudaFree(p.ipiv); cudaFree(p.status);
+    cudaFree(p.ipiv); cudaFree(p.status); cudaFree(p.aux);
     cudaFree(c->cubic_scratch);
     if (c->own_stream) cudaStreamDestroy(c->stream);
     delete c;

@@ -987,20 +987,24 @@ __global__ void __launch_bounds__(NT) k_apply_update(vec2_t<T> *x, const vec2_t<
 }
 
 // Arc length: squared image-to-image distance over every site (no mask, no
-// dx^2; interpolation.cu:39-92).  Each thread walks its sites through the
-// images, carrying image n-1 in registers, so every value is read once.
+// dx^2; interpolation.cu:39-92).  Block (bx, by) covers sites
+// [bx * NT * ARC_SPT, ...) and the images of chunk by; it reads the image
+// before its chunk first as the previous one, so each (image, site block)
+// partial is the sum one walk through all images would give.  The chunks
+// spread a string of few sites over enough blocks to fill the GPU.
 constexpr int ARC_SPT = 4;
 
 template <class T>
 __global__ void __launch_bounds__(NT) k_arc_partial(const T *f0, const T *f1, const T *f2, int w0, int w1, int w2,
-                                                    long sites, int F, double *part)
+                                                    long sites, int F, int per_chunk, double *part)
 {
     __shared__ double red[NT / 32];
     const T *fs[3] = {f0, f1, f2};
     const int ws[3] = {w0, w1, w2};
     T prev[3][ARC_SPT][2];
     const long base = (long)blockIdx.x * NT * ARC_SPT + threadIdx.x;
-    for (int n = 0; n < F; ++n) {
+    const int n0 = (int)blockIdx.y * per_chunk, n1 = n0 + per_chunk < F ? n0 + per_chunk : F;
+    for (int n = n0 > 0 ? n0 - 1 : 0; n < n1; ++n) {
         T acc = 0;
 #pragma unroll
         for (int q = 0; q < ARC_SPT; ++q) {
@@ -1010,16 +1014,25 @@ __global__ void __launch_bounds__(NT) k_arc_partial(const T *f0, const T *f1, co
 #pragma unroll
             for (int f = 0; f < 3; ++f) {
                 if (!fs[f]) continue;
+                T v[2];
+                if (ws[f] == 2) {   // one vector load per site
+                    const vec2_t<T> p2 = reinterpret_cast<const vec2_t<T> *>(fs[f])[(long)n * sites + s];
+                    v[0] = p2.x;
+                    v[1] = p2.y;
+                } else {
+                    v[0] = fs[f][(long)n * sites + s];
+                    v[1] = 0;
+                }
 #pragma unroll
                 for (int w = 0; w < 2; ++w) {
                     if (w >= ws[f]) continue;
-                    const T v = fs[f][((long)n * sites + s) * ws[f] + w];
-                    if (n > 0) d2 += (v - prev[f][q][w]) * (v - prev[f][q][w]);
-                    prev[f][q][w] = v;
+                    if (n > 0 && n >= n0) d2 += (v[w] - prev[f][q][w]) * (v[w] - prev[f][q][w]);
+                    prev[f][q][w] = v[w];
                 }
             }
             acc += d2;
         }
+        if (n < n0) continue;   // the previous image of the chunk: loaded, not summed (block-uniform)
         const T vv[1] = {acc};
         double tot[1];
         block_sum<1>(vv, tot, red);
@@ -1169,84 +1182,200 @@ __global__ void k_winding(const vec2_t<T> *__restrict__ psi, int nx, int ny, int
     }
 }
 
-// computeArcLength (interpolation.cu:126-140): cumulative sqrt, s[F-1] = 1.
-__global__ void k_arc_finish(const double *part, int nblocks, int F, double *s)
+// computeArcLength (interpolation.cu:126-140), first half: block n adds
+// image n's partials.
+__global__ void k_arc_sum(const double *part, int nblocks, double *s)
 {
     __shared__ double red[NT / 32];
-    for (int n = 0; n < F; ++n) {
-        double v[1] = {0.0};
-        for (int b = threadIdx.x; b < nblocks; b += NT) v[0] += part[(size_t)n * nblocks + b];
-        double tot[1];
-        block_sum<1>(v, tot, red);
-        if (threadIdx.x == 0) s[n] = tot[0];
-    }
-    if (threadIdx.x == 0) {
-        s[0] = 0.0;
-        for (int n = 1; n < F; ++n) s[n] = s[n - 1] + sqrt(s[n]);
-        for (int n = 0; n < F; ++n) s[n] /= s[F - 1];
-    }
+    const int n = blockIdx.x;
+    double v[1] = {0.0};
+    for (int b = threadIdx.x; b < nblocks; b += NT) v[0] += part[(size_t)n * nblocks + b];
+    double tot[1];
+    block_sum<1>(v, tot, red);
+    if (threadIdx.x == 0) s[n] = tot[0];
 }
 
-// Redistribution plan (one thread): segment and weight per output image,
-// and for the cubic spline the Forsythe-Malcolm-Moler matrix (buildHMatrix,
+// Second half: cumulative sqrt, normalised so that s[F-1] = 1.  The square
+// roots and the divisions (slow in FP64 here) run across the block; one
+// thread adds in image order.  Strings of more than ARC_CUM_MAX images run
+// it all in one thread.
+constexpr int ARC_CUM_MAX = 4096;
+
+__global__ void k_arc_cumulate(int F, double *s)
+{
+    __shared__ double r[ARC_CUM_MAX];
+    __shared__ double total;
+    if (F > ARC_CUM_MAX) {
+        if (threadIdx.x == 0) {
+            double acc = 0.0;
+            s[0] = 0.0;
+            for (int n = 1; n < F; ++n) {
+                acc += sqrt(s[n]);
+                s[n] = acc;
+            }
+            for (int n = 0; n < F; ++n) s[n] /= acc;
+        }
+        return;
+    }
+    for (int n = threadIdx.x; n < F; n += blockDim.x) r[n] = n == 0 ? 0.0 : sqrt(s[n]);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double acc = 0.0;
+        for (int n = 1; n < F; ++n) {
+            acc += r[n];
+            r[n] = acc;
+        }
+        total = acc;
+    }
+    __syncthreads();
+    for (int n = threadIdx.x; n < F; n += blockDim.x) s[n] = r[n] / total;
+}
+
+// Redistribution plan: segment and weight per output image, and for the
+// cubic spline the Forsythe-Malcolm-Moler matrix (buildHMatrix,
 // interpolation.cu:252-290) factorised once by Gaussian elimination with
 // partial pivoting (the LAPACK gtsv algorithm) for every site's system.
-__global__ void k_redist_plan(const double *s, int F, int F_new, int cubic, int spline, RedistPlan p)
+// One block of 32 threads.  The segment walk and the elimination are
+// sequential (thread 0); everything that is not (differences h, output
+// positions, weights, and the reciprocals and per-image coefficients that
+// spare the cubic resample its divisions) is spread over the block, because
+// every FP64 division and square root is slow on this GPU.  The arrays live
+// in shared memory when they fit, else in the plan's global arrays.
+
+// Shared-memory bytes of the plan kernel: s, h, dl, d, du, du2 [F or F+1],
+// output positions and segment starts [F_new] as doubles; ipiv [F] and the
+// segments [F_new] as ints.
+__host__ __device__ inline size_t redist_plan_smem(int F, int F_new)
 {
-    if (threadIdx.x != 0 || blockIdx.x != 0) return;
-    double *h = p.h;
-    h[0] = 0.0;
-    for (int n = 1; n < F; ++n) h[n] = s[n] - s[n - 1];
-    h[F] = INFINITY;
+    return (size_t)(6 * F + 1 + 2 * F_new) * sizeof(double) + (size_t)(F + F_new) * sizeof(int);
+}
+
+__global__ void k_redist_plan(const double *s_in, int F, int F_new, int cubic, int spline, RedistPlan p, int use_smem)
+{
+    if (blockIdx.x != 0) return;
+    extern __shared__ double plan_sm[];
+    const int t = threadIdx.x, nt = blockDim.x;
+    const double *s = s_in;
+    double *h = p.h, *dl = p.dl, *d = p.d, *du = p.du, *du2 = p.du2, *snew = nullptr, *sst = nullptr;
+    int *ipiv = p.ipiv, *kk = p.k;
+    if (use_smem) {
+        double *ss = plan_sm;
+        h = ss + F;
+        dl = h + F + 1;
+        d = dl + F;
+        du = d + F;
+        du2 = du + F;
+        snew = du2 + F;
+        sst = snew + F_new;
+        ipiv = reinterpret_cast<int *>(sst + F_new);
+        kk = ipiv + F;
+        for (int n = t; n < F; n += nt) ss[n] = s_in[n];
+        s = ss;
+        __syncthreads();
+    }
+    // h[n] = s[n] - s[n-1]; output positions n / (F_new - 1)
+    for (int n = t; n <= F; n += nt) h[n] = n == 0 ? 0.0 : (n == F ? INFINITY : s[n] - s[n - 1]);
+    if (use_smem)
+        for (int n = t; n < F_new; n += nt) snew[n] = (double)n / (double)(F_new - 1);
+    __syncthreads();
     const bool walk_sum = cubic && spline == 0;
-    int k = 1;
-    double seg_start = 0.0, seg_end = walk_sum ? h[1] : s[1];
-    for (int n = 0; n < F_new; ++n) {
-        const double s_new = (double)n / (double)(F_new - 1);
-        if (walk_sum) {
-            while (seg_end < s_new) { k++; seg_start += h[k - 1]; seg_end += h[k]; }
-        } else {
-            while (seg_end < s_new && k < F - 1) { k++; seg_start = s[k - 1]; seg_end = s[k]; }
-        }
-        if (k >= F) k = F - 1;
-        p.k[n] = k;
-        p.w[n] = (s_new - seg_start) / (cubic ? h[k] : (s[k] - s[k - 1]));
-    }
-    if (!cubic) return;
-    double *dl = p.dl, *d = p.d, *du = p.du, *du2 = p.du2;
-    int *ipiv = p.ipiv;
-    for (int n = 0; n < F; ++n) { dl[n] = d[n] = du[n] = du2[n] = 0.0; ipiv[n] = 0; }
-    d[0] = -h[1];
-    du[0] = h[1];
-    for (int n = 1; n < F - 1; ++n) { dl[n] = h[n]; d[n] = 2 * (h[n] + h[n + 1]); du[n] = h[n + 1]; }
-    dl[F - 1] = h[F - 1];
-    d[F - 1] = -h[F - 1];
-    for (int q = 0; q < F - 1; ++q) {
-        const double sub = dl[q + 1];
-        if (fabs(d[q]) >= fabs(sub)) {
-            if (d[q] != 0) {
-                const double l = sub / d[q];
-                dl[q + 1] = l;
-                d[q + 1] = d[q + 1] - l * du[q];
+    if (t == 0) {
+        // segment walk (comparisons and additions only when the positions are staged)
+        int k = 1;
+        double seg_start = 0.0, seg_end = walk_sum ? h[1] : s[1];
+        for (int n = 0; n < F_new; ++n) {
+            const double s_new = use_smem ? snew[n] : (double)n / (double)(F_new - 1);
+            if (walk_sum) {
+                while (seg_end < s_new) { k++; seg_start += h[k - 1]; seg_end += h[k]; }
             } else {
-                dl[q + 1] = 0;
+                while (seg_end < s_new && k < F - 1) { k++; seg_start = s[k - 1]; seg_end = s[k]; }
             }
-        } else {
-            const double l = d[q] / sub;
-            d[q] = sub;
-            dl[q + 1] = l;
-            const double tmp = du[q];
-            du[q] = d[q + 1];
-            d[q + 1] = tmp - l * d[q + 1];
-            if (q < F - 2) {
-                du2[q] = du[q + 1];
-                du[q + 1] = -l * du[q + 1];
-            }
-            ipiv[q] = 1;
+            if (k >= F) k = F - 1;
+            kk[n] = k;
+            if (use_smem) sst[n] = seg_start;
+            else p.w[n] = (s_new - seg_start) / (cubic ? h[k] : (s[k] - s[k - 1]));
         }
     }
-    for (int q = 0; q < F; ++q)
-        if (d[q] == 0 && p.status) *p.status = 1;
+    __syncthreads();
+    if (use_smem)
+        for (int n = t; n < F_new; n += nt) {
+            const int k = kk[n];
+            p.k[n] = k;
+            p.w[n] = (snew[n] - sst[n]) / (cubic ? h[k] : (s[k] - s[k - 1]));
+        }
+    if (!cubic) {
+        if (use_smem)
+            for (int n = t; n <= F; n += nt) p.h[n] = h[n];
+        return;
+    }
+    if (t == 0) {
+        for (int n = 0; n < F; ++n) { dl[n] = d[n] = du[n] = du2[n] = 0.0; ipiv[n] = 0; }
+        d[0] = -h[1];
+        du[0] = h[1];
+        for (int n = 1; n < F - 1; ++n) { dl[n] = h[n]; d[n] = 2 * (h[n] + h[n + 1]); du[n] = h[n + 1]; }
+        dl[F - 1] = h[F - 1];
+        d[F - 1] = -h[F - 1];
+        for (int q = 0; q < F - 1; ++q) {
+            const double sub = dl[q + 1];
+            if (fabs(d[q]) >= fabs(sub)) {
+                if (d[q] != 0) {
+                    const double l = sub / d[q];
+                    dl[q + 1] = l;
+                    d[q + 1] = d[q + 1] - l * du[q];
+                } else {
+                    dl[q + 1] = 0;
+                }
+            } else {
+                const double l = d[q] / sub;
+                d[q] = sub;
+                dl[q + 1] = l;
+                const double tmp = du[q];
+                du[q] = d[q + 1];
+                d[q + 1] = tmp - l * d[q + 1];
+                if (q < F - 2) {
+                    du2[q] = du[q + 1];
+                    du[q + 1] = -l * du[q + 1];
+                }
+                ipiv[q] = 1;
+            }
+        }
+        for (int q = 0; q < F; ++q)
+            if (d[q] == 0 && p.status) *p.status = 1;
+    }
+    __syncthreads();
+    // factors out (from shared memory), and the cubic resample's uniform coefficients
+    double *rh = p.aux, *rd = rh + F, *ev = rd + F, *ends = ev + 4 * F_new;
+    for (int n = t; n <= F; n += nt) {
+        if (use_smem) p.h[n] = h[n];
+        if (n == F) continue;
+        if (use_smem) {
+            p.dl[n] = dl[n];
+            p.d[n] = d[n];
+            p.du[n] = du[n];
+            p.du2[n] = du2[n];
+            p.ipiv[n] = ipiv[n];
+        }
+        rh[n] = n > 0 ? 1.0 / h[n] : 0.0;
+        rd[n] = 1.0 / d[n];
+    }
+    for (int n = t; n < F_new; n += nt) {
+        const int k = kk[n];
+        const double w = p.w[n], wm = spline == 0 ? (w - 1) : (1 - w), hk2 = h[k] * h[k];
+        ev[4 * n] = w;
+        ev[4 * n + 1] = 1 - w;
+        ev[4 * n + 2] = hk2 * (w * w * w - w);
+        ev[4 * n + 3] = hk2 * (wm * wm * wm - wm);
+    }
+    if (t == 0) {   // end conditions: third divided differences at both ends
+        ends[0] = 1.0 / (h[3] + h[2]);
+        ends[1] = 1.0 / (h[2] + h[1]);
+        ends[2] = 1.0 / (h[3] + h[2] + h[1]);
+        ends[3] = h[1] * h[1];
+        ends[4] = 1.0 / (h[F - 1] + h[F - 2]);
+        ends[5] = 1.0 / (h[F - 2] + h[F - 3]);
+        ends[6] = 1.0 / (h[F - 1] + h[F - 2] + h[F - 3]);
+        ends[7] = -(h[F - 1] * h[F - 1]);
+    }
 }
 
 template <class T>
@@ -1265,52 +1394,124 @@ __global__ void __launch_bounds__(NT) k_redist_linear(const T *f, T *fnew, long 
 
 // Cubic resample (computeDeltaX/Y + gtsv + generateNewFramesCubic,
 // interpolation.cu:292-402), one thread per real of a site: builds the
-// right-hand side in the strided scratch, solves with the shared factors,
-// evaluates the new images.  Double throughout.
-template <class T>
-__global__ void __launch_bounds__(NT) k_redist_cubic(const T *f, T *fnew, double *sig, long reals, int F, int F_new,
-                                                     int spline, RedistPlan p)
+// right-hand side, solves with the shared factors, evaluates the new
+// images.  The arithmetic type C is that of the fields: float for FP32
+// fields, as the reference's FP32 build computes its spline, and double for
+// FP64 ones.  Every division is a product with a reciprocal the plan made
+// once, and the per-image evaluation weights come from the plan too, so a
+// real costs about ten multiply-adds per image.  SG(n), the thread's column
+// of the solution, lives in shared memory ([n][thread]) or, for strings too
+// long for that, in the strided global scratch.
+
+// Uniform data of one resample in type C, staged in shared memory per block.
+template <class C>
+struct CubicUniform {
+    C *rh, *rd, *dl, *du, *du2, *ev, *ends;
+    int *ipiv, *kk;
+};
+
+template <class C>
+__host__ __device__ inline size_t cubic_uniform_bytes(int F, int F_new)
 {
-    for (long e = blockIdx.x * (long)NT + threadIdx.x; e < reals; e += (long)gridDim.x * NT) {
-        const double *h = p.h;
-#define FV(n) ((double)f[(long)(n) * reals + e])
-#define SG(n) sig[(long)(n) * reals + e]
-        // first divided differences D[n] = (f_n - f_{n-1}) / h_n, n >= 1
-        const double D1 = (FV(1) - FV(0)) / h[1], D2 = (FV(2) - FV(1)) / h[2], D3 = (FV(3) - FV(2)) / h[3];
-        const double Dm1 = (FV(F - 1) - FV(F - 2)) / h[F - 1], Dm2 = (FV(F - 2) - FV(F - 3)) / h[F - 2];
-        const double Dm3 = (FV(F - 3) - FV(F - 4)) / h[F - 3];
-        const double d3s = ((D3 - D2) / (h[3] + h[2]) - (D2 - D1) / (h[2] + h[1])) / (h[3] + h[2] + h[1]);
-        const double d3e = ((Dm1 - Dm2) / (h[F - 1] + h[F - 2]) - (Dm2 - Dm3) / (h[F - 2] + h[F - 3])) /
-                           (h[F - 1] + h[F - 2] + h[F - 3]);
-        double Dn = D1;
-        for (int n = 1; n < F - 1; ++n) {
-            const double Dn1 = (FV(n + 1) - FV(n)) / h[n + 1];
-            SG(n) = Dn1 - Dn;
-            Dn = Dn1;
+    return ((size_t)(5 * F + 4 * F_new + 8) * sizeof(C) + (size_t)(F + F_new) * sizeof(int) + 15) & ~(size_t)15;
+}
+
+template <class C>
+__device__ __forceinline__ CubicUniform<C> stage_cubic_uniform(const RedistPlan &p, int F, int F_new, char *sm)
+{
+    CubicUniform<C> u;
+    u.rh = reinterpret_cast<C *>(sm);
+    u.rd = u.rh + F;
+    u.dl = u.rd + F;
+    u.du = u.dl + F;
+    u.du2 = u.du + F;
+    u.ev = u.du2 + F;
+    u.ends = u.ev + 4 * F_new;
+    u.ipiv = reinterpret_cast<int *>(u.ends + 8);
+    u.kk = u.ipiv + F;
+    const double *rh = p.aux, *rd = rh + F, *ev = rd + F, *ends = ev + 4 * F_new;
+    for (int n = threadIdx.x; n < F; n += blockDim.x) {
+        u.rh[n] = (C)rh[n];
+        u.rd[n] = (C)rd[n];
+        u.dl[n] = (C)p.dl[n];
+        u.du[n] = (C)p.du[n];
+        u.du2[n] = (C)p.du2[n];
+        u.ipiv[n] = p.ipiv[n];
+    }
+    for (int n = threadIdx.x; n < 4 * F_new; n += blockDim.x) u.ev[n] = (C)ev[n];
+    for (int n = threadIdx.x; n < F_new; n += blockDim.x) u.kk[n] = p.k[n];
+    if (threadIdx.x < 8) u.ends[threadIdx.x] = (C)ends[threadIdx.x];
+    __syncthreads();
+    return u;
+}
+
+template <class T, class C, bool SMEM>
+__device__ __forceinline__ void redist_cubic_real(const T *f, T *fnew, C *sig, long reals, long e, int F, int F_new,
+                                                  const CubicUniform<C> &u)
+{
+#define FV(n) ((C)f[(long)(n) * reals + e])
+#define SG(n) (SMEM ? sig[(n) * (int)blockDim.x + (int)threadIdx.x] : sig[(long)(n) * reals + e])
+    // first divided differences D[n] = (f_n - f_{n-1}) / h_n, n >= 1
+    const C D1 = (FV(1) - FV(0)) * u.rh[1], D2 = (FV(2) - FV(1)) * u.rh[2], D3 = (FV(3) - FV(2)) * u.rh[3];
+    const C Dm1 = (FV(F - 1) - FV(F - 2)) * u.rh[F - 1], Dm2 = (FV(F - 2) - FV(F - 3)) * u.rh[F - 2];
+    const C Dm3 = (FV(F - 3) - FV(F - 4)) * u.rh[F - 3];
+    const C d3s = ((D3 - D2) * u.ends[0] - (D2 - D1) * u.ends[1]) * u.ends[2];
+    const C d3e = ((Dm1 - Dm2) * u.ends[4] - (Dm2 - Dm3) * u.ends[5]) * u.ends[6];
+    C Dn = D1;
+    for (int n = 1; n < F - 1; ++n) {
+        const C Dn1 = (FV(n + 1) - FV(n)) * u.rh[n + 1];
+        SG(n) = Dn1 - Dn;
+        Dn = Dn1;
+    }
+    SG(0) = u.ends[3] * d3s;
+    SG(F - 1) = u.ends[7] * d3e;
+    // forward elimination with the recorded pivots
+    for (int q = 0; q < F - 1; ++q) {
+        const C bk = SG(q), bk1 = SG(q + 1);
+        if (u.ipiv[q]) {
+            SG(q) = bk1;
+            SG(q + 1) = bk - u.dl[q + 1] * bk1;
+        } else {
+            SG(q + 1) = bk1 - u.dl[q + 1] * bk;
         }
-        SG(0) = h[1] * h[1] * d3s;
-        SG(F - 1) = -(h[F - 1] * h[F - 1]) * d3e;
-        // forward elimination with the recorded pivots
-        for (int q = 0; q < F - 1; ++q) {
-            const double bk = SG(q), bk1 = SG(q + 1);
-            if (p.ipiv[q]) {
-                SG(q) = bk1;
-                SG(q + 1) = bk - p.dl[q + 1] * bk1;
-            } else {
-                SG(q + 1) = bk1 - p.dl[q + 1] * bk;
-            }
-        }
-        SG(F - 1) = SG(F - 1) / p.d[F - 1];
-        SG(F - 2) = (SG(F - 2) - p.du[F - 2] * SG(F - 1)) / p.d[F - 2];
-        for (int q = F - 3; q >= 0; --q) SG(q) = (SG(q) - p.du[q] * SG(q + 1) - p.du2[q] * SG(q + 2)) / p.d[q];
-        for (int n = 0; n < F_new; ++n) {
-            const int k = p.k[n];
-            const double w = p.w[n], wm = spline == 0 ? (w - 1) : (1 - w), hk2 = h[k] * h[k];
-            fnew[(long)n * reals + e] =
-                (T)(w * FV(k) + (1 - w) * FV(k - 1) + hk2 * ((w * w * w - w) * SG(k) + (wm * wm * wm - wm) * SG(k - 1)));
-        }
+    }
+    SG(F - 1) = SG(F - 1) * u.rd[F - 1];
+    SG(F - 2) = (SG(F - 2) - u.du[F - 2] * SG(F - 1)) * u.rd[F - 2];
+    for (int q = F - 3; q >= 0; --q) SG(q) = (SG(q) - u.du[q] * SG(q + 1) - u.du2[q] * SG(q + 2)) * u.rd[q];
+    for (int n = 0; n < F_new; ++n) {
+        const int k = u.kk[n];
+        const C *c = u.ev + 4 * n;
+        fnew[(long)n * reals + e] = (T)(c[0] * FV(k) + c[1] * FV(k - 1) + c[2] * SG(k) + c[3] * SG(k - 1));
+    }
 #undef FV
 #undef SG
+}
+
+// Arithmetic type of the cubic resample for fields of type T.
+template <class T> using cubic_t = T;
+
+template <class T>
+__global__ void __launch_bounds__(NT) k_redist_cubic(const T *f, T *fnew, cubic_t<T> *sig, long reals, int F,
+                                                     int F_new, RedistPlan p)
+{
+    extern __shared__ __align__(16) char cubic_sm[];
+    const CubicUniform<cubic_t<T>> u = stage_cubic_uniform<cubic_t<T>>(p, F, F_new, cubic_sm);
+    for (long e = blockIdx.x * (long)NT + threadIdx.x; e < reals; e += (long)gridDim.x * NT)
+        redist_cubic_real<T, cubic_t<T>, false>(f, fnew, sig, reals, e, F, F_new, u);
+}
+
+// Shared-memory columns: after the uniform data, F * blockDim.x values;
+// each thread owns one column, so no barrier is needed after the staging.
+template <class T>
+__global__ void __launch_bounds__(128) k_redist_cubic_s(const T *f, T *fnew, long reals, int F, int F_new,
+                                                        RedistPlan p)
+{
+    extern __shared__ __align__(16) char cubic_sm[];
+    const CubicUniform<cubic_t<T>> u = stage_cubic_uniform<cubic_t<T>>(p, F, F_new, cubic_sm);
+    cubic_t<T> *cols = reinterpret_cast<cubic_t<T> *>(cubic_sm + cubic_uniform_bytes<cubic_t<T>>(F, F_new));
+    for (long e0 = blockIdx.x * (long)blockDim.x; e0 < reals; e0 += (long)gridDim.x * blockDim.x) {
+        const long e = e0 + threadIdx.x;
+        if (e < reals) redist_cubic_real<T, cubic_t<T>, true>(f, fnew, cols, reals, e, F, F_new, u);
     }
 }
 
@@ -1553,15 +1754,22 @@ cudaError_t launch_arc_length(int precision, const void *const *fields, const in
                               double *part, double *s, cudaStream_t st)
 {
     const int nb = (int)((sites + (long)NT * ARC_SPT - 1) / ((long)NT * ARC_SPT));
+    // image chunks: about 1024 blocks in all (4 per SM at least), each chunk a run of images
+    int chunks = (1024 + nb - 1) / nb;
+    chunks = chunks < 1 ? 1 : (chunks > F ? F : chunks);
+    const int per_chunk = (F + chunks - 1) / chunks;
+    chunks = (F + per_chunk - 1) / per_chunk;
+    const dim3 grid(nb, chunks);
     const void *f[3] = {nf > 0 ? fields[0] : nullptr, nf > 1 ? fields[1] : nullptr, nf > 2 ? fields[2] : nullptr};
     const int w[3] = {nf > 0 ? width[0] : 0, nf > 1 ? width[1] : 0, nf > 2 ? width[2] : 0};
     if (precision == 1)
-        k_arc_partial<double><<<nb, NT, 0, st>>>((const double *)f[0], (const double *)f[1], (const double *)f[2],
-                                                 w[0], w[1], w[2], sites, F, part);
+        k_arc_partial<double><<<grid, NT, 0, st>>>((const double *)f[0], (const double *)f[1], (const double *)f[2],
+                                                   w[0], w[1], w[2], sites, F, per_chunk, part);
     else
-        k_arc_partial<float><<<nb, NT, 0, st>>>((const float *)f[0], (const float *)f[1], (const float *)f[2], w[0],
-                                                w[1], w[2], sites, F, part);
-    k_arc_finish<<<1, NT, 0, st>>>(part, nb, F, s);
+        k_arc_partial<float><<<grid, NT, 0, st>>>((const float *)f[0], (const float *)f[1], (const float *)f[2],
+                                                  w[0], w[1], w[2], sites, F, per_chunk, part);
+    k_arc_sum<<<F, NT, 0, st>>>(part, nb, s);
+    k_arc_cumulate<<<1, NT, 0, st>>>(F, s);
     return cudaGetLastError();
 }
 
@@ -1601,7 +1809,9 @@ cudaError_t launch_winding(int precision, const void *psi, int nx, int ny, int F
 cudaError_t launch_redist_plan(const double *s, int F, int F_new, int cubic, int spline, const RedistPlan &p,
                                cudaStream_t st)
 {
-    k_redist_plan<<<1, 32, 0, st>>>(s, F, F_new, cubic, spline, p);
+    const size_t sm = redist_plan_smem(F, F_new);
+    const int use_smem = sm <= 48 * 1024;
+    k_redist_plan<<<1, 32, use_smem ? sm : 0, st>>>(s, F, F_new, cubic, spline, p, use_smem);
     return cudaGetLastError();
 }
 
@@ -1621,13 +1831,44 @@ cudaError_t launch_redist_linear(int precision, const void *f, void *fnew, long 
 cudaError_t launch_redist_cubic(int precision, const void *f, void *fnew, void *sigma, long pairs, int F, int F_new,
                                 int spline, const RedistPlan &p, cudaStream_t st)
 {
+    (void)spline;   // folded into the plan's evaluation weights
     const long reals = 2 * pairs;
+    const size_t cs = precision == 1 ? sizeof(double) : sizeof(float);
+    const size_t ub = precision == 1 ? cubic_uniform_bytes<double>(F, F_new) : cubic_uniform_bytes<float>(F, F_new);
+    // shared-memory columns: 32 KB of them per block where F allows (128 threads, 64 or
+    // 32), up to 200 KB in all at 32 threads; longer strings use the global scratch
+    int tpb = 128;
+    while (tpb > 32 && (size_t)tpb * F * cs > 32 * 1024) tpb >>= 1;
+    const size_t sm = ub + (size_t)tpb * F * cs;
+    cudaError_t e = cudaSuccess;
+    if (sm <= 200 * 1024) {
+        const long blocks = (reals + tpb - 1) / tpb;
+        const int grid = (int)(blocks < 152 * 32 ? blocks : 152 * 32);
+        if (precision == 1) {
+            if (sm > 48 * 1024)
+                e = cudaFuncSetAttribute(k_redist_cubic_s<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+            if (e != cudaSuccess) return e;
+            k_redist_cubic_s<double><<<grid, tpb, sm, st>>>((const double *)f, (double *)fnew, reals, F, F_new, p);
+        } else {
+            if (sm > 48 * 1024)
+                e = cudaFuncSetAttribute(k_redist_cubic_s<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+            if (e != cudaSuccess) return e;
+            k_redist_cubic_s<float><<<grid, tpb, sm, st>>>((const float *)f, (float *)fnew, reals, F, F_new, p);
+        }
+        return cudaGetLastError();
+    }
+    if (ub > 200 * 1024) return cudaErrorInvalidValue;   // more than about 2,800 images
+    if (ub > 48 * 1024)
+        e = precision == 1
+                ? cudaFuncSetAttribute(k_redist_cubic<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ub)
+                : cudaFuncSetAttribute(k_redist_cubic<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ub);
+    if (e != cudaSuccess) return e;
     if (precision == 1)
-        k_redist_cubic<double><<<grid_for(reals), NT, 0, st>>>((const double *)f, (double *)fnew, (double *)sigma,
-                                                               reals, F, F_new, spline, p);
+        k_redist_cubic<double><<<grid_for(reals), NT, ub, st>>>((const double *)f, (double *)fnew, (double *)sigma,
+                                                                reals, F, F_new, p);
     else
-        k_redist_cubic<float><<<grid_for(reals), NT, 0, st>>>((const float *)f, (float *)fnew, (double *)sigma, reals,
-                                                              F, F_new, spline, p);
+        k_redist_cubic<float><<<grid_for(reals), NT, ub, st>>>((const float *)f, (float *)fnew, (float *)sigma, reals,
+                                                               F, F_new, p);
     return cudaGetLastError();
 }
 

@@ -102,7 +102,12 @@ struct RedistPlan {
     double *dl, *d, *du, *du2;   // [F]
     int *ipiv;       // [F]
     int *status;
+    // cubic: 1 / h [F], 1 / d [F], per output image {w, 1 - w, h_k^2 (w^3 - w),
+    // h_k^2 (wm^3 - wm)} [4 F_new], the end conditions' factors [8]
+    double *aux;
 };
+// doubles of RedistPlan::aux for a plan of capacity `cap` images
+inline size_t redist_aux_size(int cap) { return (size_t)6 * cap + 8; }
 cudaError_t launch_redist_plan(const double *s, int F, int F_new, int cubic, int spline, const RedistPlan &p,
                                cudaStream_t st);
 // Linear resample of `pairs` interleaved pairs per image (precision real).

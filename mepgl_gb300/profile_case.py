@@ -12,6 +12,13 @@ before the one it records.  Prints the per-pass CUDA-event times.
 each, which a build with fused FP32 steps runs as two persistent launches
 (a capture with ``-k regex:k_nlcg_s -s 1 -c 1`` records the second); prints
 the second call's milliseconds per step.
+
+``--reparam linear|cubic``: instead, ``--steps`` reparametrization events
+(``mepgl_redistribute`` with the image count kept: arc lengths of the fields
+and of B, J, the plan, one resample launch per field, the status check), one
+warm-up event first; prints milliseconds per event and the HBM rate over its
+algorithmic bytes: x read three times (two arc lengths' sources and the
+resample) and written once, B and J written and read once, the masks once.
 """
 from __future__ import annotations
 
@@ -28,12 +35,33 @@ def main(argv=None):
     ap.add_argument("--fp64-arith", choices=("native", "paired"), default="native",
                     help="FP64 NLCG passes in double or in float-float pairs")
     ap.add_argument("--fused", action="store_true", help="whole nlcg_steps calls (one launch each when fused)")
+    ap.add_argument("--reparam", choices=("linear", "cubic"), help="time reparametrization events instead")
     a = ap.parse_args(argv)
     from . import native, workloads
     prob, st = workloads.config2(n=a.n, images=a.images)
     ctx = native.StringContext(prob, st.n_images, a.precision, use_graphs=0, line_polynomial=native.POLY_EXACT,
                                fp64_arith=native.FP64_PAIRED if a.fp64_arith == "paired" else native.FP64_NATIVE)
     ctx.set_state(st)
+    if a.reparam:
+        import torch
+        kind = native.REDIST_LINEAR if a.reparam == "linear" else native.REDIST_CUBIC
+        ctx.nlcg_steps(2)
+        ctx.redistribute(kind)
+        ctx.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(a.steps):
+            ctx.redistribute(kind)
+        e1.record()
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / a.steps
+        rs = 4 if a.precision == "fp32" else 8
+        units = a.n * a.n * a.images
+        per_unit = 4 * 6 * rs + 2 * 5 * rs + 2   # 4S + B, J (5 reals) out and in + masks
+        print(json.dumps({"precision": a.precision, "reparam": a.reparam, "n": a.n, "images": a.images,
+                          "events": a.steps, "ms_per_event": ms, "bytes_per_event": units * per_unit,
+                          "gbs": units * per_unit / ms / 1e6}))
+        return
     if a.fused:
         import time
         ctx.nlcg_steps(a.steps)

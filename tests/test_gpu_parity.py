@@ -85,6 +85,25 @@ def test_redistribution_golden(golden, cubic):
         assert relmax(got, want) < 1e-11, fnew
 
 
+@pytest.mark.parametrize("cubic", [False, True])
+def test_redistribution_golden_fp32(golden, cubic):
+    """FP32 fields: the linear resample in float, the cubic one in float
+    arithmetic as the reference's FP32 build computes its spline (plan and
+    factors in double); against the reference kernels' FP64 goldens."""
+    prob, st, z = golden
+    F = st.n_images
+    for fnew in (F, F + 3):
+        c = make(prob, st, "fp32")
+        if cubic:
+            c.redistribute_cubic(fnew)
+        else:
+            c.redistribute_linear(fnew)
+        got = c.get_state().psi_1
+        assert got.shape[0] == fnew
+        want = z[f"{'cubic' if cubic else 'linear'}_{fnew}"]
+        assert relmax(got, want) < 2e-5, fnew
+
+
 def test_loop_golden(golden):
     """Whole runs of the reference's loop() in each mode, compat options."""
     prob, st, z = golden
