@@ -987,57 +987,65 @@ __global__ void __launch_bounds__(NT) k_apply_update(vec2_t<T> *x, const vec2_t<
 }
 
 // Arc length: squared image-to-image distance over every site (no mask, no
-// dx^2; interpolation.cu:39-92).  Block (bx, by) covers sites
-// [bx * NT * ARC_SPT, ...) and the images of chunk by; it reads the image
-// before its chunk first as the previous one, so each (image, site block)
-// partial is the sum one walk through all images would give.  The chunks
-// spread a string of few sites over enough blocks to fill the GPU.
+// dx^2; interpolation.cu:39-92).  Block (bx, n) covers sites
+// [bx * NT * ARC_SPT, ...) of image n against image n - 1: each thread issues
+// all its loads of both images, then adds them in the fixed order (site,
+// field, component), so each (image, site block) partial is the same sum
+// one walk through the images would give.
 constexpr int ARC_SPT = 4;
 
 template <class T>
-__global__ void __launch_bounds__(NT) k_arc_partial(const T *f0, const T *f1, const T *f2, int w0, int w1, int w2,
-                                                    long sites, int F, int per_chunk, double *part)
+__global__ void __launch_bounds__(NT) k_arc_partial(const T *__restrict__ f0, const T *__restrict__ f1,
+                                                    const T *__restrict__ f2, int w0, int w1, int w2, long sites,
+                                                    double *part)
 {
     __shared__ double red[NT / 32];
     const T *fs[3] = {f0, f1, f2};
     const int ws[3] = {w0, w1, w2};
-    T prev[3][ARC_SPT][2];
+    const int n = blockIdx.y;
     const long base = (long)blockIdx.x * NT * ARC_SPT + threadIdx.x;
-    const int n0 = (int)blockIdx.y * per_chunk, n1 = n0 + per_chunk < F ? n0 + per_chunk : F;
-    for (int n = n0 > 0 ? n0 - 1 : 0; n < n1; ++n) {
-        T acc = 0;
+    T acc = 0;
+    if (n > 0) {
+        T cur[3][ARC_SPT][2], prv[3][ARC_SPT][2];
+#pragma unroll
+        for (int f = 0; f < 3; ++f)
+#pragma unroll
+            for (int q = 0; q < ARC_SPT; ++q) {
+                const long s = base + (long)q * NT;
+                cur[f][q][0] = cur[f][q][1] = prv[f][q][0] = prv[f][q][1] = 0;
+                if (!fs[f] || s >= sites) continue;
+                if (ws[f] == 2) {   // one vector load per site and image
+                    const vec2_t<T> *v = reinterpret_cast<const vec2_t<T> *>(fs[f]);
+                    const vec2_t<T> c = v[(long)n * sites + s], p = v[(long)(n - 1) * sites + s];
+                    cur[f][q][0] = c.x;
+                    cur[f][q][1] = c.y;
+                    prv[f][q][0] = p.x;
+                    prv[f][q][1] = p.y;
+                } else {
+                    cur[f][q][0] = fs[f][(long)n * sites + s];
+                    prv[f][q][0] = fs[f][(long)(n - 1) * sites + s];
+                }
+            }
 #pragma unroll
         for (int q = 0; q < ARC_SPT; ++q) {
-            const long s = base + (long)q * NT;
-            if (s >= sites) continue;
+            if (base + (long)q * NT >= sites) continue;
             T d2 = 0;
 #pragma unroll
             for (int f = 0; f < 3; ++f) {
                 if (!fs[f]) continue;
-                T v[2];
-                if (ws[f] == 2) {   // one vector load per site
-                    const vec2_t<T> p2 = reinterpret_cast<const vec2_t<T> *>(fs[f])[(long)n * sites + s];
-                    v[0] = p2.x;
-                    v[1] = p2.y;
-                } else {
-                    v[0] = fs[f][(long)n * sites + s];
-                    v[1] = 0;
-                }
 #pragma unroll
                 for (int w = 0; w < 2; ++w) {
                     if (w >= ws[f]) continue;
-                    if (n > 0 && n >= n0) d2 += (v[w] - prev[f][q][w]) * (v[w] - prev[f][q][w]);
-                    prev[f][q][w] = v[w];
+                    d2 += (cur[f][q][w] - prv[f][q][w]) * (cur[f][q][w] - prv[f][q][w]);
                 }
             }
             acc += d2;
         }
-        if (n < n0) continue;   // the previous image of the chunk: loaded, not summed (block-uniform)
-        const T vv[1] = {acc};
-        double tot[1];
-        block_sum<1>(vv, tot, red);
-        if (threadIdx.x == 0) part[(size_t)n * gridDim.x + blockIdx.x] = tot[0];
     }
+    const T vv[1] = {acc};
+    double tot[1];
+    block_sum<1>(vv, tot, red);
+    if (threadIdx.x == 0) part[(size_t)n * gridDim.x + blockIdx.x] = tot[0];
 }
 
 // ------------------------------------------------------- initial strings
@@ -1446,22 +1454,37 @@ __device__ __forceinline__ CubicUniform<C> stage_cubic_uniform(const RedistPlan 
 }
 
 template <class T, class C, bool SMEM>
-__device__ __forceinline__ void redist_cubic_real(const T *f, T *fnew, C *sig, long reals, long e, int F, int F_new,
-                                                  const CubicUniform<C> &u)
+__device__ __forceinline__ void redist_cubic_real(const T *__restrict__ f, T *__restrict__ fnew, C *sig, long reals,
+                                                  long e, int F, int F_new, const CubicUniform<C> &u)
 {
 #define FV(n) ((C)f[(long)(n) * reals + e])
 #define SG(n) (SMEM ? sig[(n) * (int)blockDim.x + (int)threadIdx.x] : sig[(long)(n) * reals + e])
-    // first divided differences D[n] = (f_n - f_{n-1}) / h_n, n >= 1
-    const C D1 = (FV(1) - FV(0)) * u.rh[1], D2 = (FV(2) - FV(1)) * u.rh[2], D3 = (FV(3) - FV(2)) * u.rh[3];
-    const C Dm1 = (FV(F - 1) - FV(F - 2)) * u.rh[F - 1], Dm2 = (FV(F - 2) - FV(F - 3)) * u.rh[F - 2];
-    const C Dm3 = (FV(F - 3) - FV(F - 4)) * u.rh[F - 3];
+    // the column of f into the solution's storage, eight loads in flight at a time
+    {
+        int n = 0;
+        for (; n + 8 <= F; n += 8) {
+            C v[8];
+#pragma unroll
+            for (int i = 0; i < 8; ++i) v[i] = FV(n + i);
+#pragma unroll
+            for (int i = 0; i < 8; ++i) SG(n + i) = v[i];
+        }
+        for (; n < F; ++n) SG(n) = FV(n);
+    }
+    // first divided differences D[n] = (f_n - f_{n-1}) / h_n, n >= 1; the
+    // right-hand side overwrites f in place (f_n is carried in fp)
+    const C D1 = (SG(1) - SG(0)) * u.rh[1], D2 = (SG(2) - SG(1)) * u.rh[2], D3 = (SG(3) - SG(2)) * u.rh[3];
+    const C Dm1 = (SG(F - 1) - SG(F - 2)) * u.rh[F - 1], Dm2 = (SG(F - 2) - SG(F - 3)) * u.rh[F - 2];
+    const C Dm3 = (SG(F - 3) - SG(F - 4)) * u.rh[F - 3];
     const C d3s = ((D3 - D2) * u.ends[0] - (D2 - D1) * u.ends[1]) * u.ends[2];
     const C d3e = ((Dm1 - Dm2) * u.ends[4] - (Dm2 - Dm3) * u.ends[5]) * u.ends[6];
-    C Dn = D1;
+    C Dn = D1, fp = SG(1);
     for (int n = 1; n < F - 1; ++n) {
-        const C Dn1 = (FV(n + 1) - FV(n)) * u.rh[n + 1];
+        const C fn1 = SG(n + 1);
+        const C Dn1 = (fn1 - fp) * u.rh[n + 1];
         SG(n) = Dn1 - Dn;
         Dn = Dn1;
+        fp = fn1;
     }
     SG(0) = u.ends[3] * d3s;
     SG(F - 1) = u.ends[7] * d3e;
@@ -1478,7 +1501,24 @@ __device__ __forceinline__ void redist_cubic_real(const T *f, T *fnew, C *sig, l
     SG(F - 1) = SG(F - 1) * u.rd[F - 1];
     SG(F - 2) = (SG(F - 2) - u.du[F - 2] * SG(F - 1)) * u.rd[F - 2];
     for (int q = F - 3; q >= 0; --q) SG(q) = (SG(q) - u.du[q] * SG(q + 1) - u.du2[q] * SG(q + 2)) * u.rd[q];
-    for (int n = 0; n < F_new; ++n) {
+    // new images: f re-read (from L2), four outputs' loads in flight at a time
+    int n = 0;
+    for (; n + 4 <= F_new; n += 4) {
+        C a[4], b[4];
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+            const int k = u.kk[n + i];
+            a[i] = FV(k);
+            b[i] = FV(k - 1);
+        }
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+            const int k = u.kk[n + i];
+            const C *c = u.ev + 4 * (n + i);
+            fnew[(long)(n + i) * reals + e] = (T)(c[0] * a[i] + c[1] * b[i] + c[2] * SG(k) + c[3] * SG(k - 1));
+        }
+    }
+    for (; n < F_new; ++n) {
         const int k = u.kk[n];
         const C *c = u.ev + 4 * n;
         fnew[(long)n * reals + e] = (T)(c[0] * FV(k) + c[1] * FV(k - 1) + c[2] * SG(k) + c[3] * SG(k - 1));
@@ -1754,20 +1794,15 @@ cudaError_t launch_arc_length(int precision, const void *const *fields, const in
                               double *part, double *s, cudaStream_t st)
 {
     const int nb = (int)((sites + (long)NT * ARC_SPT - 1) / ((long)NT * ARC_SPT));
-    // image chunks: about 1024 blocks in all (4 per SM at least), each chunk a run of images
-    int chunks = (1024 + nb - 1) / nb;
-    chunks = chunks < 1 ? 1 : (chunks > F ? F : chunks);
-    const int per_chunk = (F + chunks - 1) / chunks;
-    chunks = (F + per_chunk - 1) / per_chunk;
-    const dim3 grid(nb, chunks);
+    const dim3 grid(nb, F);
     const void *f[3] = {nf > 0 ? fields[0] : nullptr, nf > 1 ? fields[1] : nullptr, nf > 2 ? fields[2] : nullptr};
     const int w[3] = {nf > 0 ? width[0] : 0, nf > 1 ? width[1] : 0, nf > 2 ? width[2] : 0};
     if (precision == 1)
         k_arc_partial<double><<<grid, NT, 0, st>>>((const double *)f[0], (const double *)f[1], (const double *)f[2],
-                                                   w[0], w[1], w[2], sites, F, per_chunk, part);
+                                                   w[0], w[1], w[2], sites, part);
     else
         k_arc_partial<float><<<grid, NT, 0, st>>>((const float *)f[0], (const float *)f[1], (const float *)f[2],
-                                                  w[0], w[1], w[2], sites, F, per_chunk, part);
+                                                  w[0], w[1], w[2], sites, part);
     k_arc_sum<<<F, NT, 0, st>>>(part, nb, s);
     k_arc_cumulate<<<1, NT, 0, st>>>(F, s);
     return cudaGetLastError();
