@@ -1386,17 +1386,28 @@ __global__ void k_redist_plan(const double *s_in, int F, int F_new, int cubic, i
     }
 }
 
-template <class T>
-__global__ void __launch_bounds__(NT) k_redist_linear(const T *f, T *fnew, long reals, int F_new, const int *kk,
-                                                      const double *ww)
+// Linear resample: block row blockIdx.y is output image n, the blocks of the
+// row stride over its reals, V of them per access (V = 4 for float fields
+// whose image size allows 16-byte vectors, 2 for double, else 1).
+template <class T, int V>
+__global__ void __launch_bounds__(NT) k_redist_linear(const T *f, T *fnew, long reals, const int *kk, const double *ww)
 {
-    const long total = reals * F_new;
-    for (long e = blockIdx.x * (long)NT + threadIdx.x; e < total; e += (long)gridDim.x * NT) {
-        const int n = (int)(e / reals);
-        const long r = e - (long)n * reals;
-        const int k = kk[n];
-        const T w = (T)ww[n];
-        fnew[e] = w * f[(long)k * reals + r] + (1 - w) * f[(long)(k - 1) * reals + r];
+    using Vec = typename std::conditional<V == 4, float4, typename std::conditional<V == 2, double2, T>::type>::type;
+    const int n = blockIdx.y;
+    const int k = kk[n];
+    const T w = (T)ww[n];
+    const Vec *a = reinterpret_cast<const Vec *>(f + (long)k * reals);
+    const Vec *b = reinterpret_cast<const Vec *>(f + (long)(k - 1) * reals);
+    Vec *o = reinterpret_cast<Vec *>(fnew + (long)n * reals);
+    const long nv = reals / V;
+    for (long i = blockIdx.x * (long)NT + threadIdx.x; i < nv; i += (long)gridDim.x * NT) {
+        const Vec va = a[i], vb = b[i];
+        const T *pa = reinterpret_cast<const T *>(&va), *pb = reinterpret_cast<const T *>(&vb);
+        Vec vo;
+        T *po = reinterpret_cast<T *>(&vo);
+#pragma unroll
+        for (int c = 0; c < V; ++c) po[c] = w * pa[c] + (1 - w) * pb[c];
+        o[i] = vo;
     }
 }
 
@@ -1854,12 +1865,19 @@ cudaError_t launch_redist_linear(int precision, const void *f, void *fnew, long 
                                  cudaStream_t st)
 {
     const long reals = 2 * pairs;
-    if (precision == 1)
-        k_redist_linear<double><<<grid_for(reals * F_new), NT, 0, st>>>((const double *)f, (double *)fnew, reals,
-                                                                        F_new, p.k, p.w);
-    else
-        k_redist_linear<float><<<grid_for(reals * F_new), NT, 0, st>>>((const float *)f, (float *)fnew, reals, F_new,
-                                                                       p.k, p.w);
+    // blocks per output image: about four waves of the GPU in all
+    auto grid = [&](long nv) {
+        long bx = (nv + NT - 1) / NT, cap = (152L * 8 * 4 + F_new - 1) / F_new;
+        bx = bx < cap ? bx : cap;
+        return dim3((unsigned)(bx < 1 ? 1 : bx), (unsigned)F_new);
+    };
+    if (precision == 1) {
+        k_redist_linear<double, 2><<<grid(reals / 2), NT, 0, st>>>((const double *)f, (double *)fnew, reals, p.k, p.w);
+    } else if (reals % 4 == 0) {
+        k_redist_linear<float, 4><<<grid(reals / 4), NT, 0, st>>>((const float *)f, (float *)fnew, reals, p.k, p.w);
+    } else {
+        k_redist_linear<float, 1><<<grid(reals), NT, 0, st>>>((const float *)f, (float *)fnew, reals, p.k, p.w);
+    }
     return cudaGetLastError();
 }
 
