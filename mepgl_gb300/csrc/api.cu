@@ -60,7 +60,7 @@ struct mepgl_ctx {
     double *ds = nullptr, *ds_jb = nullptr;   // arc lengths of string 0
     RedistPlan plan{};
     int plan_cap = 0;
-    void *cubic_scratch = nullptr;   // 2 * F * sites doubles, allocated on first cubic use
+    void *cubic_scratch = nullptr;   // cubic resample columns of strings too long for shared memory
     size_t cubic_cap = 0;
     int xi = 0, di = 0;           // current x / d buffers
     bool pending = false;         // an NLCG update not yet applied to x
@@ -625,7 +625,7 @@ mepgl_status redistribute(mepgl_ctx *c, int kind, int F_new)
     const size_t rs = real_size(c->precision);
     for (int f = 0; f < 1 + c->ncomp; ++f) CK(c, cudaMalloc(&target[f], (size_t)F_new * s.M() * 2 * rs));
     if (cubic) {
-        st = ensure_cubic_scratch(c, (size_t)2 * F * s.M() * sizeof(double));
+        st = ensure_cubic_scratch(c, redist_cubic_scratch_bytes(c->precision, s.M(), F, F_new));
         if (st != MEPGL_OK) return st;
     }
     for (int f = 0; f < 1 + c->ncomp; ++f) {
@@ -675,7 +675,7 @@ mepgl_status redistribute_into_spare(mepgl_ctx *c, int si, int kind)
     mepgl_status st = arc_length(c, si, MEPGL_METRIC_FIELDS, &sp);
     if (st == MEPGL_OK) st = arc_length(c, si, MEPGL_METRIC_JB, &sp);
     if (st == MEPGL_OK) st = ensure_plan(c, F, F);
-    if (st == MEPGL_OK && cubic) st = ensure_cubic_scratch(c, (size_t)2 * F * s.M() * sizeof(double));
+    if (st == MEPGL_OK && cubic) st = ensure_cubic_scratch(c, redist_cubic_scratch_bytes(c->precision, s.M(), F, F));
     if (st != MEPGL_OK) return st;
     double *s_use = c->opt.metric == MEPGL_METRIC_FIELDS ? c->ds : c->ds_jb;
     CK(c, launch_redist_plan(s_use, F, F, cubic, c->opt.spline, c->plan, c->stream));

@@ -1881,20 +1881,40 @@ cudaError_t launch_redist_linear(int precision, const void *f, void *fnew, long 
     return cudaGetLastError();
 }
 
+// Shape of a cubic resample launch: threads per block and dynamic shared
+// memory of the shared-memory form (32 KB of columns per block where F
+// allows: 128 threads, 64 or 32; up to 200 KB in all at 32 threads), or
+// sm = 0 when the string is too long for it and the global scratch is used.
+static void cubic_shape(int precision, int F, int F_new, int *tpb_out, size_t *sm_out)
+{
+    const size_t cs = precision == 1 ? sizeof(double) : sizeof(float);
+    const size_t ub = precision == 1 ? cubic_uniform_bytes<double>(F, F_new) : cubic_uniform_bytes<float>(F, F_new);
+    int tpb = 128;
+    while (tpb > 32 && (size_t)tpb * F * cs > 32 * 1024) tpb >>= 1;
+    const size_t sm = ub + (size_t)tpb * F * cs;
+    *tpb_out = tpb;
+    *sm_out = sm <= 200 * 1024 ? sm : 0;
+}
+
+size_t redist_cubic_scratch_bytes(int precision, long pairs, int F, int F_new)
+{
+    int tpb;
+    size_t sm;
+    cubic_shape(precision, F, F_new, &tpb, &sm);
+    return sm ? 0 : (size_t)2 * pairs * F * (precision == 1 ? sizeof(double) : sizeof(float));
+}
+
 cudaError_t launch_redist_cubic(int precision, const void *f, void *fnew, void *sigma, long pairs, int F, int F_new,
                                 int spline, const RedistPlan &p, cudaStream_t st)
 {
     (void)spline;   // folded into the plan's evaluation weights
     const long reals = 2 * pairs;
-    const size_t cs = precision == 1 ? sizeof(double) : sizeof(float);
     const size_t ub = precision == 1 ? cubic_uniform_bytes<double>(F, F_new) : cubic_uniform_bytes<float>(F, F_new);
-    // shared-memory columns: 32 KB of them per block where F allows (128 threads, 64 or
-    // 32), up to 200 KB in all at 32 threads; longer strings use the global scratch
-    int tpb = 128;
-    while (tpb > 32 && (size_t)tpb * F * cs > 32 * 1024) tpb >>= 1;
-    const size_t sm = ub + (size_t)tpb * F * cs;
+    int tpb;
+    size_t sm;
+    cubic_shape(precision, F, F_new, &tpb, &sm);
     cudaError_t e = cudaSuccess;
-    if (sm <= 200 * 1024) {
+    if (sm) {
         const long blocks = (reals + tpb - 1) / tpb;
         const int grid = (int)(blocks < 152 * 32 ? blocks : 152 * 32);
         if (precision == 1) {
@@ -1910,7 +1930,7 @@ cudaError_t launch_redist_cubic(int precision, const void *f, void *fnew, void *
         }
         return cudaGetLastError();
     }
-    if (ub > 200 * 1024) return cudaErrorInvalidValue;   // more than about 2,800 images
+    if (ub > 200 * 1024 || !sigma) return cudaErrorInvalidValue;   // more than about 2,800 images
     if (ub > 48 * 1024)
         e = precision == 1
                 ? cudaFuncSetAttribute(k_redist_cubic<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ub)

@@ -114,6 +114,9 @@ cudaError_t launch_redist_plan(const double *s, int F, int F_new, int cubic, int
 cudaError_t launch_redist_linear(int precision, const void *f, void *fnew, long pairs, int F_new, const RedistPlan &p,
                                  cudaStream_t st);
 // Cubic resample; `sigma` is scratch of 2 * pairs * F reals of the precision.
+// Bytes of global scratch a cubic resample needs (0 when its columns fit in
+// shared memory, which holds for strings of up to several hundred images).
+size_t redist_cubic_scratch_bytes(int precision, long pairs, int F, int F_new);
 cudaError_t launch_redist_cubic(int precision, const void *f, void *fnew, void *sigma, long pairs, int F, int F_new,
                                 int spline, const RedistPlan &p, cudaStream_t st);
 // Precision conversion of n reals.
