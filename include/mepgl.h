@@ -43,7 +43,8 @@ typedef enum mepgl_status {
 } mepgl_status;
 
 enum { MEPGL_FP32 = 0, MEPGL_FP64 = 1 };          /* working precision of the fields  */
-enum { MEPGL_HOST = 0, MEPGL_DEVICE = 1 };        /* where a caller buffer lives      */
+enum { MEPGL_HOST = 0, MEPGL_DEVICE = 1,          /* where a caller buffer lives      */
+       MEPGL_STAGED = 2 };                         /* mepgl_set_state: the staged copy */
 enum { MEPGL_LS_COMPAT = 0, MEPGL_LS_EXACT = 1 }; /* step: geometric scan | its exact
                                                      first local minimum     */
 enum { MEPGL_POLY_COMPAT = 0, MEPGL_POLY_EXACT = 1 };       /* line polynomial        */
@@ -129,6 +130,20 @@ const char *mepgl_last_error(const mepgl_ctx *ctx);
  * mepgl_set_state resets the NLCG history (the reference starts every run
  * from zero gradients and infinite norms, mepgl/src/mepgl.cu:127-146). */
 mepgl_status mepgl_set_state(mepgl_ctx *ctx, const void *a, const void *psi_1, const void *psi_2, int memory);
+
+/* Staged upload of the next state (single-string contexts).  No counterpart
+ * in the reference, which loads its state once per run.  For callers that
+ * feed a new state every few steps from host memory: the copy of a, psi_1,
+ * psi_2 (host or device memory, the context's precision and shape) into a
+ * staging buffer of the context runs on a second stream and this call
+ * returns at once, so the copy overlaps whatever the context computes
+ * meanwhile.  mepgl_set_state(ctx, NULL, NULL, NULL, MEPGL_STAGED) then
+ * waits for that copy on the context's stream and installs it (a device
+ * copy, then the history reset of mepgl_set_state).  Host arrays should be
+ * pinned for the copy to be asynchronous, and must stay unchanged until that
+ * mepgl_set_state returns.  A later stage replaces an earlier one that was
+ * not installed.  The staging buffer (one state) is kept until destroy. */
+mepgl_status mepgl_stage_state(mepgl_ctx *ctx, const void *a, const void *psi_1, const void *psi_2, int memory);
 mepgl_status mepgl_get_state(mepgl_ctx *ctx, void *a, void *psi_1, void *psi_2, int memory);
 
 /* Initial string built on the device, for lattices too large to build on the

@@ -69,6 +69,13 @@ struct mepgl_ctx {
     std::map<std::tuple<int, int, int, int>, cudaGraphExec_t> graphs;
     std::vector<double> host_s, host_sjb;
     int sm_count = 152;
+    // staged state (mepgl_stage_state): a copy of the next state in flight on
+    // a second stream while the context computes
+    void *stage[3] = {nullptr, nullptr, nullptr};
+    size_t stage_bytes = 0;
+    cudaStream_t copy_stream = nullptr;
+    cudaEvent_t stage_done = nullptr;
+    bool staged = false;
 };
 
 namespace {
@@ -836,6 +843,12 @@ mepgl_status mepgl_destroy(mepgl_ctx *c)
     cudaFree(p.k); cudaFree(p.w); cudaFree(p.h); cudaFree(p.dl); cudaFree(p.d); cudaFree(p.du); cudaFree(p.du2);
     cudaFree(p.ipiv); cudaFree(p.status); cudaFree(p.aux);
     cudaFree(c->cubic_scratch);
+    if (c->copy_stream) {
+        cudaStreamSynchronize(c->copy_stream);
+        cudaStreamDestroy(c->copy_stream);
+    }
+    if (c->stage_done) cudaEventDestroy(c->stage_done);
+    for (void *b : c->stage) cudaFree(b);
     if (c->own_stream) cudaStreamDestroy(c->stream);
     delete c;
     return MEPGL_OK;
@@ -843,9 +856,56 @@ mepgl_status mepgl_destroy(mepgl_ctx *c)
 
 mepgl_status mepgl_set_state(mepgl_ctx *c, const void *a, const void *psi_1, const void *psi_2, int memory)
 {
-    if (!c || !a || !psi_1 || (c->ncomp == 2 && !psi_2))
+    if (!c) return MEPGL_ERR_INVALID_ARG;
+    if (memory == MEPGL_STAGED) {
+        // the staged copy: the context's stream waits for it, then takes it over
+        if (!c->staged) return fail(c, MEPGL_ERR_INVALID_ARG, "mepgl_set_state: nothing staged");
+        if (c->strings.size() != 1) return fail(c, MEPGL_ERR_UNSUPPORTED, "staged state is for single-string contexts");
+        mepgl_status st = flush(c);
+        if (st != MEPGL_OK) return st;
+        StringHost &s = c->strings[0];
+        CK(c, cudaStreamWaitEvent(c->stream, c->stage_done, 0));
+        for (int f = 0; f < 1 + c->ncomp; ++f)
+            CK(c, cudaMemcpyAsync(s.x[c->xi][f], c->stage[f], c->stage_bytes, cudaMemcpyDeviceToDevice, c->stream));
+        c->staged = false;
+        return reset_history(c);
+    }
+    if (!a || !psi_1 || (c->ncomp == 2 && !psi_2))
         return fail(c, MEPGL_ERR_INVALID_ARG, "mepgl_set_state: null field");
     return mepgl_batch_set_state(c, 0, a, psi_1, psi_2, memory);
+}
+
+mepgl_status mepgl_stage_state(mepgl_ctx *c, const void *a, const void *psi_1, const void *psi_2, int memory)
+{
+    if (!c) return MEPGL_ERR_INVALID_ARG;
+    if (!a || !psi_1 || (c->ncomp == 2 && !psi_2))
+        return fail(c, MEPGL_ERR_INVALID_ARG, "mepgl_stage_state: null field");
+    if (memory != MEPGL_HOST && memory != MEPGL_DEVICE)
+        return fail(c, MEPGL_ERR_INVALID_ARG, "mepgl_stage_state: memory must be MEPGL_HOST or MEPGL_DEVICE");
+    if (c->strings.size() != 1) return fail(c, MEPGL_ERR_UNSUPPORTED, "staged state is for single-string contexts");
+    StringHost &s = c->strings[0];
+    const size_t bytes = (size_t)s.F * s.M() * 2 * real_size(c->precision);
+    if (!c->copy_stream) {
+        CK(c, cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking));
+        CK(c, cudaEventCreateWithFlags(&c->stage_done, cudaEventDisableTiming));
+    }
+    if (c->stage_bytes != bytes) {
+        // (re)allocation: nothing of an earlier stage may still be in flight
+        CK(c, cudaStreamSynchronize(c->copy_stream));
+        for (void *&b : c->stage) {
+            cudaFree(b);
+            b = nullptr;
+        }
+        c->stage_bytes = 0;
+        for (int f = 0; f < 1 + c->ncomp; ++f) CK(c, cudaMalloc(&c->stage[f], bytes));
+        c->stage_bytes = bytes;
+    }
+    const void *src[3] = {a, psi_1, psi_2};
+    const cudaMemcpyKind k = memory == MEPGL_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
+    for (int f = 0; f < 1 + c->ncomp; ++f) CK(c, cudaMemcpyAsync(c->stage[f], src[f], bytes, k, c->copy_stream));
+    CK(c, cudaEventRecord(c->stage_done, c->copy_stream));
+    c->staged = true;
+    return MEPGL_OK;
 }
 
 mepgl_status mepgl_batch_set_state(mepgl_ctx *c, int string, const void *a, const void *psi_1, const void *psi_2,

@@ -23,7 +23,7 @@ LIB_PATH = os.environ.get("MEPGL_LIB",
                           os.path.join(os.path.dirname(os.path.abspath(__file__)), "_lib", "libmepgl_gb300.so"))
 
 FP32, FP64 = 0, 1
-HOST, DEVICE = 0, 1
+HOST, DEVICE, STAGED = 0, 1, 2
 LS_COMPAT, LS_EXACT = 0, 1
 POLY_COMPAT, POLY_EXACT = 0, 1
 SPLINE_COMPAT, SPLINE_FMM = 0, 1
@@ -79,6 +79,7 @@ _SIGS = {
     "mepgl_create": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.POINTER(C.c_void_p)]),
     "mepgl_destroy": (C.c_int, [C.c_void_p]),
     "mepgl_set_state": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int]),
+    "mepgl_stage_state": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int]),
     "mepgl_get_state": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int]),
     "mepgl_free_energy": (C.c_int, [C.c_void_p, C.c_void_p]),
     "mepgl_energy_grad": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int]),
@@ -232,6 +233,17 @@ class StringContext:
     def set_state_device(self, a, psi_1, psi_2=None):
         """Device pointers (ints, e.g. torch ``data_ptr()``) of the context precision."""
         self._check(self.L.mepgl_set_state(self.h, _ptr(a), _ptr(psi_1), _ptr(psi_2), DEVICE))
+
+    def stage_state(self, a, psi_1, psi_2=None, memory: int = HOST):
+        """Start the upload of the next state on the context's copy stream
+        (pointers as ints, e.g. of pinned torch tensors; ``memory`` HOST or
+        DEVICE) and return at once; ``set_staged_state`` installs it."""
+        self._check(self.L.mepgl_stage_state(self.h, _ptr(a), _ptr(psi_1), _ptr(psi_2), int(memory)))
+
+    def set_staged_state(self):
+        """Wait for the staged upload and make it the current state (the
+        history reset of ``set_state``)."""
+        self._check(self.L.mepgl_set_state(self.h, None, None, None, STAGED))
 
     def get_state(self) -> StringState:
         a, p1 = np.empty(self._shape(), self.dtype), np.empty(self._shape(), self.dtype)
