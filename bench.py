@@ -22,8 +22,9 @@ the same step (the C restatement in oracle/, all host threads) on the same
 workload.
 
 ``time_to_end_state`` times FP64 against FP32-then-FP64 relaxation of the
-small single-component string to a converged end state (the barrier estimate
-of the string method itself does not converge to 1e-6; see barrier.py).
+same 256x256 string to a converged end state (the barrier estimate of the
+string method itself does not converge to 1e-6; see barrier.py);
+``--ttb-config 1`` runs it on the small single-component string instead.
 
 Multi-GPU: the path does not shard within a string; ``--gpus N`` runs N
 independent replicas (one string per GPU) and reports the aggregate.
@@ -367,10 +368,11 @@ def run_ours(args):
     # these workloads (its value drifts with the reparametrization cadence), so
     # this reports the time until the end-state energy difference F_{F-1} - F_0
     # (which does converge) stays within 1e-6 of the FP64 run's final value.
-    # Default: the small single-component string (64x64, 16 images, 50 steps per
-    # reparametrization; latency-bound, seconds).  --ttb-config 2: the 256x256
-    # two-component string (100 steps per reparametrization; several minutes),
-    # against the value its long FP64 run converges to, with paired-FP64 polish.
+    # Default (--ttb-config 2): the mixed-precision workload itself, the 256x256
+    # two-component string (100 steps per reparametrization; about 2.5 minutes),
+    # IEEE FP64 against FP32 then paired-FP64 polish, to the value its long FP64
+    # run converges to.  --ttb-config 1: the small single-component string
+    # (64x64, 16 images, 50 steps per reparametrization; latency-bound, seconds).
     ttb = None
     if rank == 0 and not args.no_ttb:
         from mepgl_gb300 import barrier as B
@@ -399,7 +401,11 @@ def run_ours(args):
                "mixed_paired_s": t_to(rmxp),        # FP32, then paired (float-float) FP64
                "fp64_paired_s": t_to(r64p),         # paired FP64 throughout
                "mixed_fp32_iterations": sum(1 for x in rmxp if x[4] == "fp32"),
+               "ends_fp64": r64[-1][3], "ends_mixed": rmxp[-1][3],
                "barrier_fp64": r64[-1][1], "barrier_mixed": rmxp[-1][1]}
+        if ttb["fp64_s"] and ttb["mixed_paired_s"]:
+            ttb["speedup_mixed_vs_fp64"] = ttb["fp64_s"] / ttb["mixed_paired_s"]
+        ttb["ends_rel_err_mixed"] = abs(ttb["ends_mixed"] - target) / abs(target)
 
     # ---- CPU baseline (rank 0, N = 1 only) ------------------------------------
     cpu = None
@@ -435,8 +441,9 @@ def main(argv=None):
     ap.add_argument("--impl", choices=("ours", "reference"), default="ours")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-ttb", action="store_true", help="skip the time-to-converged-end-state leg")
-    ap.add_argument("--ttb-config", type=int, choices=(1, 2), default=1,
-                    help="workload of that leg: 1 (64x64, seconds) or 2 (256x256, several minutes)")
+    ap.add_argument("--ttb-config", type=int, choices=(1, 2), default=2,
+                    help="workload of that leg: 2 (the 256x256 mixed-precision string, about 2.5 minutes) "
+                         "or 1 (64x64, seconds)")
     args = ap.parse_args(argv)
     if args.impl == "reference":
         return run_reference(args)
