@@ -484,7 +484,36 @@ bool use_fused(const mepgl_ctx *c)
     return true;
 }
 
+// Paired FP64 passes keep the fields x as float-float pairs (x_pairs()):
+// the current x of every string changes format before the passes and back
+// after them, so that every other kernel and copy sees double.
+bool paired_x(const mepgl_ctx *c)
+{
+    return c->precision == 1 && c->opt.fp64_arith == MEPGL_FP64_PAIRED && x_pairs();
+}
+
+mepgl_status x_format(mepgl_ctx *c, int to_pairs)
+{
+    for (auto &s : c->strings)
+        for (int f = 0; f < 1 + c->ncomp; ++f)
+            CK(c, launch_x_format(s.x[c->xi][f], (long)s.F * s.M(), to_pairs, c->stream));
+    c->launches += (int64_t)c->strings.size() * (1 + c->ncomp);
+    return MEPGL_OK;
+}
+
+mepgl_status nlcg_steps_body(mepgl_ctx *c, int iters, int use_cg, int maxwell);
+
 mepgl_status nlcg_steps(mepgl_ctx *c, int iters, int use_cg, int maxwell)
+{
+    if (iters <= 0 || !paired_x(c)) return nlcg_steps_body(c, iters, use_cg, maxwell);
+    mepgl_status st = x_format(c, 1);
+    if (st != MEPGL_OK) return st;
+    st = nlcg_steps_body(c, iters, use_cg, maxwell);
+    const mepgl_status back = x_format(c, 0);
+    return st != MEPGL_OK ? st : back;
+}
+
+mepgl_status nlcg_steps_body(mepgl_ctx *c, int iters, int use_cg, int maxwell)
 {
     if (iters > 0 && use_fused(c)) {
         // all steps of a batch in one persistent launch (per-image stages instead of kernel boundaries)
@@ -1314,6 +1343,11 @@ mepgl_status mepgl_profile_passes(mepgl_ctx *c, int steps, int use_cg, double *m
     std::vector<cudaEvent_t> ev(2 * steps + 1);
     for (auto &e : ev) CK(c, cudaEventCreate(&e));
     const int nb = (int)c->batches.size();
+    const bool px = paired_x(c);
+    if (px) {
+        mepgl_status st = x_format(c, 1);
+        if (st != MEPGL_OK) return st;
+    }
     CK(c, cudaEventRecord(ev[0], c->stream));
     for (int it = 1; it <= steps; ++it) {
         const StepFlags f = step_flags(c, it, use_cg ? 1 : 0, 0);
@@ -1325,6 +1359,10 @@ mepgl_status mepgl_profile_passes(mepgl_ctx *c, int steps, int use_cg, double *m
         c->di ^= 1;
         c->launches += (int64_t)nlcg_step_launches() * nb;
         c->pending = true;
+    }
+    if (px) {
+        mepgl_status st = x_format(c, 0);
+        if (st != MEPGL_OK) return st;
     }
     CK(c, cudaEventSynchronize(ev[2 * steps]));
     double tg = 0, td = 0;

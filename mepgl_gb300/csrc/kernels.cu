@@ -133,6 +133,14 @@ template <class T> struct GradLean {
     static constexpr bool v = MEPGL_GRAD_LEAN == 2 || (MEPGL_GRAD_LEAN == 1 && std::is_same<T, ff>::value);
 };
 
+// Paired FP64: while the NLCG passes run, the fields x hold float-float
+// pairs too (launch_x_format converts them in place before and after), so
+// the passes read and write them without double conversions.
+#ifndef MEPGL_FF_XPAIRS
+#define MEPGL_FF_XPAIRS 1
+#endif
+template <class T> struct XPairs { static constexpr bool v = MEPGL_FF_XPAIRS != 0 && std::is_same<T, ff>::value; };
+
 template <class T> struct TileRows { static constexpr int v = sizeof(T) == 4 ? MEPGL_ROWS_F32 : MEPGL_ROWS_F64; };
 // Two-component float-float NLCG passes run the packed stencils (site_pair.cuh).
 template <class T, int NC> struct FFPacked {
@@ -459,7 +467,7 @@ __global__ void __launch_bounds__(NT, MinBlocks<T>::grad) k_grad(const __grid_co
         image_ptrs<T, NC>(ip, S.x[f.xin], S.d[f.din], S.x[f.xout], off);
 #if MEPGL_GRAD_ASYNC
         if constexpr (std::is_same<T, ff>::value) {
-            stage<T, NC, TYT, 1, false, true, GradLean<T>::v>(t, S, ip, i0, j0, (T)sc.alpha_pend[img], true, true);
+            stage<T, NC, TYT, 1, XPairs<T>::v, true, GradLean<T>::v>(t, S, ip, i0, j0, (T)sc.alpha_pend[img], true, true);
         } else {
             constexpr int HW = TX + 2, HE = (TYT + 2) * HW, NI = (HE + NT - 1) / NT;
             const T alpha = (T)sc.alpha_pend[img];
@@ -499,7 +507,7 @@ __global__ void __launch_bounds__(NT, MinBlocks<T>::grad) k_grad(const __grid_co
             }
         }
 #else
-        stage<T, NC, TYT, 1, false, true, GradLean<T>::v>(t, S, ip, i0, j0, (T)sc.alpha_pend[img], true, true);
+        stage<T, NC, TYT, 1, XPairs<T>::v, true, GradLean<T>::v>(t, S, ip, i0, j0, (T)sc.alpha_pend[img], true, true);
 #endif
         using W = vec2_t<store_t<T>>;
         W *gcur[1 + NC];
@@ -605,8 +613,8 @@ __global__ void __launch_bounds__(NT, MinBlocks<T>::dir) k_dir_poly(const __grid
         image_ptrs<T, NC>(ipx, S.x[f.xout], nullptr, nullptr, off);
         image_ptrs<T, NC>(ipd, S.d[f.din], S.g[f.gcur], S.d[f.dout], off);
         if constexpr (std::is_same<T, ff>::value) {
-            // float-float tiles are converted from double: staged through registers
-            stage<T, NC, TYT, 0>(tx, S, ipx, i0, j0, (T)0, false, true);
+            // float-float tiles are staged through registers
+            stage<T, NC, TYT, 0, XPairs<T>::v>(tx, S, ipx, i0, j0, (T)0, false, true);
 #if MEPGL_SPLIT_DIR
             ImagePtrs<T, NC> ipn;
             image_ptrs<T, NC>(ipn, S.d[f.dout], nullptr, nullptr, off);
@@ -983,6 +991,26 @@ __global__ void __launch_bounds__(NT) k_apply_update(vec2_t<T> *x, const vec2_t<
         v.x = v.x + a * dd.x;
         v.y = v.y + a * dd.y;
         x[off + p] = v;
+    }
+}
+
+// Fields x between double pairs and float-float pairs, in place (an ff2
+// fills the 16 bytes of a double2).  A double holds a float-float pair that
+// the passes wrote exactly, so a round trip returns the same doubles.
+template <bool TO_PAIRS>
+__global__ void __launch_bounds__(NT) k_x_format(double2 *x, long n)
+{
+    for (long i = blockIdx.x * (long)NT + threadIdx.x; i < n; i += (long)gridDim.x * NT) {
+        if (TO_PAIRS) {
+            const double2 v = x[i];
+            ff2 w;
+            w.x = to_ff(v.x);
+            w.y = to_ff(v.y);
+            storew<ff>(x + i, w);
+        } else {
+            const ff2 w = loadw<ff>(x + i);
+            x[i] = make_double2(to_double(w.x), to_double(w.y));
+        }
     }
 }
 
@@ -1942,6 +1970,15 @@ cudaError_t launch_redist_cubic(int precision, const void *f, void *fnew, void *
     else
         k_redist_cubic<float><<<grid_for(reals), NT, ub, st>>>((const float *)f, (float *)fnew, (float *)sigma, reals,
                                                                F, F_new, p);
+    return cudaGetLastError();
+}
+
+bool x_pairs() { return MEPGL_FF_XPAIRS != 0; }
+
+cudaError_t launch_x_format(void *x, long pairs, int to_pairs, cudaStream_t st)
+{
+    if (to_pairs) k_x_format<true><<<grid_for(pairs), NT, 0, st>>>((double2 *)x, pairs);
+    else k_x_format<false><<<grid_for(pairs), NT, 0, st>>>((double2 *)x, pairs);
     return cudaGetLastError();
 }
 

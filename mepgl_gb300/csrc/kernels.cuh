@@ -58,6 +58,10 @@ cudaError_t launch_grad(const Launch &L, const Scalars &sc, const StepFlags &f);
 // tile of each image runs the line search and sets alpha, alpha_pend.
 cudaError_t launch_dir_poly(const Launch &L, const Scalars &sc, const StepFlags &f);
 // x[xbuf] += alpha_pend d[dbuf]; alpha_pend = 0.
+// Paired FP64: whether the NLCG passes keep x as float-float pairs, and the
+// in-place conversion of `pairs` complex values of x to (1) or from (0) them.
+bool x_pairs();
+cudaError_t launch_x_format(void *x, long pairs, int to_pairs, cudaStream_t st);
 cudaError_t launch_apply_update(const Launch &L, const Scalars &sc, const StringDesc *host_strings, int n_strings,
                                 int xbuf, int dbuf);
 // Energy of x[xbuf] into sc.fenergy_out (per image).
