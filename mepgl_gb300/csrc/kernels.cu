@@ -115,7 +115,7 @@ namespace mepgl {
 #define MEPGL_FF_PAIR 1
 #endif
 #ifndef MEPGL_MINB_GRAD_FF
-#define MEPGL_MINB_GRAD_FF 4
+#define MEPGL_MINB_GRAD_FF 3
 #endif
 #ifndef MEPGL_MINB_DIR_FF
 #define MEPGL_MINB_DIR_FF 2
