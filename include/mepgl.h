@@ -308,22 +308,28 @@ mepgl_status mepgl_pass_kernels(const mepgl_ctx *ctx, const char **grad, const c
 mepgl_status mepgl_fused_wait_selftest(mepgl_ctx *ctx, int *timed_out);
 
 /* Allocation-free free energy.  No counterpart in the reference.  For callers
- * that cannot allocate device memory -- code running inside someone else's
- * CUDA-graph capture or memory pool, or an embedding that owns a fixed
- * device arena -- this evaluates the per-image FP64 free energy of
- * caller-owned device arrays without a context and without any allocation.
+ * that cannot allocate device memory -- an embedding that owns a fixed
+ * device arena and hands out only pre-allocated buffers, a host framework
+ * whose memory pool owns the whole device, or a plugin whose host process
+ * forbids cudaMalloc after start-up -- this evaluates the per-image FP64
+ * free energy of caller-owned device arrays without a context and without
+ * any allocation.
  * Inputs (all device pointers): comp_code / sc_code are int32 neighbour
  * codes per site (the layout of the reference's buildNearestNeighbourMap),
  * the nine parameter arrays are per-site doubles, a / psi_1 / psi_2 are the
  * F images as double pairs; fenergy receives F doubles.  Scratch for the
  * reduction lives in fixed device arrays of the library (4 MiB + 16 KiB per
  * GPU that loads it, kept until the process exits): the string must satisfy
- * n_images <= 4096 and n_images * ceil(nx/32) * ceil(ny/8) <= 65536, else
- * MEPGL_ERR_INVALID_ARG.  The first call on a device resolves the scratch
- * addresses and uploads constant tables; make that first call before any
- * stream capture.  All calls share the scratch, so calls that overlap on
- * the GPU (different streams, no ordering) race.  Asynchronous on `stream`
- * (a cudaStream_t, NULL = default stream).  Errors: mepgl_noalloc_last_error. */
+ * n_images <= 4096 and n_images * ceil(nx/32) * ceil(ny/8) <= 65536 (and the
+ * lattice nx <= 32767*32, ny <= 32767*8), else MEPGL_ERR_INVALID_ARG.  The
+ * first call on a device resolves the scratch addresses and uploads
+ * constant tables; make that first call before any stream capture.  They
+ * are kept until exit, so a device reset afterwards is not supported.  All
+ * calls share the scratch, so calls that overlap on the GPU (different
+ * streams, no ordering) race.  A CUDA error already pending when the call
+ * starts is reported (MEPGL_ERR_CUDA) and left pending for its owner.
+ * Asynchronous on `stream` (a cudaStream_t, NULL = default stream).
+ * Errors: mepgl_noalloc_last_error. */
 mepgl_status mepgl_free_energy_noalloc(int nx, int ny, int n_images, int multicomponent, int thin_film, double dx,
                                        const int32_t *comp_code, const int32_t *sc_code, const double *a_1,
                                        const double *b_1, const double *m_xx_1, const double *m_yy_1,

@@ -1997,10 +1997,11 @@ cudaError_t launch_convert(const void *src, int src_prec, void *dst, int dst_pre
 
 // ===================================================== allocation-free energy
 //
-// Some callers cannot allocate device memory: code that runs inside a
-// framework's CUDA-graph capture or a custom memory pool, embedded solvers
-// that own a fixed device arena, or plugins whose host process forbids
-// cudaMalloc after start-up.  mepgl_free_energy_noalloc serves them: it
+// Some callers cannot allocate device memory: embedded solvers that own a
+// fixed device arena and hand out only pre-allocated buffers, host
+// frameworks whose memory pool owns the whole device, or plugins whose host
+// process forbids cudaMalloc after start-up (an allocation there can
+// synchronise the device in the middle of its pipelined work).  mepgl_free_energy_noalloc serves them: it
 // evaluates the per-image free energy of caller-owned device arrays without
 // creating a context and without any allocation.  The per-tile partial sums
 // and per-image tickets of the deterministic reduction live in the fixed
@@ -2032,7 +2033,10 @@ thread_local std::string g_noalloc_err;
 
 // Device addresses of the scratch arrays, resolved once per device with that
 // device current (a host-side reference to the array names is not a device
-// address).  Also uploads the constant neighbour-code tables.
+// address).  Also uploads the constant neighbour-code tables.  Both are kept
+// for the life of the process: a device reset (cudaDeviceReset, or a reset
+// of the primary context by the host framework) is not supported, since the
+// cached addresses and the constant tables would then be stale.
 cudaError_t noalloc_setup(int dev, NoallocScratch *out)
 {
     std::lock_guard<std::mutex> lk(g_noalloc_mu);
@@ -2078,10 +2082,20 @@ extern "C" mepgl_status mepgl_free_energy_noalloc(int nx, int ny, int n_images, 
         return noalloc_fail(MEPGL_ERR_INVALID_ARG, "null device pointer");
     const long tiles_x = (nx + TX - 1) / TX, tiles_y = (ny + rows - 1) / rows;
     const long n_tiles = tiles_x * tiles_y * n_images;
-    if (n_images > NOALLOC_MAX_IMAGES || n_tiles > NOALLOC_MAX_TILES || (long)nx * ny >= (1L << 31))
+    // tile coordinates are 16-bit (TileRef), as in mepgl_create
+    if (nx > 32767 * TX || ny > 32767 * rows || (long)nx * ny >= (1L << 31))
+        return noalloc_fail(MEPGL_ERR_INVALID_ARG, "lattice too large: need nx <= 32767*32, ny <= 32767*8 "
+                                                   "and nx * ny < 2^31");
+    if (n_images > NOALLOC_MAX_IMAGES || n_tiles > NOALLOC_MAX_TILES)
         return noalloc_fail(MEPGL_ERR_INVALID_ARG,
                             "string too large for the fixed scratch: need n_images <= 4096 and "
                             "n_images * ceil(nx/32) * ceil(ny/8) <= 65536");
+    // An error left pending by the caller's own earlier work is reported as
+    // such and left in place, not taken for a failure of this call.
+    cudaError_t pend = cudaPeekAtLastError();
+    if (pend != cudaSuccess)
+        return noalloc_fail(MEPGL_ERR_CUDA, std::string("error pending before this call (left for the caller): ") +
+                                                cudaGetErrorString(pend));
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= NOALLOC_MAX_DEVICES)
         return noalloc_fail(MEPGL_ERR_CUDA, "no usable current device");

@@ -30,7 +30,8 @@ the kernels depends on the macro.
 
 Usage: ``python oracle/ref_build.py N DX C PREC [--film]``; the Python helper
 ``oracle.refkernels.load_ref`` calls it on demand.  Requires the reference
-tree at ``$MEPGL_REFERENCE`` (default ``/root/reference``).
+tree at ``$MEPGL_REFERENCE``; without it, a checkout named ``reference``
+beside this repository's directory (``<repo>/../reference``) is used.
 """
 from __future__ import annotations
 
@@ -42,7 +43,7 @@ import sys
 import tempfile
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REF_ROOT = os.environ.get("MEPGL_REFERENCE", "/root/reference")
+REF_ROOT = os.environ.get("MEPGL_REFERENCE") or os.path.join(os.path.dirname(os.path.dirname(HERE)), "reference")
 REF_SRC = os.path.join(REF_ROOT, "mepgl", "src")
 OUT_ROOT = os.path.join(HERE, "_ref")
 

@@ -1,10 +1,10 @@
 """The allocation-free free-energy entry point (mepgl_free_energy_noalloc).
 
-It exists for callers that cannot allocate device memory -- code running
-inside someone else's CUDA-graph capture or memory pool, or an embedding that
-owns a fixed device arena.  The test allocates its inputs itself (a test may;
-the entry point may not), calls the entry point through the C ABI twice in a
-row on different strings -- the second call reuses the fixed scratch the
+It exists for callers that cannot allocate device memory -- an embedding
+that owns a fixed device arena, a host framework whose memory pool owns the
+device, or a process that forbids cudaMalloc after start-up.  The test
+allocates its inputs itself (a test may; the entry point may not), calls the
+entry point through the C ABI twice in a row on different strings -- the second call reuses the fixed scratch the
 first one left behind -- and compares each result with the context-based
 mepgl_free_energy.  Collected last so that a stop-at-first-failure run has
 already run every other test.
@@ -77,3 +77,8 @@ def test_noalloc_rejects_oversize_strings():
                                          dummy, dummy, None, dummy, None)
     assert status == 1
     assert "too large" in L.mepgl_noalloc_last_error().decode()
+    # few tiles, but a tile column past the 16-bit tile coordinates
+    status = L.mepgl_free_energy_noalloc(1280000, 2, 1, 0, 0, 0.5, *([dummy] * 11), 1.0, 1.0, 0.0, 0.0, 0.0,
+                                         dummy, dummy, None, dummy, None)
+    assert status == 1
+    assert "lattice too large" in L.mepgl_noalloc_last_error().decode()
