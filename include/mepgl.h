@@ -22,6 +22,18 @@
  * Threading: a context is bound to the CUDA stream given at creation and is
  * not re-entrant; use one context per stream.  Calls that return host data
  * synchronise that stream; the others are asynchronous.
+ *
+ * Failure detection (the reference has none: NaN fields give NaN energies,
+ * a zero-length string divides 0 by 0, mepgl/src/interpolation.cu:126-140).
+ * Each mepgl_nlcg_steps / mepgl_iteration call ends with a device check of
+ * every image's energy and |g|^2; a NaN or infinity there, a string of zero
+ * or non-finite arc length, or a fused-launch wait that ran out sets a
+ * device flag.  Asynchronous calls cannot report it; the next call that
+ * synchronises the stream (mepgl_image_scalars, mepgl_free_energy,
+ * mepgl_get_state, mepgl_arc_length, mepgl_redistribute, mepgl_iteration in
+ * modes L and C, mepgl_set_precision, mepgl_synchronize) returns
+ * MEPGL_ERR_NAN (MEPGL_ERR_CUDA for the wait) with the string and image in
+ * mepgl_last_error, and clears the flag.  The context stays usable.
  */
 #ifndef MEPGL_H
 #define MEPGL_H
@@ -36,7 +48,8 @@ typedef enum mepgl_status {
     MEPGL_OK = 0,
     MEPGL_ERR_INVALID_ARG = 1,   /* bad size, pointer or option                    */
     MEPGL_ERR_CUDA = 2,          /* a CUDA runtime call or kernel launch failed    */
-    MEPGL_ERR_NAN = 3,           /* a per-image scalar became NaN or infinite      */
+    MEPGL_ERR_NAN = 3,           /* a per-image scalar became NaN or infinite, or
+                                    the string has no arc length (see below)       */
     MEPGL_ERR_IO = 4,            /* file reading / writing (npy helpers)           */
     MEPGL_ERR_UNSUPPORTED = 5,   /* option not available for this problem         */
     MEPGL_ERR_STATE = 6          /* call not valid in the context's current state  */
@@ -236,7 +249,9 @@ mepgl_status mepgl_compute_jb(mepgl_ctx *ctx, void *b, void *j_1, void *j_2, int
 
 /* Normalised arc length (host array of F doubles) in the field metric or
  * the (B, J) metric.  Replaces arcLength / arcLengthJB
- * (mepgl/src/interpolation.cu:143-169). */
+ * (mepgl/src/interpolation.cu:143-169).  A string of zero or non-finite
+ * length (all images equal, non-finite fields) returns MEPGL_ERR_NAN and
+ * s = n / (F - 1), on which a linear resample keeps every image. */
 mepgl_status mepgl_arc_length(mepgl_ctx *ctx, int metric, double *s);
 
 /* Reparametrize the string to F_new equidistant images in the context's
@@ -245,7 +260,11 @@ mepgl_status mepgl_arc_length(mepgl_ctx *ctx, int metric, double *s);
  * mepgl/src/mepgl.cu:699-766; single-string contexts only).  With several
  * strings and F_new < 0 every string is reparametrized.  Does NOT restart CG
  * (see mepgl_reset_cg).  Replaces redistributeLinear / redistributeCubic
- * (mepgl/src/interpolation.cu:229-481). */
+ * (mepgl/src/interpolation.cu:229-481).  Needs F >= 2 (linear) or F >= 4
+ * (cubic), else MEPGL_ERR_INVALID_ARG.  Two equal adjacent images (a
+ * segment of zero length, 0/0 in the reference) resample to their state;
+ * a string of zero arc length returns MEPGL_ERR_NAN, and a singular cubic
+ * spline matrix too. */
 mepgl_status mepgl_redistribute(mepgl_ctx *ctx, int kind, int F_new);
 
 /* Batched strings.  No counterpart in the reference, which runs parameter

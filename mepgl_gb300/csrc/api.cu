@@ -503,14 +503,29 @@ mepgl_status x_format(mepgl_ctx *c, int to_pairs)
 
 mepgl_status nlcg_steps_body(mepgl_ctx *c, int iters, int use_cg, int maxwell);
 
+// After the steps of a call, one small launch checks every image's energy
+// and |g|^2 (the slot the last step wrote) for NaN / infinity; the flags are
+// reported by the next synchronising call (check_device_status).
+mepgl_status check_scalars(mepgl_ctx *c, int iters)
+{
+    if (iters <= 0) return MEPGL_OK;
+    CK(c, launch_check_scalars(c->sc, c->total_images, iters & 1, c->stream));
+    c->launches += 1;
+    return MEPGL_OK;
+}
+
 mepgl_status nlcg_steps(mepgl_ctx *c, int iters, int use_cg, int maxwell)
 {
-    if (iters <= 0 || !paired_x(c)) return nlcg_steps_body(c, iters, use_cg, maxwell);
+    if (iters <= 0 || !paired_x(c)) {
+        mepgl_status st = nlcg_steps_body(c, iters, use_cg, maxwell);
+        return st != MEPGL_OK ? st : check_scalars(c, iters);
+    }
     mepgl_status st = x_format(c, 1);
     if (st != MEPGL_OK) return st;
     st = nlcg_steps_body(c, iters, use_cg, maxwell);
     const mepgl_status back = x_format(c, 0);
-    return st != MEPGL_OK ? st : back;
+    if (st == MEPGL_OK) st = back;
+    return st != MEPGL_OK ? st : check_scalars(c, iters);
 }
 
 mepgl_status nlcg_steps_body(mepgl_ctx *c, int iters, int use_cg, int maxwell)
@@ -545,19 +560,32 @@ mepgl_status nlcg_steps_body(mepgl_ctx *c, int iters, int use_cg, int maxwell)
     return MEPGL_OK;
 }
 
-// Device-side error flags: status[0] is set when a stage wait of the fused
-// NLCG launch ran out (the launch then stopped early).  Read on the stream
-// after the work before it, then cleared.
+// Device-side error flags (STATUS_* in kernels.cuh): a stage wait of the
+// fused NLCG launch that ran out (the launch then stopped early), non-finite
+// per-image scalars after NLCG steps, a string of zero or non-finite arc
+// length.  Read on the stream after the work before it, then cleared; the
+// first raised flag is reported.
 mepgl_status check_device_status(mepgl_ctx *c)
 {
-    int st = 0;
-    CK(c, cudaMemcpyAsync(&st, c->sc.status, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+    int st[4] = {0, 0, 0, 0};
+    CK(c, cudaMemcpyAsync(st, c->sc.status, sizeof(st), cudaMemcpyDeviceToHost, c->stream));
     CK(c, cudaStreamSynchronize(c->stream));
-    if (st) {
-        CK(c, cudaMemsetAsync(c->sc.status, 0, sizeof(int), c->stream));
+    if (!(st[STATUS_WAIT] | st[STATUS_NONFINITE] | st[STATUS_ARC])) return MEPGL_OK;
+    CK(c, cudaMemsetAsync(c->sc.status, 0, sizeof(st), c->stream));
+    CK(c, cudaStreamSynchronize(c->stream));
+    if (st[STATUS_WAIT])
         return fail(c, MEPGL_ERR_CUDA, "fused NLCG launch: a per-image stage wait ran out; the steps are incomplete");
+    if (st[STATUS_NONFINITE]) {
+        int g = st[STATUS_NONFINITE_IMAGE] - 1, si = 0;
+        while (si + 1 < (int)c->hdesc.size() && g >= c->hdesc[si + 1].img_base) ++si;
+        return fail(c, MEPGL_ERR_NAN,
+                    "non-finite energy or gradient norm after NLCG steps in " + std::to_string(st[STATUS_NONFINITE]) +
+                        " image(s), first: string " + std::to_string(si) + " image " +
+                        std::to_string(g - c->hdesc[si].img_base));
     }
-    return MEPGL_OK;
+    return fail(c, MEPGL_ERR_NAN,
+                "arc length of the string is zero or not finite (all images equal, or non-finite fields); "
+                "it was taken as uniform, so a linear resample kept the images");
 }
 
 mepgl_status copy_fields(mepgl_ctx *c, StringHost &s, void *const *dst, const void *const *src, int memory, bool in)
@@ -597,7 +625,8 @@ mepgl_status arc_length(mepgl_ctx *c, int si, int metric, double **where)
         fl[2] = j[0][1]; w[2] = 2;
         *where = c->ds_jb;
     }
-    CK(c, launch_arc_length(c->precision, fl, w, nf, s.M(), s.F, c->sc.part, *where, c->stream));
+    CK(c, launch_arc_length(c->precision, fl, w, nf, s.M(), s.F, c->sc.part, *where, c->sc.status + STATUS_ARC,
+                            c->stream));
     c->launches += 2;
     return MEPGL_OK;
 }
@@ -674,6 +703,11 @@ mepgl_status redistribute(mepgl_ctx *c, int kind, int F_new)
     }
     // resize: new buffers for F_new images, state moved in, history reset
     CK(c, cudaStreamSynchronize(c->stream));
+    st = check_device_status(c);    // before build_layout renews the flags
+    if (st != MEPGL_OK) {
+        for (int f = 0; f < 1 + c->ncomp; ++f) cudaFree(target[f]);
+        return st;
+    }
     free_string_buffers(s);
     s.F = F_new;
     st = alloc_string_buffers(c, s);
@@ -1025,7 +1059,7 @@ mepgl_status mepgl_batch_get_state(mepgl_ctx *c, int string, void *a, void *psi_
     void *dst[3] = {a, psi_1, psi_2};
     const void *src[3] = {s.x[c->xi][0], s.x[c->xi][1], s.x[c->xi][2]};
     st = copy_fields(c, s, dst, src, memory, false);
-    if (st == MEPGL_OK && nlcg_fused(c->precision)) st = check_device_status(c);
+    if (st == MEPGL_OK) st = check_device_status(c);
     return st;
 }
 
@@ -1042,6 +1076,12 @@ mepgl_status mepgl_batch_free_energy(mepgl_ctx *c, int string, double *fenergy)
     CK(c, cudaMemcpyAsync(fenergy, c->dscratch + c->hdesc[string].img_base, c->strings[string].F * sizeof(double),
                           cudaMemcpyDeviceToHost, c->stream));
     CK(c, cudaStreamSynchronize(c->stream));
+    st = check_device_status(c);
+    if (st != MEPGL_OK) return st;
+    for (int n = 0; n < c->strings[string].F; ++n)
+        if (!std::isfinite(fenergy[n]))
+            return fail(c, MEPGL_ERR_NAN, "mepgl_free_energy: non-finite energy of image " + std::to_string(n) +
+                                              " (non-finite fields)");
     return MEPGL_OK;
 }
 
@@ -1141,7 +1181,7 @@ mepgl_status mepgl_batch_image_scalars(mepgl_ctx *c, int string, double *fenergy
     if (g_norm2) CK(c, cudaMemcpyAsync(g_norm2, c->sc.gn0 + o, F * 8, cudaMemcpyDeviceToHost, c->stream));
     if (alpha) CK(c, cudaMemcpyAsync(alpha, c->sc.alpha + o, F * 8, cudaMemcpyDeviceToHost, c->stream));
     CK(c, cudaStreamSynchronize(c->stream));
-    return nlcg_fused(c->precision) ? check_device_status(c) : MEPGL_OK;
+    return check_device_status(c);
 }
 
 mepgl_status mepgl_compute_jb(mepgl_ctx *c, void *b, void *j_1, void *j_2, int memory)
@@ -1215,7 +1255,7 @@ mepgl_status mepgl_batch_arc_length(mepgl_ctx *c, int string, int metric, double
     if (st != MEPGL_OK) return st;
     CK(c, cudaMemcpyAsync(s, where, c->strings[string].F * 8, cudaMemcpyDeviceToHost, c->stream));
     CK(c, cudaStreamSynchronize(c->stream));
-    return MEPGL_OK;
+    return check_device_status(c);
 }
 
 mepgl_status mepgl_redistribute(mepgl_ctx *c, int kind, int F_new)
@@ -1226,6 +1266,8 @@ mepgl_status mepgl_redistribute(mepgl_ctx *c, int kind, int F_new)
     mepgl_status st = redistribute(c, kind, F_new);
     if (st != MEPGL_OK) return st;
     CK(c, cudaStreamSynchronize(c->stream));
+    st = check_device_status(c);
+    if (st != MEPGL_OK) return st;
     int bad = 0;
     CK(c, cudaMemcpy(&bad, c->plan.status, sizeof(int), cudaMemcpyDeviceToHost));
     if (bad) {
@@ -1266,6 +1308,7 @@ mepgl_status mepgl_set_precision(mepgl_ctx *c, int precision)
         return fail(c, MEPGL_ERR_INVALID_ARG, "mepgl_set_precision: bad precision");
     if (precision == c->precision) return MEPGL_OK;
     mepgl_status st = flush(c);
+    if (st == MEPGL_OK) st = check_device_status(c);   // before build_layout renews the flags
     if (st != MEPGL_OK) return st;
     const int old = c->precision;
     for (auto &s : c->strings) {
@@ -1383,7 +1426,7 @@ mepgl_status mepgl_synchronize(mepgl_ctx *c)
 {
     if (!c) return MEPGL_ERR_INVALID_ARG;
     CK(c, cudaStreamSynchronize(c->stream));
-    return nlcg_fused(c->precision) ? check_device_status(c) : MEPGL_OK;
+    return check_device_status(c);
 }
 
 }  // extern "C"

@@ -136,19 +136,32 @@ std::vector<T> to_npy(const T *a, size_t nx, size_t ny, size_t stride = 1, size_
     return o;
 }
 
+// A failure with the library status it maps to; the process exits with
+// that status (3 = MEPGL_ERR_NAN for non-finite data, 1 for anything that
+// is not a library status).
+struct StatusError : std::runtime_error {
+    int status;
+    StatusError(int st, const std::string &m) : std::runtime_error(m), status(st) {}
+};
+
 std::vector<double> load2d(const std::string &p, size_t &nx, size_t &ny)
 {
     npy::Array a = npy::read(p);
     if (a.shape.size() != 2) throw std::runtime_error(p + ": expected a 2-D array");
     if (nx == 0) { nx = a.shape[0]; ny = a.shape[1]; }
     if (a.shape[0] != nx || a.shape[1] != ny) throw std::runtime_error(p + ": shape mismatch");
-    return to_lib(npy::as_double(a), nx, ny);
+    std::vector<double> v = npy::as_double(a);
+    // the reference reads inputs unchecked (mepgl/src/io.cu:18-125); a NaN or
+    // infinity in any input would only show as non-finite energies later
+    for (size_t k = 0; k < v.size(); ++k)
+        if (!std::isfinite(v[k]))
+            throw StatusError(MEPGL_ERR_NAN, p + ": non-finite value at flat index " + std::to_string(k));
+    return to_lib(v, nx, ny);
 }
 
 void check(mepgl_status st, mepgl_ctx *ctx, const char *what)
 {
-    if (st != MEPGL_OK)
-        throw std::runtime_error(std::string(what) + ": " + mepgl_last_error(ctx));
+    if (st != MEPGL_OK) throw StatusError(st, std::string(what) + ": " + mepgl_last_error(ctx));
 }
 
 template <class T>
@@ -209,6 +222,8 @@ int run(const Args &A)
     std::vector<int32_t> comp(cdom.begin(), cdom.end()), sc(sdom.begin(), sdom.end());
     const std::vector<double> q = npy::as_double(npy::read(in + "q.npy"));
     if (q.size() < 5) throw std::runtime_error("q.npy must hold q_1, q_2, eta, gamma, delta");
+    for (size_t k = 0; k < 5; ++k)
+        if (!std::isfinite(q[k])) throw StatusError(MEPGL_ERR_NAN, in + "q.npy: non-finite coupling");
     const bool mc = cfg.count("multicomponent") ? std::stoi(cfg["multicomponent"]) != 0 : exists(in + "0/u_2.npy");
     const int nc = mc ? 2 : 1;
     int F = A.F;
@@ -216,6 +231,12 @@ int run(const Args &A)
         F = 0;
         while (exists(in + std::to_string(F) + "/u_1.npy")) ++F;
     }
+    if (F < 1) throw StatusError(MEPGL_ERR_INVALID_ARG, in + ": no images (0/u_1.npy missing)");
+    // the arc-length resample needs two images, the cubic spline four
+    // (mepgl/src/interpolation.cu:252-322); the reference would index past its arrays
+    if ((A.mode == 'L' && F < 2) || (A.mode == 'C' && F < 4))
+        throw StatusError(MEPGL_ERR_INVALID_ARG, std::string("mode ") + A.mode + " needs at least " +
+                                                     (A.mode == 'C' ? "4" : "2") + " images, got " + std::to_string(F));
     const int F_out = A.F_out < 1 ? F : A.F_out;
     const std::string prec = opt("precision", opt("double_precision", "0") == "1" ? "fp64" : "fp32");
     const bool mixed = prec == "mixed";
@@ -399,6 +420,9 @@ int main(int argc, char **argv)
 {
     try {
         return run(parse(argc, argv));
+    } catch (const StatusError &e) {
+        std::fprintf(stderr, "mepgl: %s\n", e.what());
+        return e.status;
     } catch (const std::exception &e) {
         std::fprintf(stderr, "mepgl: %s\n", e.what());
         return 1;

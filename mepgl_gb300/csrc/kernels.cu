@@ -1235,12 +1235,25 @@ __global__ void k_arc_sum(const double *part, int nblocks, double *s)
 // roots and the divisions (slow in FP64 here) run across the block; one
 // thread adds in image order.  Strings of more than ARC_CUM_MAX images run
 // it all in one thread.
+//
+// A string of zero or non-finite length (all images equal, or a non-finite
+// field) has no arc length: the reference divides 0 by 0 there
+// (interpolation.cu:126-140).  Here *bad is set and s becomes the uniform
+// n / (F - 1), computed as the resample plan computes its output positions,
+// so that a linear resample onto as many images copies every image exactly;
+// the host reports the flag as an error.
 constexpr int ARC_CUM_MAX = 4096;
 
-__global__ void k_arc_cumulate(int F, double *s)
+__device__ __forceinline__ bool arc_total_ok(double t) { return t > 0.0 && t <= 1.7976931348623157e308; }
+
+__global__ void k_arc_cumulate(int F, double *s, int *bad)
 {
     __shared__ double r[ARC_CUM_MAX];
     __shared__ double total;
+    if (F == 1) {     // a single image has no length to normalise
+        if (threadIdx.x == 0) s[0] = 0.0;
+        return;
+    }
     if (F > ARC_CUM_MAX) {
         if (threadIdx.x == 0) {
             double acc = 0.0;
@@ -1249,7 +1262,9 @@ __global__ void k_arc_cumulate(int F, double *s)
                 acc += sqrt(s[n]);
                 s[n] = acc;
             }
-            for (int n = 0; n < F; ++n) s[n] /= acc;
+            const bool ok = arc_total_ok(acc);
+            if (!ok) atomicExch(bad, 1);
+            for (int n = 0; n < F; ++n) s[n] = ok ? s[n] / acc : (double)n / (double)(F - 1);
         }
         return;
     }
@@ -1262,9 +1277,28 @@ __global__ void k_arc_cumulate(int F, double *s)
             r[n] = acc;
         }
         total = acc;
+        if (!arc_total_ok(acc)) atomicExch(bad, 1);
     }
     __syncthreads();
-    for (int n = threadIdx.x; n < F; n += blockDim.x) s[n] = r[n] / total;
+    const bool ok = arc_total_ok(total);
+    for (int n = threadIdx.x; n < F; n += blockDim.x) s[n] = ok ? r[n] / total : (double)n / (double)(F - 1);
+}
+
+// Finiteness of the per-image scalars after a call's NLCG steps: the energy
+// (constant term of the last line polynomial) and |g|^2 of the slot the
+// last step wrote.  A NaN or infinite value (from non-finite fields, or a
+// step that overflowed) counts into status[1]; status[2] keeps the first
+// such image + 1.  The host reports them at its next synchronising call.
+__global__ void k_check_scalars(const double *fenergy, const double *gn, int n_images, int *status)
+{
+    const int n = blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= n_images) return;
+    const double e = fenergy[n], g = gn[n];
+    const double big = 1.7976931348623157e308;
+    if (!(fabs(e) <= big) || !(g <= big)) {
+        atomicAdd(status + 1, 1);
+        atomicCAS(status + 2, 0, n + 1);
+    }
 }
 
 // Redistribution plan: segment and weight per output image, and for the
@@ -1285,6 +1319,11 @@ __host__ __device__ inline size_t redist_plan_smem(int F, int F_new)
 {
     return (size_t)(6 * F + 1 + 2 * F_new) * sizeof(double) + (size_t)(F + F_new) * sizeof(int);
 }
+
+// Weight of the segment's end image.  A segment of zero length (two equal
+// adjacent images, where the reference divides 0 by 0) takes its end image:
+// both ends are the same state.
+__device__ __forceinline__ double redist_weight(double num, double len) { return len != 0.0 ? num / len : 1.0; }
 
 __global__ void k_redist_plan(const double *s_in, int F, int F_new, int cubic, int spline, RedistPlan p, int use_smem)
 {
@@ -1329,7 +1368,7 @@ __global__ void k_redist_plan(const double *s_in, int F, int F_new, int cubic, i
             if (k >= F) k = F - 1;
             kk[n] = k;
             if (use_smem) sst[n] = seg_start;
-            else p.w[n] = (s_new - seg_start) / (cubic ? h[k] : (s[k] - s[k - 1]));
+            else p.w[n] = redist_weight(s_new - seg_start, cubic ? h[k] : (s[k] - s[k - 1]));
         }
     }
     __syncthreads();
@@ -1337,7 +1376,7 @@ __global__ void k_redist_plan(const double *s_in, int F, int F_new, int cubic, i
         for (int n = t; n < F_new; n += nt) {
             const int k = kk[n];
             p.k[n] = k;
-            p.w[n] = (snew[n] - sst[n]) / (cubic ? h[k] : (s[k] - s[k - 1]));
+            p.w[n] = redist_weight(snew[n] - sst[n], cubic ? h[k] : (s[k] - s[k - 1]));
         }
     if (!cubic) {
         if (use_smem)
@@ -1829,8 +1868,14 @@ cudaError_t launch_apply_update(const Launch &L, const Scalars &sc, const String
     return cudaMemsetAsync(sc.alpha_pend, 0, sizeof(double) * total_images, L.stream);
 }
 
+cudaError_t launch_check_scalars(const Scalars &sc, int n_images, int slot, cudaStream_t st)
+{
+    k_check_scalars<<<(n_images + NT - 1) / NT, NT, 0, st>>>(sc.fenergy, slot ? sc.gn1 : sc.gn0, n_images, sc.status);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_arc_length(int precision, const void *const *fields, const int *width, int nf, long sites, int F,
-                              double *part, double *s, cudaStream_t st)
+                              double *part, double *s, int *bad, cudaStream_t st)
 {
     const int nb = (int)((sites + (long)NT * ARC_SPT - 1) / ((long)NT * ARC_SPT));
     const dim3 grid(nb, F);
@@ -1843,7 +1888,7 @@ cudaError_t launch_arc_length(int precision, const void *const *fields, const in
         k_arc_partial<float><<<grid, NT, 0, st>>>((const float *)f[0], (const float *)f[1], (const float *)f[2],
                                                   w[0], w[1], w[2], sites, part);
     k_arc_sum<<<F, NT, 0, st>>>(part, nb, s);
-    k_arc_cumulate<<<1, NT, 0, st>>>(F, s);
+    k_arc_cumulate<<<1, NT, 0, st>>>(F, s, bad);
     return cudaGetLastError();
 }
 

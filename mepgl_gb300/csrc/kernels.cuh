@@ -75,9 +75,16 @@ cudaError_t launch_jb(const Launch &L, const Scalars &sc, int xbuf, void *const 
 
 // Arc length of one string over nf per-image arrays of `width` reals per site
 // (reals of the context precision).  Result: s[0..F) (device doubles), using
-// part (>= tiles_per_image * F doubles) as scratch.
+// part (>= tiles_per_image * F doubles) as scratch.  A string of zero or
+// non-finite length sets *bad (device int) and gets the uniform s = n/(F-1).
 cudaError_t launch_arc_length(int precision, const void *const *fields, const int *width, int nf, long sites, int F,
-                              double *part, double *s, cudaStream_t st);
+                              double *part, double *s, int *bad, cudaStream_t st);
+// Device status flags (Scalars::status): [0] a stage wait of the fused NLCG
+// launch ran out; [1] count of non-finite per-image scalars after NLCG steps,
+// [2] the first such image + 1; [3] a string of zero or non-finite arc length.
+constexpr int STATUS_WAIT = 0, STATUS_NONFINITE = 1, STATUS_NONFINITE_IMAGE = 2, STATUS_ARC = 3;
+// Checks energy and |g|^2 (slot 0 or 1) of n_images images (see STATUS_NONFINITE).
+cudaError_t launch_check_scalars(const Scalars &sc, int n_images, int slot, cudaStream_t st);
 // Initial-guess parameters of launch_generate (see mepgl_guess).
 struct GuessParams {
     double x0, y0, dx, psi_abs_1, psi_abs_2, noise, b_z;
