@@ -360,6 +360,61 @@ mepgl_status mepgl_free_energy_noalloc(int nx, int ny, int n_images, int multico
 /* Message of the last failed mepgl_free_energy_noalloc on this thread. */
 const char *mepgl_noalloc_last_error(void);
 
+/* Refinement of images to stationary points of the free energy (no
+ * reference counterpart: the reference's barrier is the largest image
+ * energy of the relaxed string, mepgl/post.py:188, which depends on the
+ * image count and the reparametrization cadence).  Each image of the
+ * context's string (FP64 single-string contexts, reference discretisation)
+ * is refined in place, per kind[n]:
+ *   MEPGL_STATIONARY_MINIMUM  to a local minimum (a string end state);
+ *   MEPGL_STATIONARY_SADDLE   to an index-1 saddle (the transition state),
+ *                             by min-mode Newton: the lowest Hessian mode by
+ *                             Lanczos, an uphill Newton step along it and a
+ *                             shifted Newton step (Levenberg-Marquardt, by
+ *                             conjugate gradients) in its complement;
+ *   MEPGL_STATIONARY_SKIP     left unchanged.
+ * Each iteration first minimises over smooth gauge transformations of the
+ * image (Legendre products of total degree <= gauge_degree), along which
+ * the reference's discretisation is gauge invariant only to O(dx^2): the
+ * energy there is nearly flat and the orbits curved, which stalls Newton
+ * steps taken in straight lines.  Hessian-vector products are central
+ * differences of the gradient, in IEEE double.  mode_a / mode_psi_1 /
+ * mode_psi_2 (layout of the fields, `memory` host or device; NULL for all
+ * three continues from the modes of the previous call) give the initial
+ * direction of each saddle image, e.g. the string's chord tangent
+ * x_{k+1} - x_{k-1}; other images' entries are ignored.  Stops per image
+ * when |g| (Euclidean norm over the image's fields) <= g_tol or after
+ * max_newton iterations; the report (host array of F, may be NULL) gives
+ * energy, |g|, the lowest curvature and counts.  Workspace (about 41
+ * copies of the fields) is allocated on the first call and kept. */
+enum { MEPGL_STATIONARY_MINIMUM = 0, MEPGL_STATIONARY_SADDLE = 1, MEPGL_STATIONARY_SKIP = 2 };
+
+typedef struct mepgl_refine_options {
+    double g_tol;              /* |g| target (default 1e-8)                       */
+    int32_t max_newton;        /* Newton iterations (default 40)                  */
+    int32_t max_cg;            /* CG iterations per linear solve (default 3000)   */
+    int32_t lanczos_steps;     /* per min-mode update (default 12, 30 at start)   */
+    int32_t gauge_degree;      /* gauge polynomial degree <= 16, 0 = off,
+                                  -1 = auto: max(nx, ny) / 8 within 4..16 (default) */
+    double mu0;                /* initial Levenberg-Marquardt shift (1e-3)        */
+    double cg_eta;             /* CG relative tolerance cap (0.1)                 */
+    int32_t max_retries;       /* rejected steps retried per iteration (8)        */
+    int32_t pad;
+} mepgl_refine_options;
+
+typedef struct mepgl_refine_report {
+    double energy;             /* free energy after the refinement                */
+    double g_norm;             /* |g| after the refinement                        */
+    double min_curvature;      /* saddles: the lowest Hessian eigenvalue          */
+    double mu;                 /* Levenberg-Marquardt shift reached               */
+    int32_t newton_iterations, cg_iterations, gradient_evaluations, converged;
+} mepgl_refine_report;
+
+void mepgl_default_refine_options(mepgl_refine_options *opt);
+mepgl_status mepgl_refine_stationary(mepgl_ctx *ctx, const int32_t *kind, const void *mode_a,
+                                     const void *mode_psi_1, const void *mode_psi_2, int memory,
+                                     const mepgl_refine_options *opt, mepgl_refine_report *report);
+
 /* Wait for the context's stream. */
 mepgl_status mepgl_synchronize(mepgl_ctx *ctx);
 

@@ -24,8 +24,8 @@ CLI = os.path.join(LIB_DIR, "mepgl")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-Werror=return-type",
               "--diag-error=940", "--expt-relaxed-constexpr", "-Xptxas", "-warn-spills"]
-CU_SOURCES = ["kernels.cu", "api.cu"]
-HEADERS = ["common.cuh", "site_ops.cuh", "site_pair.cuh", "kernels.cuh", "strip.cuh", "pair_float.cuh"]
+CU_SOURCES = ["kernels.cu", "api.cu", "refine.cu"]
+HEADERS = ["common.cuh", "site_ops.cuh", "site_pair.cuh", "kernels.cuh", "strip.cuh", "pair_float.cuh", "context.h"]
 
 
 def nvcc() -> str:

@@ -16,8 +16,7 @@
 #include <tuple>
 #include <vector>
 
-#include "../../include/mepgl.h"
-#include "kernels.cuh"
+#include "context.h"
 
 using namespace mepgl;
 
@@ -25,58 +24,7 @@ namespace {
 
 thread_local std::string g_create_error;
 
-struct StringHost {
-    int nx, ny, F;
-    long M() const { return (long)nx * ny; }
-    std::vector<double> params[9];     // a1 b1 mxx1 myy1 a2 b2 mxx2 myy2 h (host copy)
-    std::vector<int32_t> comp, sc;
-    bool uniform;
-    void *dparams[9] = {};             // per-site arrays (type T) when not uniform
-    uint16_t *dmask = nullptr;
-    void *x[2][3] = {}, *g[2][3] = {}, *d[2][3] = {};
-    double q[2], eta, gamma, delta, dx;
-};
-
 }  // namespace
-
-struct mepgl_ctx {
-    int ncomp = 1, thin_film = 0, precision = 1;
-    mepgl_options opt{};
-    cudaStream_t stream = nullptr;
-    bool own_stream = false;
-    std::vector<StringHost> strings;
-    std::vector<StringDesc> hdesc;
-    // strings are grouped MAX_STRINGS at a time; each group is one launch per
-    // pass, its descriptors passed by value to the kernels
-    std::vector<Batch> batches;
-    std::vector<int> batch_tile0, batch_ntiles, string_batch;
-    TileRef *dtiles = nullptr;
-    int n_tiles = 0, total_images = 0;
-    unsigned long long *fqueue = nullptr;   // work counter of the fused NLCG launch
-    unsigned *fstage = nullptr;             // per-image stage counters of the fused NLCG launch
-    std::vector<int> string_tile0, string_ntiles;
-    Scalars sc{};
-    double *dscratch = nullptr;   // per-image temporaries (energies, 3 adjoints)
-    double *ds = nullptr, *ds_jb = nullptr;   // arc lengths of string 0
-    RedistPlan plan{};
-    int plan_cap = 0;
-    void *cubic_scratch = nullptr;   // cubic resample columns of strings too long for shared memory
-    size_t cubic_cap = 0;
-    int xi = 0, di = 0;           // current x / d buffers
-    bool pending = false;         // an NLCG update not yet applied to x
-    int64_t launches = 0;
-    std::string err;
-    std::map<std::tuple<int, int, int, int>, cudaGraphExec_t> graphs;
-    std::vector<double> host_s, host_sjb;
-    int sm_count = 152;
-    // staged state (mepgl_stage_state): a copy of the next state in flight on
-    // a second stream while the context computes
-    void *stage[3] = {nullptr, nullptr, nullptr};
-    size_t stage_bytes = 0;
-    cudaStream_t copy_stream = nullptr;
-    cudaEvent_t stage_done = nullptr;
-    bool staged = false;
-};
 
 namespace {
 
@@ -776,6 +724,13 @@ mepgl_status reset_cg(mepgl_ctx *c, int first, int last)
 
 }  // namespace
 
+namespace mepgl {
+mepgl_status ctx_fail(mepgl_ctx *c, mepgl_status st, const std::string &msg) { return fail(c, st, msg); }
+Launch ctx_string_launch(mepgl_ctx *c, int si) { return string_launch(c, si); }
+mepgl_status ctx_flush(mepgl_ctx *c) { return flush(c); }
+mepgl_status ctx_check_device_status(mepgl_ctx *c) { return check_device_status(c); }
+}  // namespace mepgl
+
 // ======================================================================= ABI
 extern "C" {
 
@@ -902,6 +857,8 @@ mepgl_status mepgl_destroy(mepgl_ctx *c)
         free_string_params(s);
     }
     free_scalars(c);
+    refine_free(c->refine);
+    c->refine = nullptr;
     RedistPlan &p = c->plan;
     cudaFree(p.k); cudaFree(p.w); cudaFree(p.h); cudaFree(p.dl); cudaFree(p.d); cudaFree(p.du); cudaFree(p.du2);
     cudaFree(p.ipiv); cudaFree(p.status); cudaFree(p.aux);

@@ -1,0 +1,1162 @@
+// refine.cu -- refinement of a string's images to stationary points of the
+// free energy: minima, and index-1 saddles (the transition state whose energy
+// above the initial minimum is the barrier, mepgl/post.py:188).
+//
+// The reference has no such step: its barrier is the largest image energy
+// of the relaxed string, which depends on the image count and on the
+// reparametrization cadence.  Here the string only seeds the refinement.
+//
+// Method (per image, all images of the context advanced by the same
+// launches, each with its own scalars):
+//
+//  * Gauge step.  The reference's linearised covariant differences and
+//    collocated curl views (mepgl/src/nlcg.cu:149-203) are gauge invariant
+//    only to O(dx^2), so smooth gauge transformations A -> A + grad chi,
+//    psi_a -> psi_a exp(i q_a chi) change the energy very little (curvature
+//    ~1e-6 for chi linear in x on the 64x64 string) and move along curved
+//    orbits, where a straight Newton step leaves the orbit and is rejected.
+//    Each Newton iteration therefore first minimises the energy over
+//    chi = sum_m c_m P_a(X) P_b(Y) (Legendre products, 1 <= a + b <= degree)
+//    along the exact orbit: the m x m Hessian of E(c) comes from central
+//    differences of the orbit gradient dE/dc_m = g . J phi_m, and the step is
+//    applied as an exact gauge transformation.
+//  * Min mode (saddles).  The lowest Hessian eigenpair (lambda_1, v_1) by
+//    Lanczos with full reorthogonalisation, restarted from the previous v_1
+//    (first call: the caller's direction, e.g. the string's chord tangent).
+//  * Newton step.  Along v_1: p_1 = g.v_1 / |lambda_1| (uphill); in the
+//    complement: (H + mu) p = -(g - (g.v_1) v_1) projected, by conjugate
+//    gradients.  Minima use plain shifted CG.  Hessian-vector products are
+//    central differences of the gradient kernel, H u = (g(x + h u) -
+//    g(x - h u)) / 2h, with |h u| = 1e-6 sqrt(dof).
+//  * Globalisation.  The step is kept when it lowers |g|^2 (for an index-1
+//    saddle the modified force -g + 2 (g.v_1) v_1 is a descent direction of
+//    |g|^2); then mu /= 4, else mu *= 4 and the solve is repeated
+//    (Levenberg-Marquardt).
+//
+// Everything runs in IEEE double on the context's FP64 buffers; the CG
+// scalars live on the device, so its iterations run as replays of a captured
+// CUDA graph with no host round trip inside.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <vector>
+
+#include "context.h"
+
+namespace mepgl {
+
+constexpr int RF_MAX_LZ = 32;       // Lanczos vectors
+constexpr int RF_MAX_DEG = 16;      // gauge polynomial degree
+constexpr int RF_MAX_GB = (RF_MAX_DEG + 1) * (RF_MAX_DEG + 2) / 2 - 1;   // 152 basis functions
+constexpr int RF_GB_CHUNK = 16;     // basis functions per block of the gauge-dot kernel
+constexpr int RF_DOTS = 40;         // per-image dot results kept per launch
+constexpr int RF_NB = 64;           // blocks per image of the vector kernels (upper bound)
+
+// per-image device scalars (sc[n * NSC + k])
+enum { S_ACTIVE, S_RR, S_R0, S_ETA, S_ALPHA, S_BETA, S_H, S_INV2H, S_MU, S_V1Y, S_G1, S_P1, S_DELTA, S_IT, S_NEG,
+       S_ACCEPT, S_INVB, S_ONE, NSC };
+enum { OP_NONE, OP_FDSTEP, OP_STORE_V1Y, OP_ALPHA, OP_BETA, OP_CGINIT, OP_STORE_G1, OP_UNIT };
+
+// One vector of the context's shape: nf arrays of F*M (x, y) / (Re, Im) double pairs.
+struct Vec {
+    double *p[3];
+};
+
+struct Term {
+    int in;          // input index
+    int s1, s2;      // scalar indices multiplying the coefficient (-1: none)
+    int cidx;        // coefficient column of `coef` (-1: none)
+    double mult;
+};
+
+struct LinArgs {
+    Vec in[4];
+    Term t[4];
+    int nt;
+    Vec out;
+    int gate;            // scalar index: images whose scalar is 0 are not written (-1: all)
+    Vec dw;              // partial dot of out with dw (dw.p[0] == null: none)
+    int dot_slot;        // K index of that partial
+    int dot_k;           // K of the partial buffer layout
+};
+
+struct RefineWork {
+    int F = 0, nf = 0, nx = 0, ny = 0;
+    long M = 0;
+    int nb = 1;                       // blocks per image in the vector kernels
+    double *block = nullptr;          // all workspace vectors
+    size_t vs = 0;                    // doubles per vector
+    Vec g, v1, p, r, y, s, gp, gm;
+    Vec lz[RF_MAX_LZ + 1];
+    double *part = nullptr;           // partial sums [F][K][nb]
+    double *dots = nullptr;           // [F][RF_DOTS]
+    double *sc = nullptr;             // [F][NSC]
+    double *coef = nullptr;           // [F][RF_MAX_LZ + 1] host-given coefficients
+    double *gcoef = nullptr;          // [F][RF_MAX_GB] gauge coefficients
+    double *gd = nullptr;             // gauge orbit gradients [F][(2 m + 1) m], m <= RF_MAX_GB
+    std::vector<double> lam1, mu;
+    std::vector<int> has_mode;        // a saddle image has a direction to start its Lanczos from
+    std::vector<int> fresh;           // that direction is the caller's (longer first Lanczos)
+    cudaGraphExec_t cg_graph[2] = {nullptr, nullptr};   // CG iterations, per current x buffer
+    int64_t graph_launches = 0, graph_grads = 0;        // kernels and gradients per replay
+};
+
+void refine_free(RefineWork *w)
+{
+    if (!w) return;
+    for (auto &g : w->cg_graph)
+        if (g) cudaGraphExecDestroy(g);
+    cudaFree(w->block);
+    cudaFree(w->part);
+    cudaFree(w->dots);
+    cudaFree(w->sc);
+    cudaFree(w->coef);
+    cudaFree(w->gcoef);
+    cudaFree(w->gd);
+    delete w;
+}
+
+namespace {
+
+// ------------------------------------------------------------------ kernels
+__device__ __forceinline__ double block_reduce(double v, double *sh)
+{
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+    __syncthreads();
+    if (l == 0) sh[w] = v;
+    __syncthreads();
+    double t = 0.0;
+    if (threadIdx.x == 0)
+        for (int k = 0; k < (int)(blockDim.x >> 5); ++k) t += sh[k];
+    return t;   // valid in thread 0
+}
+
+// Element e of image n of vector v (e < nf * 2M): array e / 2M, offset e % 2M.
+__device__ __forceinline__ double *velem(const Vec &v, int n, long M2, long e)
+{
+    const int f = (int)(e / M2);
+    return v.p[f] + ((long)n * M2 + (e - f * M2));
+}
+
+// out = sum_t c_t in_t, per image; optional partial dot of out with dw.
+__global__ void __launch_bounds__(NT) k_lincomb(LinArgs a, long M2, int nf, const double *sc, const double *coef,
+                                                int ccols, double *part, int nb)
+{
+    __shared__ double sh[NT / 32];
+    const int n = blockIdx.y;
+    const bool on = a.gate < 0 || sc[n * NSC + a.gate] != 0.0;
+    double c[4] = {0, 0, 0, 0};
+    for (int k = 0; k < a.nt; ++k) {
+        double v = a.t[k].mult;
+        if (a.t[k].s1 >= 0) v *= sc[n * NSC + a.t[k].s1];
+        if (a.t[k].s2 >= 0) v *= sc[n * NSC + a.t[k].s2];
+        if (a.t[k].cidx >= 0) v *= coef[n * ccols + a.t[k].cidx];
+        c[k] = v;
+    }
+    const long len = nf * M2, per = (len + nb - 1) / nb;
+    const long e0 = blockIdx.x * per, e1 = min(len, e0 + per);
+    double acc = 0.0;
+    if (on)
+        for (long e = e0 + threadIdx.x; e < e1; e += NT) {
+            double v = 0.0;
+            for (int k = 0; k < a.nt; ++k) v += c[k] * *velem(a.in[a.t[k].in], n, M2, e);
+            *velem(a.out, n, M2, e) = v;
+            if (a.dw.p[0]) acc += v * *velem(a.dw, n, M2, e);
+        }
+    if (a.dw.p[0]) {
+        const double t = block_reduce(acc, sh);
+        if (threadIdx.x == 0) part[((long)n * a.dot_k + a.dot_slot) * nb + blockIdx.x] = t;
+    }
+}
+
+// Partial dots of up to 4 pairs (u_k, w_k) per image.
+struct DotArgs {
+    Vec u[4], w[4];
+    int k;
+};
+
+__global__ void __launch_bounds__(NT) k_dots(DotArgs a, long M2, int nf, double *part, int nb)
+{
+    __shared__ double sh[NT / 32];
+    const int n = blockIdx.y;
+    const long len = nf * M2, per = (len + nb - 1) / nb;
+    const long e0 = blockIdx.x * per, e1 = min(len, e0 + per);
+    double acc[4] = {0, 0, 0, 0};
+    for (long e = e0 + threadIdx.x; e < e1; e += NT)
+        for (int k = 0; k < a.k; ++k) acc[k] += *velem(a.u[k], n, M2, e) * *velem(a.w[k], n, M2, e);
+    for (int k = 0; k < a.k; ++k) {
+        const double t = block_reduce(acc[k], sh);
+        if (threadIdx.x == 0) part[((long)n * a.k + k) * nb + blockIdx.x] = t;
+    }
+}
+
+// Partial dots of w with Lanczos vectors lz_0 .. lz_{K-1} (contiguous, stride vs).
+__global__ void __launch_bounds__(NT) k_dots_lz(Vec w, const double *lz0, size_t vs, int K, long M2, int nf,
+                                                long FM2, double *part, int nb)
+{
+    __shared__ double sh[NT / 32];
+    const int n = blockIdx.y;
+    const long len = nf * M2, per = (len + nb - 1) / nb;
+    const long e0 = blockIdx.x * per, e1 = min(len, e0 + per);
+    for (int k = 0; k < K; ++k) {
+        double acc = 0.0;
+        const double *base = lz0 + k * vs;
+        for (long e = e0 + threadIdx.x; e < e1; e += NT) {
+            const int f = (int)(e / M2);
+            acc += base[f * FM2 + (long)n * M2 + (e - f * M2)] * *velem(w, n, M2, e);
+        }
+        const double t = block_reduce(acc, sh);
+        if (threadIdx.x == 0) part[((long)n * K + k) * nb + blockIdx.x] = t;
+    }
+}
+
+// w = c0 w - sum_k d_k lz_k, d_k = d[n * dstride + k].
+__global__ void __launch_bounds__(NT) k_sub_lz(Vec w, double c0, const double *lz0, size_t vs, int K, long M2, int nf,
+                                               long FM2, const double *d, int dstride, const double *sc, int gate,
+                                               int nb)
+{
+    const int n = blockIdx.y;
+    if (gate >= 0 && sc[n * NSC + gate] == 0.0) return;
+    double dk[RF_MAX_LZ + 1];
+    for (int k = 0; k < K; ++k) dk[k] = d[n * dstride + k];
+    const long len = nf * M2, per = (len + nb - 1) / nb;
+    const long e0 = blockIdx.x * per, e1 = min(len, e0 + per);
+    for (long e = e0 + threadIdx.x; e < e1; e += NT) {
+        const int f = (int)(e / M2);
+        const long o = f * FM2 + (long)n * M2 + (e - f * M2);
+        double v = c0 * *velem(w, n, M2, e);
+        for (int k = 0; k < K; ++k) v -= dk[k] * lz0[k * vs + o];
+        *velem(w, n, M2, e) = v;
+    }
+}
+
+// Per-image sums of the partials, then the scalar step `op` (thread 0).
+__global__ void __launch_bounds__(NT) k_dot_sums(const double *part, int K, int nb, double *dots, double *sc, int op)
+{
+    __shared__ double sh[NT / 32];
+    const int n = blockIdx.x;
+    double s[RF_DOTS];
+    for (int k = 0; k < K; ++k) {
+        double v = 0.0;
+        for (int b = threadIdx.x; b < nb; b += NT) v += part[((long)n * K + k) * nb + b];
+        s[k] = block_reduce(v, sh);
+    }
+    if (threadIdx.x != 0) return;
+    for (int k = 0; k < K; ++k) dots[n * RF_DOTS + k] = s[k];
+    double *q = sc + n * NSC;
+    const bool act = q[S_ACTIVE] != 0.0;
+    switch (op) {
+    case OP_FDSTEP:   // s[0] = |u|^2: central-difference step for H u
+        if (act && s[0] > 0) {
+            q[S_H] = q[S_DELTA] / sqrt(s[0]);
+            q[S_INV2H] = 0.5 / q[S_H];
+        } else {      // inactive, or u = 0: H u = 0
+            q[S_H] = 0.0;
+            q[S_INV2H] = 0.0;
+        }
+        break;
+    case OP_STORE_V1Y: q[S_V1Y] = s[0]; break;
+    case OP_STORE_G1: q[S_G1] = s[0]; break;
+    case OP_ALPHA:    // s[0] = p . (H + mu) p
+        if (act) {
+            if (s[0] > 0) q[S_ALPHA] = q[S_RR] / s[0];
+            else { q[S_ALPHA] = 0.0; q[S_ACTIVE] = 0.0; q[S_NEG] = 1.0; }
+        } else {
+            q[S_ALPHA] = 0.0;
+        }
+        break;
+    case OP_BETA:     // s[0] = |r_new|^2
+        if (act) {
+            q[S_BETA] = q[S_RR] > 0 ? s[0] / q[S_RR] : 0.0;
+            q[S_RR] = s[0];
+            q[S_IT] += 1.0;
+            if (!(sqrt(s[0]) > q[S_ETA] * q[S_R0])) q[S_ACTIVE] = 0.0;
+        } else {
+            q[S_BETA] = 0.0;
+        }
+        break;
+    case OP_CGINIT:   // s[0] = |r_0|^2
+        q[S_RR] = s[0];
+        q[S_R0] = sqrt(s[0]);
+        q[S_IT] = 0.0;
+        q[S_NEG] = 0.0;
+        if (!(s[0] > 0)) q[S_ACTIVE] = 0.0;
+        break;
+    case OP_UNIT:     // s[0] = |w|^2: 1/|w| for normalisation
+        q[S_INVB] = s[0] > 0 ? 1.0 / sqrt(s[0]) : 0.0;
+        break;
+    default: break;
+    }
+}
+
+// ---------------------------------------------------------- gauge kernels
+// Legendre polynomials P_0..P_deg at t.
+__device__ __forceinline__ void legendre(double t, int deg, double *P)
+{
+    P[0] = 1.0;
+    if (deg >= 1) P[1] = t;
+    for (int k = 1; k < deg; ++k) P[k + 1] = ((2 * k + 1) * t * P[k] - k * P[k - 1]) / (k + 1);
+}
+
+struct GaugeBasis {
+    int deg, m;
+    unsigned char a[RF_MAX_GB], b[RF_MAX_GB];
+};
+
+__device__ __forceinline__ double coord(int i, int n) { return n > 1 ? (2.0 * i - (n - 1)) / (n - 1) : 0.0; }
+
+// chi at lattice column i, row j: sum_m c_m P_a(X_i) P_b(Y_j) (only >= 0: that basis function alone)
+__device__ double chi_at(const GaugeBasis &B, const double *c, int only, int i, int j, int nx, int ny)
+{
+    double Px[RF_MAX_DEG + 1], Py[RF_MAX_DEG + 1];
+    legendre(coord(i, nx), B.deg, Px);
+    legendre(coord(j, ny), B.deg, Py);
+    if (only >= 0) return Px[B.a[only]] * Py[B.b[only]];
+    double v = 0.0;
+    for (int m = 0; m < B.m; ++m) v += c[m] * Px[B.a[m]] * Py[B.b[m]];
+    return v;
+}
+
+struct GaugeField {
+    double chi, gx, gy;   // chi and its lattice gradient (central, one-sided at the edges)
+};
+
+__device__ GaugeField gauge_field(const GaugeBasis &B, const double *c, int only, int i, int j, int nx, int ny,
+                                  double idx)
+{
+    GaugeField G;
+    G.chi = chi_at(B, c, only, i, j, nx, ny);
+    const int il = i > 0 ? i - 1 : i, ir = i < nx - 1 ? i + 1 : i;
+    const int jd = j > 0 ? j - 1 : j, ju = j < ny - 1 ? j + 1 : j;
+    G.gx = (chi_at(B, c, only, ir, j, nx, ny) - chi_at(B, c, only, il, j, nx, ny)) * idx / (ir - il);
+    G.gy = (chi_at(B, c, only, i, ju, nx, ny) - chi_at(B, c, only, i, jd, nx, ny)) * idx / (ju - jd);
+    return G;
+}
+
+// out = U(mult * chi_n) in: A + grad chi, psi_a exp(i q_a chi); chi_n from coef[n][:] (or basis `only`).
+__global__ void __launch_bounds__(NT) k_gauge_apply(Vec in, Vec out, GaugeBasis B, const double *coef, int ccols,
+                                                    int only, double mult, int nx, int ny, int ncomp, double q1,
+                                                    double q2, double idx, const double *sc, int gate)
+{
+    const int n = blockIdx.y;
+    if (gate >= 0 && sc[n * NSC + gate] == 0.0) return;
+    const long M = (long)nx * ny;
+    for (long s = blockIdx.x * (long)NT + threadIdx.x; s < M; s += (long)gridDim.x * NT) {
+        const int i = (int)(s % nx), j = (int)(s / nx);
+        const GaugeField G = gauge_field(B, coef + n * ccols, only, i, j, nx, ny, idx);
+        const long o = 2 * ((long)n * M + s);
+        out.p[0][o] = in.p[0][o] + mult * G.gx;
+        out.p[0][o + 1] = in.p[0][o + 1] + mult * G.gy;
+        for (int a = 0; a < ncomp; ++a) {
+            double sn, cs;
+            sincos((a ? q2 : q1) * mult * G.chi, &sn, &cs);
+            const double re = in.p[1 + a][o], im = in.p[1 + a][o + 1];
+            out.p[1 + a][o] = re * cs - im * sn;
+            out.p[1 + a][o + 1] = re * sn + im * cs;
+        }
+    }
+}
+
+// Partials of dE/dc_m = g . J phi_m = sum_s g_A . grad phi_m + sum_a q_a phi_m (Re psi_a g_Im,a - Im psi_a g_Re,a),
+// for the basis functions [16 z, 16 z + 16) of block row z.
+__global__ void __launch_bounds__(NT) k_gauge_dots(Vec x, Vec g, GaugeBasis B, int nx, int ny, int ncomp, double q1,
+                                                   double q2, double idx, double *part, int nb)
+{
+    __shared__ double sh[NT / 32];
+    const int n = blockIdx.y, m0 = blockIdx.z * RF_GB_CHUNK;
+    const int mc = min(RF_GB_CHUNK, B.m - m0);
+    const long M = (long)nx * ny, per = (M + nb - 1) / nb;
+    const long s0 = blockIdx.x * per, s1 = min(M, s0 + per);
+    double acc[RF_GB_CHUNK];
+#pragma unroll
+    for (int m = 0; m < RF_GB_CHUNK; ++m) acc[m] = 0.0;
+    for (long s = s0 + threadIdx.x; s < s1; s += NT) {
+        const int i = (int)(s % nx), j = (int)(s / nx);
+        const long o = 2 * ((long)n * M + s);
+        const double gax = g.p[0][o], gay = g.p[0][o + 1];
+        double w = 0.0;
+        for (int a = 0; a < ncomp; ++a)
+            w += (a ? q2 : q1) * (x.p[1 + a][o] * g.p[1 + a][o + 1] - x.p[1 + a][o + 1] * g.p[1 + a][o]);
+        double Px[3][RF_MAX_DEG + 1], Py[3][RF_MAX_DEG + 1];
+        const int il = i > 0 ? i - 1 : i, ir = i < nx - 1 ? i + 1 : i;
+        const int jd = j > 0 ? j - 1 : j, ju = j < ny - 1 ? j + 1 : j;
+        legendre(coord(i, nx), B.deg, Px[0]);
+        legendre(coord(il, nx), B.deg, Px[1]);
+        legendre(coord(ir, nx), B.deg, Px[2]);
+        legendre(coord(j, ny), B.deg, Py[0]);
+        legendre(coord(jd, ny), B.deg, Py[1]);
+        legendre(coord(ju, ny), B.deg, Py[2]);
+        const double sx = idx / (ir - il), sy = idx / (ju - jd);
+#pragma unroll
+        for (int m = 0; m < RF_GB_CHUNK; ++m) {
+            if (m < mc) {
+                const int pa = B.a[m0 + m], pb = B.b[m0 + m];
+                const double phi = Px[0][pa] * Py[0][pb];
+                const double dxp = (Px[2][pa] - Px[1][pa]) * Py[0][pb] * sx;
+                const double dyp = Px[0][pa] * (Py[2][pb] - Py[1][pb]) * sy;
+                acc[m] += gax * dxp + gay * dyp + w * phi;
+            }
+        }
+    }
+#pragma unroll
+    for (int m = 0; m < RF_GB_CHUNK; ++m) {
+        if (m < mc) {
+            const double t = block_reduce(acc[m], sh);
+            if (threadIdx.x == 0) part[((long)n * B.m + m0 + m) * nb + blockIdx.x] = t;
+        }
+    }
+}
+
+// Sums of gauge partials into gd[n][slot * m + k].
+__global__ void __launch_bounds__(NT) k_gauge_sums(const double *part, int m, int nb, double *gd, int gstride, int slot)
+{
+    __shared__ double sh[NT / 32];
+    const int n = blockIdx.x;
+    for (int k = 0; k < m; ++k) {
+        double v = 0.0;
+        for (int b = threadIdx.x; b < nb; b += NT) v += part[((long)n * m + k) * nb + b];
+        const double t = block_reduce(v, sh);
+        if (threadIdx.x == 0) gd[(long)n * gstride + slot * m + k] = t;
+    }
+}
+
+// ------------------------------------------------------------ host helpers
+// Symmetric eigen-decomposition by cyclic Jacobi rotations: eigenvalues
+// ascending in w, eigenvectors in the columns of V (row-major n x n).
+void jacobi_eig(int n, std::vector<double> A, std::vector<double> &w, std::vector<double> &V)
+{
+    V.assign(n * n, 0.0);
+    for (int i = 0; i < n; ++i) V[i * n + i] = 1.0;
+    for (int sweep = 0; sweep < 100; ++sweep) {
+        double off = 0.0, tot = 0.0;
+        for (int i = 0; i < n; ++i)
+            for (int j = 0; j < n; ++j) {
+                tot += A[i * n + j] * A[i * n + j];
+                if (i != j) off += A[i * n + j] * A[i * n + j];
+            }
+        if (off <= 1e-30 * tot || off == 0.0) break;
+        for (int p = 0; p < n; ++p)
+            for (int q = p + 1; q < n; ++q) {
+                const double apq = A[p * n + q];
+                if (apq == 0.0) continue;
+                const double th = (A[q * n + q] - A[p * n + p]) / (2 * apq);
+                const double t = (th >= 0 ? 1.0 : -1.0) / (std::fabs(th) + std::sqrt(th * th + 1));
+                const double c = 1 / std::sqrt(t * t + 1), s = t * c;
+                for (int k = 0; k < n; ++k) {
+                    const double akp = A[k * n + p], akq = A[k * n + q];
+                    A[k * n + p] = c * akp - s * akq;
+                    A[k * n + q] = s * akp + c * akq;
+                }
+                for (int k = 0; k < n; ++k) {
+                    const double apk = A[p * n + k], aqk = A[q * n + k];
+                    A[p * n + k] = c * apk - s * aqk;
+                    A[q * n + k] = s * apk + c * aqk;
+                }
+                for (int k = 0; k < n; ++k) {
+                    const double vkp = V[k * n + p], vkq = V[k * n + q];
+                    V[k * n + p] = c * vkp - s * vkq;
+                    V[k * n + q] = s * vkp + c * vkq;
+                }
+            }
+    }
+    std::vector<int> ord(n);
+    for (int i = 0; i < n; ++i) ord[i] = i;
+    std::sort(ord.begin(), ord.end(), [&](int a, int b) { return A[a * n + a] < A[b * n + b]; });
+    w.resize(n);
+    std::vector<double> V2(n * n);
+    for (int k = 0; k < n; ++k) {
+        w[k] = A[ord[k] * n + ord[k]];
+        for (int i = 0; i < n; ++i) V2[i * n + k] = V[i * n + ord[k]];
+    }
+    V.swap(V2);
+}
+
+// Cholesky solve of the SPD system H c = -g (m x m, row-major); false if H is not positive definite.
+bool cholesky_solve(int m, std::vector<double> H, const double *g, double *c)
+{
+    for (int j = 0; j < m; ++j) {
+        double d = H[j * m + j];
+        for (int k = 0; k < j; ++k) d -= H[j * m + k] * H[j * m + k];
+        if (!(d > 0)) return false;
+        d = std::sqrt(d);
+        H[j * m + j] = d;
+        for (int i = j + 1; i < m; ++i) {
+            double v = H[i * m + j];
+            for (int k = 0; k < j; ++k) v -= H[i * m + k] * H[j * m + k];
+            H[i * m + j] = v / d;
+        }
+    }
+    std::vector<double> y(m);
+    for (int i = 0; i < m; ++i) {
+        double v = -g[i];
+        for (int k = 0; k < i; ++k) v -= H[i * m + k] * y[k];
+        y[i] = v / H[i * m + i];
+    }
+    for (int i = m - 1; i >= 0; --i) {
+        double v = y[i];
+        for (int k = i + 1; k < m; ++k) v -= H[k * m + i] * c[k];
+        c[i] = v / H[i * m + i];
+    }
+    return true;
+}
+
+struct Ctx {
+    mepgl_ctx *c;
+    RefineWork *w;
+    Launch L;
+    int F;
+    long M2;
+    cudaStream_t st;
+    int64_t grads = 0;
+    std::vector<double> hsc;   // host copy of the scalars
+
+    Vec x() const
+    {
+        const StringHost &s = c->strings[0];
+        return Vec{{(double *)s.x[c->xi][0], (double *)s.x[c->xi][1], (double *)s.x[c->xi][2]}};
+    }
+    Vec xt() const
+    {
+        const StringHost &s = c->strings[0];
+        return Vec{{(double *)s.x[c->xi ^ 1][0], (double *)s.x[c->xi ^ 1][1], (double *)s.x[c->xi ^ 1][2]}};
+    }
+    dim3 vgrid() const { return dim3(w->nb, F); }
+
+    cudaError_t grad(int xbuf, const Vec &out)
+    {
+        FieldPtrs fp;
+        for (int f = 0; f < 3; ++f) fp.p[f] = f < w->nf ? out.p[f] : nullptr;
+        ++grads;
+        c->launches += 1;
+        return launch_gradient_only(L, xbuf, fp, 0);
+    }
+    cudaError_t lin(const LinArgs &a)
+    {
+        k_lincomb<<<vgrid(), NT, 0, st>>>(a, M2, w->nf, w->sc, w->coef, RF_MAX_LZ + 1, w->part, w->nb);
+        c->launches += 1;
+        return cudaGetLastError();
+    }
+    cudaError_t sums(int K, int op)
+    {
+        k_dot_sums<<<F, NT, 0, st>>>(w->part, K, w->nb, w->dots, w->sc, op);
+        c->launches += 1;
+        return cudaGetLastError();
+    }
+    cudaError_t dots(std::initializer_list<std::pair<Vec, Vec>> pairs, int op)
+    {
+        DotArgs a;
+        memset(&a, 0, sizeof(a));
+        for (auto &pr : pairs) {
+            a.u[a.k] = pr.first;
+            a.w[a.k] = pr.second;
+            ++a.k;
+        }
+        k_dots<<<vgrid(), NT, 0, st>>>(a, M2, w->nf, w->part, w->nb);
+        c->launches += 1;
+        cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) return e;
+        return sums(a.k, op);
+    }
+    cudaError_t read_scalars()
+    {
+        hsc.resize((size_t)F * NSC);
+        cudaError_t e = cudaMemcpyAsync(hsc.data(), w->sc, hsc.size() * 8, cudaMemcpyDeviceToHost, st);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+        return e;
+    }
+    cudaError_t write_scalars()
+    {
+        return cudaMemcpyAsync(w->sc, hsc.data(), hsc.size() * 8, cudaMemcpyHostToDevice, st);
+    }
+    double &S(int n, int k) { return hsc[(size_t)n * NSC + k]; }
+};
+
+LinArgs lin_args(Vec out, int gate = -1)
+{
+    LinArgs a;
+    memset(&a, 0, sizeof(a));
+    a.out = out;
+    a.gate = gate;
+    return a;
+}
+
+void add_term(LinArgs &a, Vec v, double mult, int s1 = -1, int s2 = -1, int cidx = -1)
+{
+    a.in[a.nt] = v;
+    a.t[a.nt] = Term{a.nt, s1, s2, cidx, mult};
+    ++a.nt;
+}
+
+#define RK(call)                                                                                    \
+    do {                                                                                            \
+        cudaError_t e_ = (call);                                                                    \
+        if (e_ != cudaSuccess)                                                                      \
+            return ctx_fail(R.c, MEPGL_ERR_CUDA, std::string("refine: ") + #call + ": " + cudaGetErrorString(e_)); \
+    } while (0)
+
+// y = (H + mu) u by central differences (u's step from S_DELTA / |u|); images gated by S_ACTIVE.
+mepgl_status hess_vec(Ctx &R, const Vec &u, const Vec &y, bool with_mu)
+{
+    RefineWork *w = R.w;
+    const int xb = R.c->xi ^ 1;
+    RK(R.dots({{u, u}}, OP_FDSTEP));
+    LinArgs a = lin_args(R.xt());
+    add_term(a, R.x(), 1.0);
+    add_term(a, u, 1.0, S_H);
+    RK(R.lin(a));
+    RK(R.grad(xb, w->gp));
+    a = lin_args(R.xt());
+    add_term(a, R.x(), 1.0);
+    add_term(a, u, -1.0, S_H);
+    RK(R.lin(a));
+    RK(R.grad(xb, w->gm));
+    a = lin_args(y);
+    add_term(a, w->gp, 1.0, S_INV2H);
+    add_term(a, w->gm, -1.0, S_INV2H);
+    if (with_mu) add_term(a, u, 1.0, S_MU);
+    RK(R.lin(a));
+    return MEPGL_OK;
+}
+
+// Gauge-subspace Newton step on every image with S_ACTIVE != 0.
+mepgl_status gauge_step(Ctx &R, const GaugeBasis &B, double h)
+{
+    RefineWork *w = R.w;
+    const StringHost &s = R.c->strings[0];
+    const int m = B.m, gstride = (2 * m + 1) * m;
+    const double q1 = s.q[0], q2 = s.q[1], idx = 1.0 / s.dx;
+    const int nc = R.c->ncomp, xb = R.c->xi ^ 1;
+    const dim3 gg((unsigned)std::min<long>((s.M() + NT - 1) / NT, 1024), R.F);
+    const dim3 gdg(w->nb, R.F, (m + RF_GB_CHUNK - 1) / RF_GB_CHUNK);
+    auto gdots = [&](Vec xx, Vec gv, int slot) -> mepgl_status {
+        k_gauge_dots<<<gdg, NT, 0, R.st>>>(xx, gv, B, s.nx, s.ny, nc, q1, q2, idx, w->part, w->nb);
+        k_gauge_sums<<<R.F, NT, 0, R.st>>>(w->part, m, w->nb, w->gd, gstride, slot);
+        R.c->launches += 2;
+        RK(cudaGetLastError());
+        return MEPGL_OK;
+    };
+    RK(R.grad(R.c->xi, w->g));
+    mepgl_status st = gdots(R.x(), w->g, 0);
+    if (st != MEPGL_OK) return st;
+    for (int k = 0; k < m; ++k)
+        for (int sg = 0; sg < 2; ++sg) {
+            k_gauge_apply<<<gg, NT, 0, R.st>>>(R.x(), R.xt(), B, w->gcoef, RF_MAX_GB, k, sg ? -h : h, s.nx, s.ny, nc,
+                                              q1, q2, idx, w->sc, -1);
+            R.c->launches += 1;
+            RK(cudaGetLastError());
+            RK(R.grad(xb, w->gp));
+            st = gdots(R.xt(), w->gp, 1 + 2 * k + sg);
+            if (st != MEPGL_OK) return st;
+        }
+    std::vector<double> gd((size_t)R.F * gstride);
+    RK(cudaMemcpyAsync(gd.data(), w->gd, gd.size() * 8, cudaMemcpyDeviceToHost, R.st));
+    RK(R.read_scalars());
+    std::vector<double> coef((size_t)R.F * RF_MAX_GB, 0.0);
+    for (int n = 0; n < R.F; ++n) {
+        if (R.S(n, S_ACTIVE) == 0.0) continue;
+        const double *G = gd.data() + (size_t)n * gstride;
+        std::vector<double> H(m * m);
+        for (int i = 0; i < m; ++i)
+            for (int k = 0; k < m; ++k) H[k * m + i] = (G[(1 + 2 * i) * m + k] - G[(2 + 2 * i) * m + k]) / (2 * h);
+        for (int i = 0; i < m; ++i)
+            for (int k = 0; k < i; ++k) H[i * m + k] = H[k * m + i] = 0.5 * (H[i * m + k] + H[k * m + i]);
+        double *c = coef.data() + (size_t)n * RF_MAX_GB;
+        if (!cholesky_solve(m, H, G, c)) {
+            // not positive definite: c = -H^+ g over the positive part of the spectrum
+            std::vector<double> ev, V;
+            jacobi_eig(m, H, ev, V);
+            std::fill(c, c + m, 0.0);
+            for (int e = 0; e < m; ++e) {
+                if (!(ev[e] > 1e-12 * std::fabs(ev[m - 1]))) continue;
+                double proj = 0.0;
+                for (int i = 0; i < m; ++i) proj += V[i * m + e] * G[i];
+                for (int i = 0; i < m; ++i) c[i] -= V[i * m + e] * proj / ev[e];
+            }
+        }
+    }
+    RK(cudaMemcpyAsync(w->gcoef, coef.data(), coef.size() * 8, cudaMemcpyHostToDevice, R.st));
+    k_gauge_apply<<<gg, NT, 0, R.st>>>(R.x(), R.x(), B, w->gcoef, RF_MAX_GB, -1, 1.0, s.nx, s.ny, nc, q1, q2, idx,
+                                      w->sc, S_ACTIVE);
+    R.c->launches += 1;
+    RK(cudaGetLastError());
+    return MEPGL_OK;
+}
+
+// Lanczos on the saddle images (S_ACTIVE gates them): `steps` steps from
+// w->v1 with full reorthogonalisation (twice); v1 <- the lowest Ritz vector,
+// normalised; lam <- its Ritz value.
+mepgl_status lanczos(Ctx &R, int steps, std::vector<double> &lam)
+{
+    RefineWork *w = R.w;
+    const long FM2 = (long)R.F * R.M2;
+    const int F = R.F;
+    RK(R.dots({{w->v1, w->v1}}, OP_UNIT));
+    LinArgs a = lin_args(w->lz[0], S_ACTIVE);
+    add_term(a, w->v1, 1.0, S_INVB);
+    RK(R.lin(a));
+    std::vector<double> alpha((size_t)F * steps, 0.0), beta((size_t)F * steps, 0.0);
+    std::vector<double> hd((size_t)F * RF_DOTS);
+    int done = 0;
+    for (int j = 0; j < steps; ++j) {
+        mepgl_status st = hess_vec(R, w->lz[j], w->lz[j + 1], false);
+        if (st != MEPGL_OK) return st;
+        for (int pass = 0; pass < 2; ++pass) {
+            k_dots_lz<<<R.vgrid(), NT, 0, R.st>>>(w->lz[j + 1], w->lz[0].p[0], w->vs, j + 1, R.M2, w->nf, FM2,
+                                                 w->part, w->nb);
+            RK(cudaGetLastError());
+            RK(R.sums(j + 1, OP_NONE));
+            if (pass == 0) {
+                RK(cudaMemcpyAsync(hd.data(), w->dots, hd.size() * 8, cudaMemcpyDeviceToHost, R.st));
+                RK(cudaStreamSynchronize(R.st));
+                for (int n = 0; n < F; ++n) alpha[(size_t)n * steps + j] = hd[(size_t)n * RF_DOTS + j];
+            }
+            k_sub_lz<<<R.vgrid(), NT, 0, R.st>>>(w->lz[j + 1], 1.0, w->lz[0].p[0], w->vs, j + 1, R.M2, w->nf, FM2,
+                                                w->dots, RF_DOTS, w->sc, S_ACTIVE, w->nb);
+            R.c->launches += 2;
+            RK(cudaGetLastError());
+        }
+        RK(R.dots({{w->lz[j + 1], w->lz[j + 1]}}, OP_UNIT));
+        RK(R.read_scalars());
+        for (int n = 0; n < F; ++n) {
+            const double ib = R.S(n, S_INVB);
+            beta[(size_t)n * steps + j] = ib > 0 ? 1.0 / ib : 0.0;
+        }
+        LinArgs b = lin_args(w->lz[j + 1], S_ACTIVE);
+        add_term(b, w->lz[j + 1], 1.0, S_INVB);
+        RK(R.lin(b));
+        done = j + 1;
+    }
+    // Ritz pair of the lowest eigenvalue of T per image
+    std::vector<double> coef((size_t)F * (RF_MAX_LZ + 1), 0.0);
+    RK(R.read_scalars());
+    lam.assign(F, 0.0);
+    for (int n = 0; n < F; ++n) {
+        if (R.S(n, S_ACTIVE) == 0.0) continue;
+        std::vector<double> T(done * done, 0.0), ev, V;
+        for (int j = 0; j < done; ++j) {
+            T[j * done + j] = alpha[(size_t)n * steps + j];
+            if (j + 1 < done) T[j * done + j + 1] = T[(j + 1) * done + j] = beta[(size_t)n * steps + j];
+        }
+        jacobi_eig(done, T, ev, V);
+        lam[n] = ev[0];
+        for (int j = 0; j < done; ++j) coef[(size_t)n * (RF_MAX_LZ + 1) + j] = -V[j * done + 0];
+    }
+    RK(cudaMemcpyAsync(w->coef, coef.data(), coef.size() * 8, cudaMemcpyHostToDevice, R.st));
+    // v1 = 0 * v1 - sum_j (-y_j) lz_j
+    k_sub_lz<<<R.vgrid(), NT, 0, R.st>>>(w->v1, 0.0, w->lz[0].p[0], w->vs, done, R.M2, w->nf, FM2, w->coef,
+                                        RF_MAX_LZ + 1, w->sc, S_ACTIVE, w->nb);
+    R.c->launches += 1;
+    RK(cudaGetLastError());
+    RK(R.dots({{w->v1, w->v1}}, OP_UNIT));
+    LinArgs b = lin_args(w->v1, S_ACTIVE);
+    add_term(b, w->v1, 1.0, S_INVB);
+    RK(R.lin(b));
+    return MEPGL_OK;
+}
+
+// One CG iteration on the images with S_ACTIVE != 0 (device scalars only,
+// so that a run of iterations can be captured as one CUDA graph).
+mepgl_status cg_iteration(Ctx &R)
+{
+    RefineWork *w = R.w;
+    mepgl_status st = hess_vec(R, w->p, w->y, true);
+    if (st != MEPGL_OK) return st;
+    // y -= (v1 . y) v1, then p . y
+    RK(R.dots({{w->v1, w->y}}, OP_STORE_V1Y));
+    LinArgs a = lin_args(w->y, S_ACTIVE);
+    add_term(a, w->y, 1.0);
+    add_term(a, w->v1, -1.0, S_V1Y);
+    a.dw = w->p;
+    a.dot_k = 1;
+    a.dot_slot = 0;
+    RK(R.lin(a));
+    RK(R.sums(1, OP_ALPHA));
+    a = lin_args(w->s, S_ACTIVE);
+    add_term(a, w->s, 1.0);
+    add_term(a, w->p, 1.0, S_ALPHA);
+    RK(R.lin(a));
+    a = lin_args(w->r, S_ACTIVE);
+    add_term(a, w->r, 1.0);
+    add_term(a, w->y, -1.0, S_ALPHA);
+    a.dw = w->r;
+    a.dot_k = 1;
+    a.dot_slot = 0;
+    RK(R.lin(a));
+    RK(R.sums(1, OP_BETA));
+    a = lin_args(w->p, S_ACTIVE);
+    add_term(a, w->r, 1.0);
+    add_term(a, w->p, 1.0, S_BETA);
+    RK(R.lin(a));
+    return MEPGL_OK;
+}
+
+constexpr int CG_GRAPH_ITERS = 8;     // CG iterations per graph replay
+
+// Projected shifted CG for the images with S_ACTIVE != 0 at entry:
+// (H + mu) s = -(g - g1 v1), s orthogonal to v1 (v1 = 0 for minima).
+// The iterations run as replays of a captured graph of CG_GRAPH_ITERS
+// iterations (images that converge inside a replay stop updating).
+mepgl_status cg_solve(Ctx &R, int max_it)
+{
+    RefineWork *w = R.w;
+    LinArgs a = lin_args(w->r, S_ACTIVE);
+    add_term(a, w->g, -1.0);
+    add_term(a, w->v1, 1.0, S_G1);
+    a.dw = w->r;   // |r|^2
+    a.dot_k = 1;
+    a.dot_slot = 0;
+    RK(R.lin(a));
+    RK(R.sums(1, OP_CGINIT));
+    a = lin_args(w->p, S_ACTIVE);
+    add_term(a, w->r, 1.0);
+    RK(R.lin(a));
+    a = lin_args(w->s, S_ACTIVE);
+    add_term(a, w->s, 0.0);
+    RK(R.lin(a));
+    cudaGraphExec_t &ex = w->cg_graph[R.c->xi & 1];
+    const int64_t l0 = R.c->launches, g0 = R.grads;
+    if (!ex) {
+        RK(cudaStreamBeginCapture(R.st, cudaStreamCaptureModeThreadLocal));
+        mepgl_status st = MEPGL_OK;
+        for (int k = 0; k < CG_GRAPH_ITERS && st == MEPGL_OK; ++k) st = cg_iteration(R);
+        cudaGraph_t g = nullptr;
+        const cudaError_t e = cudaStreamEndCapture(R.st, &g);
+        if (st != MEPGL_OK) return st;
+        RK(e);
+        RK(cudaGraphInstantiate(&ex, g, 0));
+        cudaGraphDestroy(g);
+        w->graph_launches = R.c->launches - l0;
+        w->graph_grads = R.grads - g0;
+        R.c->launches = l0;
+        R.grads = g0;
+    }
+    for (int it = 0; it < max_it; it += CG_GRAPH_ITERS) {
+        RK(cudaGraphLaunch(ex, R.st));
+        R.c->launches += w->graph_launches;
+        R.grads += w->graph_grads;
+        if ((it / CG_GRAPH_ITERS) % 2 == 1 || it + CG_GRAPH_ITERS >= max_it) {
+            RK(R.read_scalars());
+            bool any = false;
+            for (int n = 0; n < R.F; ++n) any |= R.S(n, S_ACTIVE) != 0.0;
+            if (!any) break;
+        }
+    }
+    return MEPGL_OK;
+}
+
+mepgl_status alloc_work(mepgl_ctx *c)
+{
+    const StringHost &s = c->strings[0];
+    RefineWork *w = c->refine;
+    if (w && w->F == s.F && w->M == s.M() && w->nf == 1 + c->ncomp) return MEPGL_OK;
+    refine_free(w);
+    w = c->refine = new RefineWork();
+    w->F = s.F;
+    w->M = s.M();
+    w->nx = s.nx;
+    w->ny = s.ny;
+    w->nf = 1 + c->ncomp;
+    const long len = (long)w->nf * 2 * w->M;
+    w->nb = (int)std::max<long>(1, std::min<long>(RF_NB, (len + 4L * NT - 1) / (4L * NT)));
+    w->vs = (size_t)w->nf * w->F * 2 * w->M;
+    const int nvec = 8 + RF_MAX_LZ + 1;
+    cudaError_t e = cudaMalloc(&w->block, nvec * w->vs * sizeof(double));
+    if (e == cudaSuccess) e = cudaMemsetAsync(w->block, 0, nvec * w->vs * sizeof(double), c->stream);
+    if (e != cudaSuccess) return ctx_fail(c, MEPGL_ERR_CUDA, std::string("refine workspace: ") + cudaGetErrorString(e));
+    auto vec = [&](int k) {
+        Vec v;
+        for (int f = 0; f < 3; ++f)
+            v.p[f] = f < w->nf ? w->block + k * w->vs + (size_t)f * w->F * 2 * w->M : nullptr;
+        return v;
+    };
+    // lz vectors first and contiguous (the multi-dot kernels index them by stride)
+    for (int k = 0; k <= RF_MAX_LZ; ++k) w->lz[k] = vec(k);
+    int k = RF_MAX_LZ + 1;
+    for (Vec *v : {&w->g, &w->v1, &w->p, &w->r, &w->y, &w->s, &w->gp, &w->gm}) *v = vec(k++);
+    const size_t parts = (size_t)w->F * std::max(RF_DOTS, RF_MAX_GB) * w->nb;
+    e = cudaMalloc(&w->part, parts * sizeof(double));
+    if (e == cudaSuccess) e = cudaMalloc(&w->dots, (size_t)w->F * RF_DOTS * sizeof(double));
+    if (e == cudaSuccess) e = cudaMalloc(&w->sc, (size_t)w->F * NSC * sizeof(double));
+    if (e == cudaSuccess) e = cudaMalloc(&w->coef, (size_t)w->F * (RF_MAX_LZ + 1) * sizeof(double));
+    if (e == cudaSuccess) e = cudaMalloc(&w->gcoef, (size_t)w->F * RF_MAX_GB * sizeof(double));
+    if (e == cudaSuccess)
+        e = cudaMalloc(&w->gd, (size_t)w->F * (2 * RF_MAX_GB + 1) * RF_MAX_GB * sizeof(double));
+    if (e == cudaSuccess) e = cudaMemsetAsync(w->sc, 0, (size_t)w->F * NSC * sizeof(double), c->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(w->coef, 0, (size_t)w->F * (RF_MAX_LZ + 1) * sizeof(double), c->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(w->gcoef, 0, (size_t)w->F * RF_MAX_GB * sizeof(double), c->stream);
+    if (e != cudaSuccess) return ctx_fail(c, MEPGL_ERR_CUDA, std::string("refine workspace: ") + cudaGetErrorString(e));
+    w->lam1.assign(w->F, 0.0);
+    w->mu.assign(w->F, 0.0);
+    w->has_mode.assign(w->F, 0);
+    w->fresh.assign(w->F, 0);
+    return MEPGL_OK;
+}
+
+}  // namespace
+}  // namespace mepgl
+
+using namespace mepgl;
+
+extern "C" {
+
+void mepgl_default_refine_options(mepgl_refine_options *o)
+{
+    if (!o) return;
+    memset(o, 0, sizeof(*o));
+    o->g_tol = 1e-8;
+    o->max_newton = 40;
+    o->max_cg = 3000;
+    o->lanczos_steps = 12;
+    o->gauge_degree = -1;
+    o->mu0 = 1e-3;
+    o->cg_eta = 0.1;
+    o->max_retries = 8;
+}
+
+mepgl_status mepgl_refine_stationary(mepgl_ctx *c, const int32_t *kind, const void *mode_a, const void *mode_psi_1,
+                                     const void *mode_psi_2, int memory, const mepgl_refine_options *opt_in,
+                                     mepgl_refine_report *report)
+{
+    if (!c || !kind) return MEPGL_ERR_INVALID_ARG;
+    if (c->strings.size() != 1)
+        return ctx_fail(c, MEPGL_ERR_UNSUPPORTED, "mepgl_refine_stationary: single-string contexts only");
+    if (c->precision != MEPGL_FP64)
+        return ctx_fail(c, MEPGL_ERR_UNSUPPORTED, "mepgl_refine_stationary: the refinement runs on FP64 contexts");
+    if (c->opt.discretization != MEPGL_DISC_REFERENCE)
+        return ctx_fail(c, MEPGL_ERR_UNSUPPORTED, "mepgl_refine_stationary: reference discretisation only");
+    mepgl_refine_options opt;
+    mepgl_default_refine_options(&opt);
+    if (opt_in) opt = *opt_in;
+    if (opt.lanczos_steps < 2 || opt.lanczos_steps > RF_MAX_LZ || opt.gauge_degree < -1 ||
+        opt.gauge_degree > RF_MAX_DEG || opt.max_newton < 0 || opt.max_cg < 1 || !(opt.g_tol >= 0) ||
+        !(opt.mu0 > 0) || !(opt.cg_eta > 0 && opt.cg_eta < 1) || opt.max_retries < 0)
+        return ctx_fail(c, MEPGL_ERR_INVALID_ARG, "mepgl_refine_stationary: option out of range");
+    const int F = c->strings[0].F;
+    for (int n = 0; n < F; ++n)
+        if (kind[n] != MEPGL_STATIONARY_MINIMUM && kind[n] != MEPGL_STATIONARY_SADDLE && kind[n] != MEPGL_STATIONARY_SKIP)
+            return ctx_fail(c, MEPGL_ERR_INVALID_ARG, "mepgl_refine_stationary: bad image kind");
+    mepgl_status st = ctx_flush(c);
+    if (st != MEPGL_OK) return st;
+    st = alloc_work(c);
+    if (st != MEPGL_OK) return st;
+    RefineWork *w = c->refine;
+    const bool new_modes = mode_a || mode_psi_1 || mode_psi_2;
+    for (int n = 0; n < F; ++n)
+        if (kind[n] == MEPGL_STATIONARY_SADDLE && !new_modes && !w->has_mode[n])
+            return ctx_fail(c, MEPGL_ERR_INVALID_ARG,
+                            "mepgl_refine_stationary: a saddle image needs an initial direction on its first call");
+    Ctx R{c, w, ctx_string_launch(c, 0), F, 2 * w->M, c->stream};
+    R.L.paired = 0;     // IEEE double gradients
+    const StringHost &s = c->strings[0];
+    // initial min modes: the caller's directions (then the history restarts)
+    if (new_modes) {
+        const void *src[3] = {mode_a, mode_psi_1, mode_psi_2};
+        const size_t bytes = (size_t)F * s.M() * 2 * sizeof(double);
+        for (int f = 0; f < w->nf; ++f) {
+            if (src[f])
+                RK(cudaMemcpyAsync(w->v1.p[f], src[f], bytes,
+                                   memory == MEPGL_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, R.st));
+            else
+                RK(cudaMemsetAsync(w->v1.p[f], 0, bytes, R.st));
+        }
+        for (int n = 0; n < F; ++n) {
+            w->has_mode[n] = kind[n] == MEPGL_STATIONARY_SADDLE;
+            w->fresh[n] = 1;
+            w->mu[n] = opt.mu0;
+        }
+    }
+    for (int n = 0; n < F; ++n)
+        if (w->mu[n] <= 0) w->mu[n] = opt.mu0;
+    // minima and skipped images carry a zero mode (the projections vanish)
+    {
+        RK(R.read_scalars());
+        for (int n = 0; n < F; ++n) R.S(n, S_ACTIVE) = kind[n] == MEPGL_STATIONARY_SADDLE ? 0.0 : 1.0;
+        RK(R.write_scalars());
+        LinArgs a = lin_args(w->v1, S_ACTIVE);
+        add_term(a, w->v1, 0.0);
+        RK(R.lin(a));
+    }
+    GaugeBasis B;
+    memset(&B, 0, sizeof(B));
+    // auto: one degree per 8 lattice sites of the longer side, 4 to 16
+    const int nmax = std::max(s.nx, s.ny);
+    B.deg = opt.gauge_degree >= 0 ? opt.gauge_degree : std::min(RF_MAX_DEG, std::max(4, nmax / 8));
+    if (c->thin_film) B.deg = 0;
+    for (int d = 1; d <= B.deg; ++d)
+        for (int k = 0; k <= d; ++k) {
+            B.a[B.m] = (unsigned char)(d - k);
+            B.b[B.m] = (unsigned char)k;
+            ++B.m;
+        }
+    const double dof = (double)w->nf * 2 * s.M();
+    std::vector<int> done(F, 0), newton_it(F, 0), cg_it(F, 0);
+    std::vector<double> gnorm(F, 0.0), energy(F, 0.0);
+    for (int n = 0; n < F; ++n) done[n] = kind[n] == MEPGL_STATIONARY_SKIP;
+    auto set_active = [&](const std::vector<int> &on) -> mepgl_status {
+        RK(R.read_scalars());
+        for (int n = 0; n < F; ++n) {
+            R.S(n, S_ACTIVE) = on[n] ? 1.0 : 0.0;
+            R.S(n, S_DELTA) = 1e-6 * std::sqrt(dof);
+            R.S(n, S_MU) = w->mu[n];
+            R.S(n, S_ONE) = 1.0;
+        }
+        RK(R.write_scalars());
+        return MEPGL_OK;
+    };
+    auto measure = [&]() -> mepgl_status {    // energies and |g| of x
+        RK(R.grad(c->xi, w->g));
+        RK(R.dots({{w->g, w->g}}, OP_NONE));
+        std::vector<double> hd((size_t)F * RF_DOTS);
+        RK(cudaMemcpyAsync(hd.data(), w->dots, hd.size() * 8, cudaMemcpyDeviceToHost, R.st));
+        RK(launch_energy(R.L, c->sc, c->xi, c->dscratch));
+        c->launches += 1;
+        RK(cudaMemcpyAsync(energy.data(), c->dscratch, F * 8, cudaMemcpyDeviceToHost, R.st));
+        RK(cudaStreamSynchronize(R.st));
+        for (int n = 0; n < F; ++n) gnorm[n] = std::sqrt(hd[(size_t)n * RF_DOTS]);
+        return MEPGL_OK;
+    };
+    st = measure();
+    if (st != MEPGL_OK) return st;
+    // MEPGL_REFINE_LOG=1: one line per image and Newton iteration on stderr
+    const char *env = std::getenv("MEPGL_REFINE_LOG");
+    const bool log = env && env[0] == '1';
+    for (int it = 0; it < opt.max_newton; ++it) {
+        std::vector<int> act(F);
+        bool any = false;
+        for (int n = 0; n < F; ++n) {
+            if (!done[n] && gnorm[n] <= opt.g_tol) done[n] = 1;
+            act[n] = !done[n];
+            any |= act[n] != 0;
+        }
+        if (!any) break;
+        // 1. gauge-subspace step
+        if (B.m > 0) {
+            st = set_active(act);
+            if (st == MEPGL_OK) st = gauge_step(R, B, 1e-4);
+            if (st != MEPGL_OK) return st;
+        }
+        // 2. min modes of the saddle images
+        std::vector<int> sad(F);
+        bool any_sad = false;
+        for (int n = 0; n < F; ++n) {
+            sad[n] = act[n] && kind[n] == MEPGL_STATIONARY_SADDLE;
+            any_sad |= sad[n] != 0;
+        }
+        if (any_sad) {
+            st = set_active(sad);
+            if (st != MEPGL_OK) return st;
+            std::vector<double> lam;
+            int steps = opt.lanczos_steps;
+            for (int n = 0; n < F; ++n)
+                if (sad[n] && w->fresh[n]) steps = std::max(steps, std::min(RF_MAX_LZ, 30));
+            st = lanczos(R, steps, lam);
+            if (st != MEPGL_OK) return st;
+            for (int n = 0; n < F; ++n)
+                if (sad[n]) {
+                    w->lam1[n] = lam[n];
+                    w->fresh[n] = 0;
+                }
+        }
+        // 3. gradient, g1 = v1 . g, uphill step along v1, shifted CG in the complement
+        st = set_active(act);
+        if (st != MEPGL_OK) return st;
+        RK(R.grad(c->xi, w->g));
+        RK(R.dots({{w->v1, w->g}, {w->g, w->g}}, OP_STORE_G1));
+        std::vector<double> hd((size_t)F * RF_DOTS);
+        RK(cudaMemcpyAsync(hd.data(), w->dots, hd.size() * 8, cudaMemcpyDeviceToHost, R.st));
+        RK(R.read_scalars());
+        std::vector<double> g2(F);
+        for (int n = 0; n < F; ++n) {
+            g2[n] = hd[(size_t)n * RF_DOTS + 1];
+            const double g1 = R.S(n, S_G1);
+            double p1 = 0.0;
+            if (kind[n] == MEPGL_STATIONARY_SADDLE && act[n]) {
+                p1 = g1 / std::max(std::fabs(w->lam1[n]), 1e-8);
+                const double cap = 1.0;
+                if (std::fabs(p1) > cap) p1 = p1 > 0 ? cap : -cap;
+            }
+            R.S(n, S_P1) = p1;
+        }
+        RK(R.write_scalars());
+        std::vector<int> pending = act, cg_before = cg_it, tries_used(F, 0);
+        for (int tries = 0; tries <= opt.max_retries; ++tries) {
+            for (int n = 0; n < F; ++n) tries_used[n] += pending[n];
+            st = set_active(pending);
+            if (st != MEPGL_OK) return st;
+            RK(R.read_scalars());
+            // forcing term: sqrt|g| (superlinear), but no tighter than the target needs
+            for (int n = 0; n < F; ++n) {
+                const double gn = std::sqrt(g2[n]);
+                R.S(n, S_ETA) = std::min(opt.cg_eta, std::max(std::sqrt(gn), gn > 0 ? 0.5 * opt.g_tol / gn : 0.0));
+            }
+            RK(R.write_scalars());
+            st = cg_solve(R, opt.max_cg);
+            if (st != MEPGL_OK) return st;
+            RK(R.read_scalars());
+            for (int n = 0; n < F; ++n)
+                if (pending[n]) cg_it[n] += (int)R.S(n, S_IT);
+            // trial x + s + p1 v1 (pending images), merit |g(trial)|^2
+            for (int n = 0; n < F; ++n) R.S(n, S_ACTIVE) = pending[n] ? 1.0 : 0.0;
+            RK(R.write_scalars());
+            LinArgs a = lin_args(R.xt());
+            add_term(a, R.x(), 1.0);
+            add_term(a, w->s, 1.0, S_ACTIVE);
+            add_term(a, w->v1, 1.0, S_P1, S_ACTIVE);
+            RK(R.lin(a));
+            RK(R.grad(c->xi ^ 1, w->gp));
+            RK(R.dots({{w->gp, w->gp}}, OP_NONE));
+            RK(cudaMemcpyAsync(hd.data(), w->dots, hd.size() * 8, cudaMemcpyDeviceToHost, R.st));
+            RK(cudaStreamSynchronize(R.st));
+            bool again = false;
+            for (int n = 0; n < F; ++n) {
+                R.S(n, S_ACCEPT) = 0.0;
+                if (!pending[n]) continue;
+                const double gt2 = hd[(size_t)n * RF_DOTS];
+                if (std::isfinite(gt2) && gt2 < g2[n] * (1 - 1e-4)) {
+                    R.S(n, S_ACCEPT) = 1.0;
+                    w->mu[n] = std::max(w->mu[n] / 4, 1e-12);
+                    pending[n] = 0;
+                } else {
+                    w->mu[n] *= 4;
+                    again = true;
+                }
+            }
+            RK(R.write_scalars());
+            a = lin_args(R.x(), S_ACCEPT);
+            add_term(a, R.xt(), 1.0);
+            RK(R.lin(a));
+            if (!again) break;
+        }
+        for (int n = 0; n < F; ++n)
+            if (act[n]) ++newton_it[n];
+        st = measure();
+        if (st != MEPGL_OK) return st;
+        if (log)
+            for (int n = 0; n < F; ++n)
+                if (act[n])
+                    std::fprintf(stderr,
+                                 "refine image %d (%s): |g| %.3e -> %.3e  E %.13f  mu %.2e  tries %d  cg %d  "
+                                 "lambda1 %.5f  grads %lld\n",
+                                 n, kind[n] == MEPGL_STATIONARY_SADDLE ? "saddle" : "minimum", std::sqrt(g2[n]),
+                                 gnorm[n], energy[n], w->mu[n], tries_used[n], cg_it[n] - cg_before[n], w->lam1[n],
+                                 (long long)R.grads);
+    }
+    if (report)
+        for (int n = 0; n < F; ++n) {
+            mepgl_refine_report &r = report[n];
+            r.energy = energy[n];
+            r.g_norm = gnorm[n];
+            r.min_curvature = kind[n] == MEPGL_STATIONARY_SADDLE ? w->lam1[n] : 0.0;
+            r.mu = w->mu[n];
+            r.newton_iterations = newton_it[n];
+            r.cg_iterations = cg_it[n];
+            r.gradient_evaluations = (int32_t)std::min<int64_t>(R.grads, INT32_MAX);
+            r.converged = kind[n] == MEPGL_STATIONARY_SKIP || gnorm[n] <= opt.g_tol;
+        }
+    return ctx_check_device_status(c);
+}
+
+}  // extern "C"

@@ -61,6 +61,21 @@ class MepglVortex(C.Structure):
                 ("winding", C.c_void_p)]
 
 
+class MepglRefineOptions(C.Structure):
+    _fields_ = [("g_tol", C.c_double), ("max_newton", C.c_int32), ("max_cg", C.c_int32),
+                ("lanczos_steps", C.c_int32), ("gauge_degree", C.c_int32), ("mu0", C.c_double),
+                ("cg_eta", C.c_double), ("max_retries", C.c_int32), ("pad", C.c_int32)]
+
+
+class MepglRefineReport(C.Structure):
+    _fields_ = [("energy", C.c_double), ("g_norm", C.c_double), ("min_curvature", C.c_double), ("mu", C.c_double),
+                ("newton_iterations", C.c_int32), ("cg_iterations", C.c_int32),
+                ("gradient_evaluations", C.c_int32), ("converged", C.c_int32)]
+
+
+STATIONARY_MINIMUM, STATIONARY_SADDLE, STATIONARY_SKIP = 0, 1, 2
+
+
 class MepglGuess(C.Structure):
     _fields_ = [("x0", C.c_double), ("y0", C.c_double), ("psi_abs_1", C.c_double), ("psi_abs_2", C.c_double),
                 ("noise", C.c_double), ("b_z", C.c_double), ("gauge", C.c_int32), ("profile", C.c_int32),
@@ -114,6 +129,9 @@ _SIGS = {
     "mepgl_batch_generate_string": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p]),
     "mepgl_batch_observables": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]),
     "mepgl_batch_param_adjoint": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "mepgl_default_refine_options": (None, [C.c_void_p]),
+    "mepgl_refine_stationary": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int,
+                                          C.c_void_p, C.c_void_p]),
 }
 
 
@@ -385,6 +403,34 @@ class StringContext:
 
     def synchronize(self):
         self._check(self.L.mepgl_synchronize(self.h))
+
+    def refine_stationary(self, kinds, mode: StringState | None = None, **options):
+        """Refine the images in place to stationary points (mepgl_refine_stationary).
+
+        kinds: per image STATIONARY_MINIMUM / _SADDLE / _SKIP.  mode: initial
+        direction of each saddle image (fields' shape; None continues from the
+        previous call's modes).  options: fields of mepgl_refine_options.
+        Returns a list of per-image report dicts."""
+        k = np.ascontiguousarray(kinds, np.int32)
+        if k.shape != (self.F,):
+            raise ValueError(f"need {self.F} kinds")
+        o = MepglRefineOptions()
+        self.L.mepgl_default_refine_options(C.byref(o))
+        for key, v in options.items():
+            setattr(o, key, v)
+        rep = (MepglRefineReport * self.F)()
+        ptrs = [None, None, None]
+        keep = []
+        if mode is not None:
+            for f, arr in enumerate((mode.a, mode.psi_1, mode.psi_2 if self.ncomp == 2 else None)):
+                if arr is not None:
+                    a = np.ascontiguousarray(arr, np.float64)
+                    if a.shape != self._shape():
+                        raise ValueError(f"mode shape {a.shape} != {self._shape()}")
+                    keep.append(a)
+                    ptrs[f] = _ptr(a)
+        self._check(self.L.mepgl_refine_stationary(self.h, _ptr(k), *ptrs, HOST, C.byref(o), rep))
+        return [{f: getattr(r, f) for f, _ in MepglRefineReport._fields_} for r in rep]
 
 
 class StringBatch(StringContext):
