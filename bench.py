@@ -49,6 +49,13 @@ WORKLOAD = "two-component GL 256x256 dx=0.4, 64 images (mixed-precision config)"
 RELAX = 10
 
 
+def bench_config(world: int) -> dict:
+    """The `config` of both arms' JSON lines (the same dict, so that the lines compare)."""
+    return {"workload": WORKLOAD, "sites": 256 * 256, "images": 64, "components": 2,
+            "line_polynomial": "exact", "line_search": "compat scan",
+            "cache": "inputs larger than L2 (no flush)", "parallelism": f"replicas x{world}"}
+
+
 def peaks():
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
@@ -208,8 +215,7 @@ def run_reference(args):
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * dt / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "sites": prob.nx * prob.ny, "images": 64, "components": 2,
-                   "cache": "inputs larger than L2"},
+        "config": bench_config(args.gpus),
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": cref.threads(), "kind": "port", "sample": sample,
                          "host": host_cpu()},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -420,9 +426,7 @@ def run_ours(args):
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": WORKLOAD, "sites": sites, "images": F, "components": 2,
-                       "line_polynomial": "exact", "line_search": "compat scan",
-                       "cache": "inputs larger than L2 (no flush)", "parallelism": f"replicas x{world}"},
+            "config": bench_config(world),
             "e2e": e2e, "gpu_launches": launches, "roofline": roofline, "kernels": kern, "fp64": fp64,
             "cpu_baseline": cpu, "clocks": clk.summary(), "time_to_end_state": ttb,
         }

@@ -81,6 +81,56 @@ def run(cfg: int, relax: int, iterations: int, schedule: str = "fp64", fp32_iter
     return rec, sens
 
 
+def time_to_barrier(cfg: int, schedule: str = "fp64", relax: int = 10, max_string: int = 300, window: int = 5,
+                    plateau: float = 1e-3, g_tol: float = 1e-8, max_newton: int = 40, **refine_options):
+    """One timed run of the barrier protocol on a workload.
+
+    String phase: outer iterations of loop() in mode L (one linear
+    reparametrization + ``relax`` NLCG steps, exact line polynomial and
+    search) in the schedule's precision -- ``fp64`` IEEE double, ``fp64_paired``
+    float-float NLCG passes, ``mixed`` FP32 -- until the string's interior
+    energy maximum stays on the same image for ``window`` iterations and its
+    estimate max_n F_n - F_0 changes by at most ``plateau`` (relative) over
+    them.  Refinement: image 0 to its minimum and that image to an index-1
+    saddle in IEEE double (saddle.refine_barrier) to |g| <= g_tol.
+
+    Returns a dict with the trace [(seconds, barrier estimate, phase)] --
+    the string's estimate during the string phase, F(saddle) - F(minimum)
+    during the refinement -- and the final refined barrier."""
+    from . import saddle
+    prob, st = _workload(cfg)
+    prec = "fp32" if schedule == "mixed" else "fp64"
+    arith = native.FP64_PAIRED if schedule == "fp64_paired" else native.FP64_NATIVE
+    c = native.StringContext(prob, st.n_images, prec, line_polynomial=native.POLY_EXACT,
+                             line_search=native.LS_EXACT, spline=native.SPLINE_FMM, fp64_arith=arith)
+    c.set_state(st)
+    c.synchronize()
+    t0 = time.perf_counter()
+    trace, hist = [], []
+    for it in range(max_string):
+        c.loop_iteration("L", relax)
+        fe = c.compute_free_energy()
+        k = saddle.seed_image(fe)
+        est = float(fe.max() - fe[0])
+        trace.append((time.perf_counter() - t0, est, "string"))
+        hist.append((k, est))
+        if len(hist) > window:
+            ks = {h[0] for h in hist[-window - 1:]}
+            if len(ks) == 1 and abs(est - hist[-window - 1][1]) <= plateau * abs(est):
+                break
+    state = c.get_state()
+    fe = c.compute_free_energy()
+    c.close()
+    t_string = time.perf_counter() - t0
+    r = saddle.refine_barrier(prob, state, fe, g_tol=g_tol, max_newton=max_newton, t0=t0, adjoint=False,
+                              **refine_options)
+    trace += [(t, b, "refine") for t, b, _, _ in r.trace]
+    return dict(schedule=schedule, trace=trace, barrier=r.barrier, string_iterations=len(hist),
+                string_s=t_string, total_s=trace[-1][0], seed_image=r.seed_image, is_saddle=r.is_saddle,
+                converged=r.converged, newton=len(r.trace) - 1, min_curvature=r.reports[1]["min_curvature"],
+                g_norms=(r.reports[0]["g_norm"], r.reports[1]["g_norm"]), energies=r.energies)
+
+
 def summarise(rec, target_ends=None, rtol=1e-6):
     t = np.array([r[0] for r in rec])
     dF = np.array([r[1] for r in rec])

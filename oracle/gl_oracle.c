@@ -33,6 +33,28 @@
 MEPGL_DEFINE_GTTRF(glo_gttrf_d, double)
 MEPGL_DEFINE_GTTRS(glo_gttrs_d, double)
 
+/* A x = b for an n x n tridiagonal matrix (dl[k] = A[k][k-1], dl[0] unused;
+ * d diagonal; du[k] = A[k][k+1]) and nrhs right-hand sides stored one after
+ * another in b, overwritten by the solutions: the restated LAPACK gtsv
+ * algorithm of tridiag.h, exported so that tests can check it against a
+ * LAPACK build.  Returns 0, or k + 1 if the pivot U(k,k) is exactly zero. */
+int glo_gtsv_d(int n, const double *dl, const double *d, const double *du, double *b, int nrhs)
+{
+    double *w = (double *)malloc(sizeof(double) * 4 * (size_t)n);
+    int *ipiv = (int *)malloc(sizeof(int) * (size_t)n);
+    if (!w || !ipiv) { free(w); free(ipiv); return -1; }
+    double *l = w, *dd = w + n, *u = w + 2 * n, *u2 = w + 3 * n;
+    memcpy(l, dl, sizeof(double) * n);
+    memcpy(dd, d, sizeof(double) * n);
+    memcpy(u, du, sizeof(double) * n);
+    const int info = glo_gttrf_d(n, l, dd, u, u2, ipiv);
+    if (info == 0)
+        for (int r = 0; r < nrhs; ++r) glo_gttrs_d(n, l, dd, u, u2, ipiv, b + (size_t)r * n, 1);
+    free(w);
+    free(ipiv);
+    return info;
+}
+
 /* Images are independent in every per-image loop, so they run in parallel
  * when built with OpenMP; results do not depend on the thread count. */
 #ifdef _OPENMP
