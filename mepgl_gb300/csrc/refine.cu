@@ -37,6 +37,7 @@
 // scalars live on the device, so its iterations run as replays of a captured
 // CUDA graph with no host round trip inside.
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -52,7 +53,7 @@ constexpr int RF_MAX_DEG = 16;      // gauge polynomial degree
 constexpr int RF_MAX_GB = (RF_MAX_DEG + 1) * (RF_MAX_DEG + 2) / 2 - 1;   // 152 basis functions
 constexpr int RF_GB_CHUNK = 16;     // basis functions per block of the gauge-dot kernel
 constexpr int RF_DOTS = 40;         // per-image dot results kept per launch
-constexpr int RF_NB = 64;           // blocks per image of the vector kernels (upper bound)
+constexpr int RF_NB = 256;          // blocks per image of the vector kernels (upper bound)
 
 // per-image device scalars (sc[n * NSC + k])
 enum { S_ACTIVE, S_RR, S_R0, S_ETA, S_ALPHA, S_BETA, S_H, S_INV2H, S_MU, S_V1Y, S_G1, S_P1, S_DELTA, S_IT, S_NEG,
@@ -134,39 +135,61 @@ __device__ __forceinline__ double block_reduce(double v, double *sh)
     return t;   // valid in thread 0
 }
 
-// Element e of image n of vector v (e < nf * 2M): array e / 2M, offset e % 2M.
-__device__ __forceinline__ double *velem(const Vec &v, int n, long M2, long e)
+// The vector kernels run on a grid (nb, F): block b of image n covers the
+// range [b * per, (b + 1) * per) of each of the image's nf arrays of 2M
+// doubles (per even, so that 16-byte pairs stay aligned).
+__device__ __forceinline__ void vrange(long M2, int nb, long &r0, long &r1)
 {
-    const int f = (int)(e / M2);
-    return v.p[f] + ((long)n * M2 + (e - f * M2));
+    long per = (M2 + nb - 1) / nb;
+    per += per & 1;
+    r0 = blockIdx.x * per;
+    r1 = min(M2, r0 + per);
 }
 
 // out = sum_t c_t in_t, per image; optional partial dot of out with dw.
+template <int NTT>
 __global__ void __launch_bounds__(NT) k_lincomb(LinArgs a, long M2, int nf, const double *sc, const double *coef,
                                                 int ccols, double *part, int nb)
 {
     __shared__ double sh[NT / 32];
     const int n = blockIdx.y;
     const bool on = a.gate < 0 || sc[n * NSC + a.gate] != 0.0;
-    double c[4] = {0, 0, 0, 0};
-    for (int k = 0; k < a.nt; ++k) {
+    double c[NTT];
+#pragma unroll
+    for (int k = 0; k < NTT; ++k) {
         double v = a.t[k].mult;
         if (a.t[k].s1 >= 0) v *= sc[n * NSC + a.t[k].s1];
         if (a.t[k].s2 >= 0) v *= sc[n * NSC + a.t[k].s2];
         if (a.t[k].cidx >= 0) v *= coef[n * ccols + a.t[k].cidx];
         c[k] = v;
     }
-    const long len = nf * M2, per = (len + nb - 1) / nb;
-    const long e0 = blockIdx.x * per, e1 = min(len, e0 + per);
+    long r0, r1;
+    vrange(M2, nb, r0, r1);
+    const long off = (long)n * M2;
+    const bool dot = a.dw.p[0] != nullptr;
     double acc = 0.0;
     if (on)
-        for (long e = e0 + threadIdx.x; e < e1; e += NT) {
-            double v = 0.0;
-            for (int k = 0; k < a.nt; ++k) v += c[k] * *velem(a.in[a.t[k].in], n, M2, e);
-            *velem(a.out, n, M2, e) = v;
-            if (a.dw.p[0]) acc += v * *velem(a.dw, n, M2, e);
+#pragma unroll
+        for (int f = 0; f < 3; ++f) {
+            if (f >= nf) break;
+            double2 *o = reinterpret_cast<double2 *>(a.out.p[f] + off);
+            const double2 *dw = dot ? reinterpret_cast<const double2 *>(a.dw.p[f] + off) : nullptr;
+            for (long r = r0 / 2 + threadIdx.x; r < r1 / 2; r += NT) {
+                double2 v = make_double2(0.0, 0.0);
+#pragma unroll
+                for (int k = 0; k < NTT; ++k) {
+                    const double2 x = reinterpret_cast<const double2 *>(a.in[k].p[f] + off)[r];
+                    v.x += c[k] * x.x;
+                    v.y += c[k] * x.y;
+                }
+                o[r] = v;
+                if (dot) {
+                    const double2 d = dw[r];
+                    acc += v.x * d.x + v.y * d.y;
+                }
+            }
         }
-    if (a.dw.p[0]) {
+    if (dot) {
         const double t = block_reduce(acc, sh);
         if (threadIdx.x == 0) part[((long)n * a.dot_k + a.dot_slot) * nb + blockIdx.x] = t;
     }
@@ -178,35 +201,55 @@ struct DotArgs {
     int k;
 };
 
+template <int K>
 __global__ void __launch_bounds__(NT) k_dots(DotArgs a, long M2, int nf, double *part, int nb)
 {
     __shared__ double sh[NT / 32];
     const int n = blockIdx.y;
-    const long len = nf * M2, per = (len + nb - 1) / nb;
-    const long e0 = blockIdx.x * per, e1 = min(len, e0 + per);
-    double acc[4] = {0, 0, 0, 0};
-    for (long e = e0 + threadIdx.x; e < e1; e += NT)
-        for (int k = 0; k < a.k; ++k) acc[k] += *velem(a.u[k], n, M2, e) * *velem(a.w[k], n, M2, e);
-    for (int k = 0; k < a.k; ++k) {
+    long r0, r1;
+    vrange(M2, nb, r0, r1);
+    const long off = (long)n * M2;
+    double acc[K];
+#pragma unroll
+    for (int k = 0; k < K; ++k) acc[k] = 0.0;
+#pragma unroll
+    for (int f = 0; f < 3; ++f) {
+        if (f >= nf) break;
+        for (long r = r0 / 2 + threadIdx.x; r < r1 / 2; r += NT) {
+#pragma unroll
+            for (int k = 0; k < K; ++k) {
+                const double2 u = reinterpret_cast<const double2 *>(a.u[k].p[f] + off)[r];
+                const double2 w = reinterpret_cast<const double2 *>(a.w[k].p[f] + off)[r];
+                acc[k] += u.x * w.x + u.y * w.y;
+            }
+        }
+    }
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
         const double t = block_reduce(acc[k], sh);
-        if (threadIdx.x == 0) part[((long)n * a.k + k) * nb + blockIdx.x] = t;
+        if (threadIdx.x == 0) part[((long)n * K + k) * nb + blockIdx.x] = t;
     }
 }
 
-// Partial dots of w with Lanczos vectors lz_0 .. lz_{K-1} (contiguous, stride vs).
+// Partial dots of w with Lanczos vectors lz_0 .. lz_{K-1} (contiguous, stride vs;
+// array f of a vector at offset f * FM2).
 __global__ void __launch_bounds__(NT) k_dots_lz(Vec w, const double *lz0, size_t vs, int K, long M2, int nf,
                                                 long FM2, double *part, int nb)
 {
     __shared__ double sh[NT / 32];
     const int n = blockIdx.y;
-    const long len = nf * M2, per = (len + nb - 1) / nb;
-    const long e0 = blockIdx.x * per, e1 = min(len, e0 + per);
+    long r0, r1;
+    vrange(M2, nb, r0, r1);
+    const long off = (long)n * M2;
     for (int k = 0; k < K; ++k) {
         double acc = 0.0;
-        const double *base = lz0 + k * vs;
-        for (long e = e0 + threadIdx.x; e < e1; e += NT) {
-            const int f = (int)(e / M2);
-            acc += base[f * FM2 + (long)n * M2 + (e - f * M2)] * *velem(w, n, M2, e);
+        for (int f = 0; f < nf; ++f) {
+            const double2 *b = reinterpret_cast<const double2 *>(lz0 + k * vs + f * FM2 + off);
+            const double2 *x = reinterpret_cast<const double2 *>(w.p[f] + off);
+            for (long r = r0 / 2 + threadIdx.x; r < r1 / 2; r += NT) {
+                const double2 u = b[r], v = x[r];
+                acc += u.x * v.x + u.y * v.y;
+            }
         }
         const double t = block_reduce(acc, sh);
         if (threadIdx.x == 0) part[((long)n * K + k) * nb + blockIdx.x] = t;
@@ -222,14 +265,22 @@ __global__ void __launch_bounds__(NT) k_sub_lz(Vec w, double c0, const double *l
     if (gate >= 0 && sc[n * NSC + gate] == 0.0) return;
     double dk[RF_MAX_LZ + 1];
     for (int k = 0; k < K; ++k) dk[k] = d[n * dstride + k];
-    const long len = nf * M2, per = (len + nb - 1) / nb;
-    const long e0 = blockIdx.x * per, e1 = min(len, e0 + per);
-    for (long e = e0 + threadIdx.x; e < e1; e += NT) {
-        const int f = (int)(e / M2);
-        const long o = f * FM2 + (long)n * M2 + (e - f * M2);
-        double v = c0 * *velem(w, n, M2, e);
-        for (int k = 0; k < K; ++k) v -= dk[k] * lz0[k * vs + o];
-        *velem(w, n, M2, e) = v;
+    long r0, r1;
+    vrange(M2, nb, r0, r1);
+    const long off = (long)n * M2;
+    for (int f = 0; f < nf; ++f) {
+        double2 *x = reinterpret_cast<double2 *>(w.p[f] + off);
+        for (long r = r0 / 2 + threadIdx.x; r < r1 / 2; r += NT) {
+            double2 v = x[r];
+            v.x *= c0;
+            v.y *= c0;
+            for (int k = 0; k < K; ++k) {
+                const double2 b = reinterpret_cast<const double2 *>(lz0 + k * vs + f * FM2 + off)[r];
+                v.x -= dk[k] * b.x;
+                v.y -= dk[k] * b.y;
+            }
+            x[r] = v;
+        }
     }
 }
 
@@ -535,7 +586,14 @@ struct Ctx {
     }
     cudaError_t lin(const LinArgs &a)
     {
-        k_lincomb<<<vgrid(), NT, 0, st>>>(a, M2, w->nf, w->sc, w->coef, RF_MAX_LZ + 1, w->part, w->nb);
+        const double *cf = w->coef;
+        const int cc = RF_MAX_LZ + 1;
+        switch (a.nt) {
+        case 1: k_lincomb<1><<<vgrid(), NT, 0, st>>>(a, M2, w->nf, w->sc, cf, cc, w->part, w->nb); break;
+        case 2: k_lincomb<2><<<vgrid(), NT, 0, st>>>(a, M2, w->nf, w->sc, cf, cc, w->part, w->nb); break;
+        case 3: k_lincomb<3><<<vgrid(), NT, 0, st>>>(a, M2, w->nf, w->sc, cf, cc, w->part, w->nb); break;
+        default: k_lincomb<4><<<vgrid(), NT, 0, st>>>(a, M2, w->nf, w->sc, cf, cc, w->part, w->nb); break;
+        }
         c->launches += 1;
         return cudaGetLastError();
     }
@@ -554,7 +612,12 @@ struct Ctx {
             a.w[a.k] = pr.second;
             ++a.k;
         }
-        k_dots<<<vgrid(), NT, 0, st>>>(a, M2, w->nf, w->part, w->nb);
+        switch (a.k) {
+        case 1: k_dots<1><<<vgrid(), NT, 0, st>>>(a, M2, w->nf, w->part, w->nb); break;
+        case 2: k_dots<2><<<vgrid(), NT, 0, st>>>(a, M2, w->nf, w->part, w->nb); break;
+        case 3: k_dots<3><<<vgrid(), NT, 0, st>>>(a, M2, w->nf, w->part, w->nb); break;
+        default: k_dots<4><<<vgrid(), NT, 0, st>>>(a, M2, w->nf, w->part, w->nb); break;
+        }
         c->launches += 1;
         cudaError_t e = cudaGetLastError();
         if (e != cudaSuccess) return e;
@@ -859,8 +922,8 @@ mepgl_status alloc_work(mepgl_ctx *c)
     w->nx = s.nx;
     w->ny = s.ny;
     w->nf = 1 + c->ncomp;
-    const long len = (long)w->nf * 2 * w->M;
-    w->nb = (int)std::max<long>(1, std::min<long>(RF_NB, (len + 4L * NT - 1) / (4L * NT)));
+    // about four 16-byte pairs per thread and array
+    w->nb = (int)std::max<long>(1, std::min<long>(RF_NB, (2 * w->M + 8L * NT - 1) / (8L * NT)));
     w->vs = (size_t)w->nf * w->F * 2 * w->M;
     const int nvec = 8 + RF_MAX_LZ + 1;
     cudaError_t e = cudaMalloc(&w->block, nvec * w->vs * sizeof(double));
@@ -1082,6 +1145,8 @@ mepgl_status mepgl_refine_stationary(mepgl_ctx *c, const int32_t *kind, const vo
         }
         RK(R.write_scalars());
         std::vector<int> pending = act, cg_before = cg_it, tries_used(F, 0);
+        double cg_seconds = 0.0;
+        const auto tn0 = std::chrono::steady_clock::now();
         for (int tries = 0; tries <= opt.max_retries; ++tries) {
             for (int n = 0; n < F; ++n) tries_used[n] += pending[n];
             st = set_active(pending);
@@ -1093,9 +1158,11 @@ mepgl_status mepgl_refine_stationary(mepgl_ctx *c, const int32_t *kind, const vo
                 R.S(n, S_ETA) = std::min(opt.cg_eta, std::max(std::sqrt(gn), gn > 0 ? 0.5 * opt.g_tol / gn : 0.0));
             }
             RK(R.write_scalars());
+            const auto tc0 = std::chrono::steady_clock::now();
             st = cg_solve(R, opt.max_cg);
             if (st != MEPGL_OK) return st;
             RK(R.read_scalars());
+            cg_seconds += std::chrono::duration<double>(std::chrono::steady_clock::now() - tc0).count();
             for (int n = 0; n < F; ++n)
                 if (pending[n]) cg_it[n] += (int)R.S(n, S_IT);
             // trial x + s + p1 v1 (pending images), merit |g(trial)|^2
@@ -1139,10 +1206,12 @@ mepgl_status mepgl_refine_stationary(mepgl_ctx *c, const int32_t *kind, const vo
                 if (act[n])
                     std::fprintf(stderr,
                                  "refine image %d (%s): |g| %.3e -> %.3e  E %.13f  mu %.2e  tries %d  cg %d  "
-                                 "lambda1 %.5f  grads %lld\n",
+                                 "lambda1 %.5f  grads %lld  newton-step %.3f s of which CG %.3f s\n",
                                  n, kind[n] == MEPGL_STATIONARY_SADDLE ? "saddle" : "minimum", std::sqrt(g2[n]),
                                  gnorm[n], energy[n], w->mu[n], tries_used[n], cg_it[n] - cg_before[n], w->lam1[n],
-                                 (long long)R.grads);
+                                 (long long)R.grads,
+                                 std::chrono::duration<double>(std::chrono::steady_clock::now() - tn0).count(),
+                                 cg_seconds);
     }
     if (report)
         for (int n = 0; n < F; ++n) {
