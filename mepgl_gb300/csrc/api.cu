@@ -876,6 +876,7 @@ mepgl_status mepgl_destroy(mepgl_ctx *c)
 
 mepgl_status mepgl_set_state(mepgl_ctx *c, const void *a, const void *psi_1, const void *psi_2, int memory)
 {
+    if (c) ++c->state_version;
     if (!c) return MEPGL_ERR_INVALID_ARG;
     if (memory == MEPGL_STAGED) {
         // the staged copy: the context's stream waits for it, then takes it over
@@ -931,6 +932,7 @@ mepgl_status mepgl_stage_state(mepgl_ctx *c, const void *a, const void *psi_1, c
 mepgl_status mepgl_batch_set_state(mepgl_ctx *c, int string, const void *a, const void *psi_1, const void *psi_2,
                                    int memory)
 {
+    if (c) ++c->state_version;
     if (!c || string < 0 || string >= (int)c->strings.size() || !a || !psi_1 || (c->ncomp == 2 && !psi_2))
         return fail(c, MEPGL_ERR_INVALID_ARG, "mepgl_batch_set_state: bad string index or null field");
     mepgl_status st = flush(c);
@@ -945,11 +947,13 @@ mepgl_status mepgl_batch_set_state(mepgl_ctx *c, int string, const void *a, cons
 
 mepgl_status mepgl_generate_string(mepgl_ctx *c, const mepgl_guess *g)
 {
+    if (c) ++c->state_version;
     return mepgl_batch_generate_string(c, 0, g);
 }
 
 mepgl_status mepgl_batch_generate_string(mepgl_ctx *c, int string, const mepgl_guess *g)
 {
+    if (c) ++c->state_version;
     if (!c || !g || string < 0 || string >= (int)c->strings.size() || (g->n_vortices > 0 && !g->vortices) ||
         g->n_vortices < 0 || g->gauge < 0 || g->gauge > 3 || g->profile < 0 || g->profile > 1)
         return fail(c, MEPGL_ERR_INVALID_ARG, "mepgl_generate_string: bad string index or guess");
@@ -1111,6 +1115,7 @@ mepgl_status mepgl_energy_grad(mepgl_ctx *c, double *fenergy, void *g_a, void *g
 
 mepgl_status mepgl_nlcg_steps(mepgl_ctx *c, int iterations, int use_cg, int maxwell_only)
 {
+    if (c) ++c->state_version;
     if (!c || iterations < 0) return fail(c, MEPGL_ERR_INVALID_ARG, "mepgl_nlcg_steps: bad argument");
     if (c->opt.discretization == MEPGL_DISC_LINK)
         return fail(c, MEPGL_ERR_UNSUPPORTED,
@@ -1217,6 +1222,7 @@ mepgl_status mepgl_batch_arc_length(mepgl_ctx *c, int string, int metric, double
 
 mepgl_status mepgl_redistribute(mepgl_ctx *c, int kind, int F_new)
 {
+    if (c) ++c->state_version;
     if (!c) return MEPGL_ERR_INVALID_ARG;
     if (kind != MEPGL_REDIST_LINEAR && kind != MEPGL_REDIST_CUBIC)
         return fail(c, MEPGL_ERR_INVALID_ARG, "mepgl_redistribute: unknown kind");
@@ -1261,6 +1267,7 @@ mepgl_status mepgl_iteration(mepgl_ctx *c, char mode, int relaxation_steps, int 
 
 mepgl_status mepgl_set_precision(mepgl_ctx *c, int precision)
 {
+    if (c) ++c->state_version;
     if (!c || (precision != MEPGL_FP32 && precision != MEPGL_FP64))
         return fail(c, MEPGL_ERR_INVALID_ARG, "mepgl_set_precision: bad precision");
     if (precision == c->precision) return MEPGL_OK;

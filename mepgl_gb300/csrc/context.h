@@ -70,6 +70,9 @@ struct mepgl_ctx {
     bool staged = false;
     // workspace of mepgl_refine_stationary (refine.cu), allocated on first use
     mepgl::RefineWork *refine = nullptr;
+    // bumped by every call that changes the fields other than the refinement
+    // (which keeps per-state caches in its workspace)
+    uint64_t state_version = 0;
 };
 
 namespace mepgl {

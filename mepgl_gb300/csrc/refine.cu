@@ -102,6 +102,12 @@ struct RefineWork {
     std::vector<int> fresh;           // that direction is the caller's (longer first Lanczos)
     cudaGraphExec_t cg_graph[2] = {nullptr, nullptr};   // CG iterations, per current x buffer
     int64_t graph_launches = 0, graph_grads = 0;        // kernels and gradients per replay
+    // gauge-subspace Hessians kept between Newton iterations (and calls on
+    // the same state): per image m x m, its age in iterations
+    std::vector<std::vector<double>> gauge_h;
+    std::vector<int> gauge_age;
+    int gauge_m = -1;
+    uint64_t state_version = ~0ull;   // the context's state version after the last refinement call
 };
 
 void refine_free(RefineWork *w)
@@ -684,8 +690,10 @@ mepgl_status hess_vec(Ctx &R, const Vec &u, const Vec &y, bool with_mu)
     return MEPGL_OK;
 }
 
-// Gauge-subspace Newton step on every image with S_ACTIVE != 0.
-mepgl_status gauge_step(Ctx &R, const GaugeBasis &B, double h)
+// Gauge-subspace Newton step on every image with S_ACTIVE != 0.  The m x m
+// Hessian (2m gradient evaluations) is rebuilt when older than `refresh`
+// iterations; in between only the orbit gradient is evaluated.
+mepgl_status gauge_step(Ctx &R, const GaugeBasis &B, double h, int refresh)
 {
     RefineWork *w = R.w;
     const StringHost &s = R.c->strings[0];
@@ -704,7 +712,16 @@ mepgl_status gauge_step(Ctx &R, const GaugeBasis &B, double h)
     RK(R.grad(R.c->xi, w->g));
     mepgl_status st = gdots(R.x(), w->g, 0);
     if (st != MEPGL_OK) return st;
-    for (int k = 0; k < m; ++k)
+    RK(R.read_scalars());
+    if (w->gauge_m != m) {
+        w->gauge_h.assign(R.F, std::vector<double>());
+        w->gauge_age.assign(R.F, 1 << 30);
+        w->gauge_m = m;
+    }
+    bool rebuild = false;
+    for (int n = 0; n < R.F; ++n)
+        if (R.S(n, S_ACTIVE) != 0.0 && w->gauge_age[n] >= refresh) rebuild = true;
+    for (int k = 0; k < m && rebuild; ++k)
         for (int sg = 0; sg < 2; ++sg) {
             k_gauge_apply<<<gg, NT, 0, R.st>>>(R.x(), R.xt(), B, w->gcoef, RF_MAX_GB, k, sg ? -h : h, s.nx, s.ny, nc,
                                               q1, q2, idx, w->sc, -1);
@@ -716,16 +733,21 @@ mepgl_status gauge_step(Ctx &R, const GaugeBasis &B, double h)
         }
     std::vector<double> gd((size_t)R.F * gstride);
     RK(cudaMemcpyAsync(gd.data(), w->gd, gd.size() * 8, cudaMemcpyDeviceToHost, R.st));
-    RK(R.read_scalars());
+    RK(cudaStreamSynchronize(R.st));
     std::vector<double> coef((size_t)R.F * RF_MAX_GB, 0.0);
     for (int n = 0; n < R.F; ++n) {
         if (R.S(n, S_ACTIVE) == 0.0) continue;
         const double *G = gd.data() + (size_t)n * gstride;
-        std::vector<double> H(m * m);
-        for (int i = 0; i < m; ++i)
-            for (int k = 0; k < m; ++k) H[k * m + i] = (G[(1 + 2 * i) * m + k] - G[(2 + 2 * i) * m + k]) / (2 * h);
-        for (int i = 0; i < m; ++i)
-            for (int k = 0; k < i; ++k) H[i * m + k] = H[k * m + i] = 0.5 * (H[i * m + k] + H[k * m + i]);
+        std::vector<double> &H = w->gauge_h[n];
+        if (rebuild) {
+            H.assign(m * m, 0.0);
+            for (int i = 0; i < m; ++i)
+                for (int k = 0; k < m; ++k) H[k * m + i] = (G[(1 + 2 * i) * m + k] - G[(2 + 2 * i) * m + k]) / (2 * h);
+            for (int i = 0; i < m; ++i)
+                for (int k = 0; k < i; ++k) H[i * m + k] = H[k * m + i] = 0.5 * (H[i * m + k] + H[k * m + i]);
+            w->gauge_age[n] = 0;
+        }
+        ++w->gauge_age[n];
         double *c = coef.data() + (size_t)n * RF_MAX_GB;
         if (!cholesky_solve(m, H, G, c)) {
             // not positive definite: c = -H^+ g over the positive part of the spectrum
@@ -977,6 +999,7 @@ void mepgl_default_refine_options(mepgl_refine_options *o)
     o->mu0 = 1e-3;
     o->cg_eta = 0.1;
     o->max_retries = 8;
+    o->gauge_refresh = 4;
 }
 
 mepgl_status mepgl_refine_stationary(mepgl_ctx *c, const int32_t *kind, const void *mode_a, const void *mode_psi_1,
@@ -995,7 +1018,7 @@ mepgl_status mepgl_refine_stationary(mepgl_ctx *c, const int32_t *kind, const vo
     if (opt_in) opt = *opt_in;
     if (opt.lanczos_steps < 2 || opt.lanczos_steps > RF_MAX_LZ || opt.gauge_degree < -1 ||
         opt.gauge_degree > RF_MAX_DEG || opt.max_newton < 0 || opt.max_cg < 1 || !(opt.g_tol >= 0) ||
-        !(opt.mu0 > 0) || !(opt.cg_eta > 0 && opt.cg_eta < 1) || opt.max_retries < 0)
+        !(opt.mu0 > 0) || !(opt.cg_eta > 0 && opt.cg_eta < 1) || opt.max_retries < 0 || opt.gauge_refresh < 1)
         return ctx_fail(c, MEPGL_ERR_INVALID_ARG, "mepgl_refine_stationary: option out of range");
     const int F = c->strings[0].F;
     for (int n = 0; n < F; ++n)
@@ -1011,6 +1034,8 @@ mepgl_status mepgl_refine_stationary(mepgl_ctx *c, const int32_t *kind, const vo
         if (kind[n] == MEPGL_STATIONARY_SADDLE && !new_modes && !w->has_mode[n])
             return ctx_fail(c, MEPGL_ERR_INVALID_ARG,
                             "mepgl_refine_stationary: a saddle image needs an initial direction on its first call");
+    if (new_modes || w->state_version != c->state_version)
+        for (auto &a : w->gauge_age) a = 1 << 30;
     Ctx R{c, w, ctx_string_launch(c, 0), F, 2 * w->M, c->stream};
     R.L.paired = 0;     // IEEE double gradients
     const StringHost &s = c->strings[0];
@@ -1087,6 +1112,7 @@ mepgl_status mepgl_refine_stationary(mepgl_ctx *c, const int32_t *kind, const vo
     const char *env = std::getenv("MEPGL_REFINE_LOG");
     const bool log = env && env[0] == '1';
     for (int it = 0; it < opt.max_newton; ++it) {
+        double t_gauge = 0.0;
         std::vector<int> act(F);
         bool any = false;
         for (int n = 0; n < F; ++n) {
@@ -1098,10 +1124,13 @@ mepgl_status mepgl_refine_stationary(mepgl_ctx *c, const int32_t *kind, const vo
         // 1. gauge-subspace step
         if (B.m > 0) {
             st = set_active(act);
-            if (st == MEPGL_OK) st = gauge_step(R, B, 1e-4);
+            const auto tg0 = std::chrono::steady_clock::now();
+            if (st == MEPGL_OK) st = gauge_step(R, B, 1e-4, opt.gauge_refresh);
             if (st != MEPGL_OK) return st;
+            t_gauge = std::chrono::duration<double>(std::chrono::steady_clock::now() - tg0).count();
         }
         // 2. min modes of the saddle images
+        const auto tl0 = std::chrono::steady_clock::now();
         std::vector<int> sad(F);
         bool any_sad = false;
         for (int n = 0; n < F; ++n) {
@@ -1123,6 +1152,7 @@ mepgl_status mepgl_refine_stationary(mepgl_ctx *c, const int32_t *kind, const vo
                     w->fresh[n] = 0;
                 }
         }
+        const double t_lanczos = std::chrono::duration<double>(std::chrono::steady_clock::now() - tl0).count();
         // 3. gradient, g1 = v1 . g, uphill step along v1, shifted CG in the complement
         st = set_active(act);
         if (st != MEPGL_OK) return st;
@@ -1146,6 +1176,7 @@ mepgl_status mepgl_refine_stationary(mepgl_ctx *c, const int32_t *kind, const vo
         RK(R.write_scalars());
         std::vector<int> pending = act, cg_before = cg_it, tries_used(F, 0);
         double cg_seconds = 0.0;
+        std::vector<int> neg_hits(F, 0);
         const auto tn0 = std::chrono::steady_clock::now();
         for (int tries = 0; tries <= opt.max_retries; ++tries) {
             for (int n = 0; n < F; ++n) tries_used[n] += pending[n];
@@ -1164,7 +1195,10 @@ mepgl_status mepgl_refine_stationary(mepgl_ctx *c, const int32_t *kind, const vo
             RK(R.read_scalars());
             cg_seconds += std::chrono::duration<double>(std::chrono::steady_clock::now() - tc0).count();
             for (int n = 0; n < F; ++n)
-                if (pending[n]) cg_it[n] += (int)R.S(n, S_IT);
+                if (pending[n]) {
+                    cg_it[n] += (int)R.S(n, S_IT);
+                    neg_hits[n] += R.S(n, S_NEG) != 0.0;
+                }
             // trial x + s + p1 v1 (pending images), merit |g(trial)|^2
             for (int n = 0; n < F; ++n) R.S(n, S_ACTIVE) = pending[n] ? 1.0 : 0.0;
             RK(R.write_scalars());
@@ -1206,13 +1240,15 @@ mepgl_status mepgl_refine_stationary(mepgl_ctx *c, const int32_t *kind, const vo
                 if (act[n])
                     std::fprintf(stderr,
                                  "refine image %d (%s): |g| %.3e -> %.3e  E %.13f  mu %.2e  tries %d  cg %d  "
-                                 "lambda1 %.5f  grads %lld  newton-step %.3f s of which CG %.3f s\n",
+                                 "lambda1 %.5f  grads %lld  newton-step %.3f s of which CG %.3f s  gauge %.3f s  "
+                                 "lanczos %.3f s  cg-negative %d\n",
                                  n, kind[n] == MEPGL_STATIONARY_SADDLE ? "saddle" : "minimum", std::sqrt(g2[n]),
                                  gnorm[n], energy[n], w->mu[n], tries_used[n], cg_it[n] - cg_before[n], w->lam1[n],
                                  (long long)R.grads,
                                  std::chrono::duration<double>(std::chrono::steady_clock::now() - tn0).count(),
-                                 cg_seconds);
+                                 cg_seconds, t_gauge, t_lanczos, neg_hits[n]);
     }
+    w->state_version = c->state_version;
     if (report)
         for (int n = 0; n < F; ++n) {
             mepgl_refine_report &r = report[n];

@@ -64,7 +64,7 @@ class MepglVortex(C.Structure):
 class MepglRefineOptions(C.Structure):
     _fields_ = [("g_tol", C.c_double), ("max_newton", C.c_int32), ("max_cg", C.c_int32),
                 ("lanczos_steps", C.c_int32), ("gauge_degree", C.c_int32), ("mu0", C.c_double),
-                ("cg_eta", C.c_double), ("max_retries", C.c_int32), ("pad", C.c_int32)]
+                ("cg_eta", C.c_double), ("max_retries", C.c_int32), ("gauge_refresh", C.c_int32)]
 
 
 class MepglRefineReport(C.Structure):
