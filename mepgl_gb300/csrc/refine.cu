@@ -692,81 +692,119 @@ mepgl_status hess_vec(Ctx &R, const Vec &u, const Vec &y, bool with_mu)
 
 // Gauge-subspace Newton step on every image with S_ACTIVE != 0.  The m x m
 // Hessian (2m gradient evaluations) is rebuilt when older than `refresh`
-// iterations; in between only the orbit gradient is evaluated.
+// iterations; in between only the orbit gradient is evaluated.  The step is
+// a trial: it is kept only where the energy does not rise; where it does,
+// a reused Hessian is rebuilt and the step recomputed once, and a step from
+// a fresh Hessian that still raises the energy is dropped.
 mepgl_status gauge_step(Ctx &R, const GaugeBasis &B, double h, int refresh)
 {
     RefineWork *w = R.w;
     const StringHost &s = R.c->strings[0];
-    const int m = B.m, gstride = (2 * m + 1) * m;
+    const int m = B.m, gstride = (2 * m + 1) * m, F = R.F;
     const double q1 = s.q[0], q2 = s.q[1], idx = 1.0 / s.dx;
     const int nc = R.c->ncomp, xb = R.c->xi ^ 1;
-    const dim3 gg((unsigned)std::min<long>((s.M() + NT - 1) / NT, 1024), R.F);
-    const dim3 gdg(w->nb, R.F, (m + RF_GB_CHUNK - 1) / RF_GB_CHUNK);
+    const dim3 gg((unsigned)std::min<long>((s.M() + NT - 1) / NT, 1024), F);
+    const dim3 gdg(w->nb, F, (m + RF_GB_CHUNK - 1) / RF_GB_CHUNK);
     auto gdots = [&](Vec xx, Vec gv, int slot) -> mepgl_status {
         k_gauge_dots<<<gdg, NT, 0, R.st>>>(xx, gv, B, s.nx, s.ny, nc, q1, q2, idx, w->part, w->nb);
-        k_gauge_sums<<<R.F, NT, 0, R.st>>>(w->part, m, w->nb, w->gd, gstride, slot);
+        k_gauge_sums<<<F, NT, 0, R.st>>>(w->part, m, w->nb, w->gd, gstride, slot);
         R.c->launches += 2;
         RK(cudaGetLastError());
+        return MEPGL_OK;
+    };
+    auto energies = [&](int xbuf, std::vector<double> &e) -> mepgl_status {
+        RK(launch_energy(R.L, R.c->sc, xbuf, R.c->dscratch));
+        R.c->launches += 1;
+        e.resize(F);
+        RK(cudaMemcpyAsync(e.data(), R.c->dscratch, F * 8, cudaMemcpyDeviceToHost, R.st));
+        RK(cudaStreamSynchronize(R.st));
         return MEPGL_OK;
     };
     RK(R.grad(R.c->xi, w->g));
     mepgl_status st = gdots(R.x(), w->g, 0);
     if (st != MEPGL_OK) return st;
+    std::vector<double> e0, e1;
+    st = energies(R.c->xi, e0);
+    if (st != MEPGL_OK) return st;
     RK(R.read_scalars());
     if (w->gauge_m != m) {
-        w->gauge_h.assign(R.F, std::vector<double>());
-        w->gauge_age.assign(R.F, 1 << 30);
+        w->gauge_h.assign(F, std::vector<double>());
+        w->gauge_age.assign(F, 1 << 30);
         w->gauge_m = m;
     }
-    bool rebuild = false;
-    for (int n = 0; n < R.F; ++n)
-        if (R.S(n, S_ACTIVE) != 0.0 && w->gauge_age[n] >= refresh) rebuild = true;
-    for (int k = 0; k < m && rebuild; ++k)
-        for (int sg = 0; sg < 2; ++sg) {
-            k_gauge_apply<<<gg, NT, 0, R.st>>>(R.x(), R.xt(), B, w->gcoef, RF_MAX_GB, k, sg ? -h : h, s.nx, s.ny, nc,
-                                              q1, q2, idx, w->sc, -1);
-            R.c->launches += 1;
-            RK(cudaGetLastError());
-            RK(R.grad(xb, w->gp));
-            st = gdots(R.xt(), w->gp, 1 + 2 * k + sg);
-            if (st != MEPGL_OK) return st;
+    std::vector<int> todo(F, 0);
+    for (int n = 0; n < F; ++n) todo[n] = R.S(n, S_ACTIVE) != 0.0;
+    std::vector<double> gd((size_t)F * gstride);
+    for (int attempt = 0; attempt < 2; ++attempt) {
+        bool rebuild = false, any = false;
+        for (int n = 0; n < F; ++n) {
+            any |= todo[n] != 0;
+            if (todo[n] && (attempt > 0 || w->gauge_age[n] >= refresh)) rebuild = true;
         }
-    std::vector<double> gd((size_t)R.F * gstride);
-    RK(cudaMemcpyAsync(gd.data(), w->gd, gd.size() * 8, cudaMemcpyDeviceToHost, R.st));
-    RK(cudaStreamSynchronize(R.st));
-    std::vector<double> coef((size_t)R.F * RF_MAX_GB, 0.0);
-    for (int n = 0; n < R.F; ++n) {
-        if (R.S(n, S_ACTIVE) == 0.0) continue;
-        const double *G = gd.data() + (size_t)n * gstride;
-        std::vector<double> &H = w->gauge_h[n];
-        if (rebuild) {
-            H.assign(m * m, 0.0);
-            for (int i = 0; i < m; ++i)
-                for (int k = 0; k < m; ++k) H[k * m + i] = (G[(1 + 2 * i) * m + k] - G[(2 + 2 * i) * m + k]) / (2 * h);
-            for (int i = 0; i < m; ++i)
-                for (int k = 0; k < i; ++k) H[i * m + k] = H[k * m + i] = 0.5 * (H[i * m + k] + H[k * m + i]);
-            w->gauge_age[n] = 0;
-        }
-        ++w->gauge_age[n];
-        double *c = coef.data() + (size_t)n * RF_MAX_GB;
-        if (!cholesky_solve(m, H, G, c)) {
-            // not positive definite: c = -H^+ g over the positive part of the spectrum
-            std::vector<double> ev, V;
-            jacobi_eig(m, H, ev, V);
-            std::fill(c, c + m, 0.0);
-            for (int e = 0; e < m; ++e) {
-                if (!(ev[e] > 1e-12 * std::fabs(ev[m - 1]))) continue;
-                double proj = 0.0;
-                for (int i = 0; i < m; ++i) proj += V[i * m + e] * G[i];
-                for (int i = 0; i < m; ++i) c[i] -= V[i * m + e] * proj / ev[e];
+        if (!any) break;
+        for (int k = 0; k < m && rebuild; ++k)
+            for (int sg = 0; sg < 2; ++sg) {
+                k_gauge_apply<<<gg, NT, 0, R.st>>>(R.x(), R.xt(), B, w->gcoef, RF_MAX_GB, k, sg ? -h : h, s.nx, s.ny,
+                                                  nc, q1, q2, idx, w->sc, -1);
+                R.c->launches += 1;
+                RK(cudaGetLastError());
+                RK(R.grad(xb, w->gp));
+                st = gdots(R.xt(), w->gp, 1 + 2 * k + sg);
+                if (st != MEPGL_OK) return st;
+            }
+        RK(cudaMemcpyAsync(gd.data(), w->gd, gd.size() * 8, cudaMemcpyDeviceToHost, R.st));
+        RK(cudaStreamSynchronize(R.st));
+        std::vector<double> coef((size_t)F * RF_MAX_GB, 0.0);
+        for (int n = 0; n < F; ++n) {
+            if (!todo[n]) continue;
+            const double *G = gd.data() + (size_t)n * gstride;
+            std::vector<double> &H = w->gauge_h[n];
+            if (rebuild) {
+                H.assign(m * m, 0.0);
+                for (int i = 0; i < m; ++i)
+                    for (int k = 0; k < m; ++k)
+                        H[k * m + i] = (G[(1 + 2 * i) * m + k] - G[(2 + 2 * i) * m + k]) / (2 * h);
+                for (int i = 0; i < m; ++i)
+                    for (int k = 0; k < i; ++k) H[i * m + k] = H[k * m + i] = 0.5 * (H[i * m + k] + H[k * m + i]);
+                w->gauge_age[n] = 0;
+            }
+            double *c = coef.data() + (size_t)n * RF_MAX_GB;
+            if (!cholesky_solve(m, H, G, c)) {
+                // not positive definite: c = -H^+ g over the positive part of the spectrum
+                std::vector<double> ev, V;
+                jacobi_eig(m, H, ev, V);
+                std::fill(c, c + m, 0.0);
+                for (int e = 0; e < m; ++e) {
+                    if (!(ev[e] > 1e-12 * std::fabs(ev[m - 1]))) continue;
+                    double proj = 0.0;
+                    for (int i = 0; i < m; ++i) proj += V[i * m + e] * G[i];
+                    for (int i = 0; i < m; ++i) c[i] -= V[i * m + e] * proj / ev[e];
+                }
             }
         }
+        RK(cudaMemcpyAsync(w->gcoef, coef.data(), coef.size() * 8, cudaMemcpyHostToDevice, R.st));
+        k_gauge_apply<<<gg, NT, 0, R.st>>>(R.x(), R.xt(), B, w->gcoef, RF_MAX_GB, -1, 1.0, s.nx, s.ny, nc, q1, q2, idx,
+                                          w->sc, -1);
+        R.c->launches += 1;
+        RK(cudaGetLastError());
+        st = energies(xb, e1);
+        if (st != MEPGL_OK) return st;
+        RK(R.read_scalars());
+        for (int n = 0; n < F; ++n) {
+            const bool ok = todo[n] && std::isfinite(e1[n]) && e1[n] <= e0[n] + 1e-13 * std::fabs(e0[n]);
+            R.S(n, S_ACCEPT) = ok ? 1.0 : 0.0;
+            if (ok) {
+                todo[n] = 0;
+                ++w->gauge_age[n];
+            } else if (todo[n] && rebuild) {
+                todo[n] = 0;           // a fresh Hessian's step that raises the energy: no gauge step
+            }
+        }
+        RK(R.write_scalars());
+        LinArgs a = lin_args(R.x(), S_ACCEPT);
+        add_term(a, R.xt(), 1.0);
+        RK(R.lin(a));
     }
-    RK(cudaMemcpyAsync(w->gcoef, coef.data(), coef.size() * 8, cudaMemcpyHostToDevice, R.st));
-    k_gauge_apply<<<gg, NT, 0, R.st>>>(R.x(), R.x(), B, w->gcoef, RF_MAX_GB, -1, 1.0, s.nx, s.ny, nc, q1, q2, idx,
-                                      w->sc, S_ACTIVE);
-    R.c->launches += 1;
-    RK(cudaGetLastError());
     return MEPGL_OK;
 }
 
