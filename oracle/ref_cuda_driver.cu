@@ -17,9 +17,9 @@
 // with CUDA events, nlcgSteps(steps, ...) -- the reference's host loop with
 // its own synchronisations, as loop() calls it once per outer iteration
 // (mepgl/src/mepgl.cu:156-172) -- and prints one JSON
-// line with the time per step and the per-image energies after the steps
-// (computeFreeEnergy), so that the reference build's results can be compared
-// with this library's on the same input.
+// line with the time per step and the per-image energies of the last step,
+// so that the reference build's results can be compared with this
+// library's on the same input.
 //
 //   ref_nlcg INPUT STEPS WARMUP [maxwell]
 #include <cmath>
@@ -150,11 +150,11 @@ int main(int argc, char **argv)
     CK(cudaEventSynchronize(e1));
     float ms = 0.f;
     CK(cudaEventElapsedTime(&ms, e0, e1));
-    real *dev_fe = nullptr;
-    CK(cudaMallocManaged(&dev_fe, F * sizeof(real)));
-    computeFreeEnergy(F, dev_comp_nn, dev_sc_nn, dp[0], dp[1], dp[2], dp[3], dp[4], dp[5], dp[6], dp[7], dp[8],
-                      dq[0], dq[1], dq[2], dq[3], dq[4], x[0], x[1], x[2], dev_fe);
-    CK(cudaDeviceSynchronize());
+    // the per-image energies nlcgSteps reports (the last line polynomial's
+    // constant term: F before the last update, mepgl/src/nlcg.cu:1036,1567);
+    // computeFreeEnergy is not used: it accumulates into an uninitialised
+    // scratch buffer (mepgl/src/nlcg.cu:223-232)
+    const real *dev_fe = fenergy;
     std::printf("{\"n\": %d, \"images\": %d, \"real_bytes\": %d, \"steps\": %d, \"warmup\": %d, \"ms_per_step\": %.6f, "
                 "\"site_images_per_s\": %.6e, \"fenergy\": [",
                 N, F, (int)sizeof(real), steps, warmup, ms / steps, (double)F * M * steps / (ms / 1e3));

@@ -1,7 +1,7 @@
 """The reference's own CUDA build (its unmodified nlcg.cu and parallel_sum.cu
 compiled for this GPU by oracle/ref_cuda_build.py) against this library on the
 same input: after the same NLCG steps with the reference's options the
-per-image energies agree.  Skipped where the reference sources were not
+per-image energies of the last step agree.  Skipped where the reference sources were not
 staged into baseline/_ref (they come from the reference tree, which only some
 machines have)."""
 import numpy as np
@@ -37,6 +37,6 @@ def test_reference_cuda_build_matches_the_library(native, cfg, prec, steps, rtol
     c.set_state(st)
     c.nlcg_steps(warmup)
     c.nlcg_steps(steps)
-    got = c.compute_free_energy()
+    got = c.image_scalars()["fenergy"]        # F before the last update, as the reference reports it
     np.testing.assert_allclose(got, ref["fenergy"], rtol=rtol)
     c.close()
