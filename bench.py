@@ -21,10 +21,14 @@ per step).  ``--impl reference`` times the CPU implementation of
 the same step (the C restatement in oracle/, all host threads) on the same
 workload.
 
-``time_to_end_state`` times FP64 against FP32-then-FP64 relaxation of the
-same 256x256 string to a converged end state (the barrier estimate of the
-string method itself does not converge to 1e-6; see barrier.py);
-``--ttb-config 1`` runs it on the small single-component string instead.
+``time_to_barrier`` times the barrier protocol on the same 256x256 string:
+a string phase (IEEE FP64, or FP32 for the mixed schedule) seeds an IEEE
+FP64 refinement of the initial minimum and of the index-1 saddle; the time
+is until dF = F(saddle) - F(minimum) stays within 1e-6 of the converged FP64
+value measured in the same run; ``--ttb-config 1`` runs it on the small
+single-component string instead.  ``reference_cuda`` times the reference's
+own CUDA NLCG (its unmodified nlcg.cu built for this GPU) beside this
+library on configs 2 (FP32) and 1 (FP64).
 
 Multi-GPU: the path does not shard within a string; ``--gpus N`` runs N
 independent replicas (one string per GPU) and reports the aggregate.
@@ -320,6 +324,47 @@ def run_ours(args):
     fp64 = fp64_leg(native.FP64_NATIVE)
     fp64["paired"] = fp64_leg(native.FP64_PAIRED)
 
+    # ---- the reference's own CUDA build on this GPU ---------------------------
+    # its unmodified nlcg.cu / parallel_sum.cu compiled for sm_103a (staged from
+    # the reference tree into baseline/_ref by build()), one nlcgSteps call of
+    # `steps` steps timed with CUDA events, beside this library on the same
+    # workload and precision (compat line search and polynomial, as the
+    # reference); config 2 in FP32 and config 1 in FP64
+    refcuda = None
+    if rank == 0 and not args.no_refcuda:
+        from oracle import ref_cuda_build as RC
+        if not RC.staged():
+            refcuda = {"unavailable": "reference CUDA sources not staged in baseline/_ref (no reference tree "
+                                      "where build() ran)"}
+        else:
+            refcuda = {}
+            prob1, st1 = workloads.config1()
+            for key, (pr, s0, prec, ours_prec) in {"config2_fp32": (prob, st, "f32", "fp32"),
+                                                   "config1_fp64": (prob1, st1, "f64", "fp64")}.items():
+                try:
+                    k_steps = 20
+                    r = RC.run(pr, s0, prec, k_steps, 3)
+                    c_o = native.StringContext(pr, s0.n_images, ours_prec, stream=stream.cuda_stream)
+                    c_o.set_state(s0)
+                    c_o.nlcg_steps(3)
+                    barrier()
+                    ev0.record(stream)
+                    c_o.nlcg_steps(k_steps)
+                    ev1.record(stream)
+                    barrier()
+                    ms_o = ev0.elapsed_time(ev1) / k_steps
+                    c_o.close()
+                    units = pr.nx * pr.ny * s0.n_images
+                    refcuda[key] = {"reference_ms_per_step": r["ms_per_step"],
+                                    "reference_site_images_per_s": r["site_images_per_s"],
+                                    "ours_ms_per_step": ms_o, "ours_site_images_per_s": units / (ms_o / 1e3),
+                                    "speedup": r["ms_per_step"] / ms_o,
+                                    "note": "reference: nlcgSteps (12 launches, 4 two-level sums with per-call "
+                                            "cudaMalloc/cudaFree, host syncs per step); ours: the library's "
+                                            "default NLCG path, same options"}
+                except Exception as e:          # a failed reference build must not lose the bench line
+                    refcuda[key] = {"unavailable": f"{type(e).__name__}: {str(e)[:200]}"}
+
     # ---- end to end through the C ABI with pinned host buffers -----------------
     shape = (F, prob.ny, prob.nx, 2)
     host = [torch.from_numpy(np.ascontiguousarray(x, np.float32)).pin_memory()
@@ -370,49 +415,46 @@ def run_ours(args):
                    f"+ {RELAX} NLCG steps + per-image energies to host",
            "serial": {"value": rate(serial_s), "step": "the same with a synchronous state upload per step"}}
 
-    # ---- time to a converged end state, FP64 vs FP32+FP64 (small string) -------
-    # The barrier estimate of the string method does not converge to 1e-6 on
-    # these workloads (its value drifts with the reparametrization cadence), so
-    # this reports the time until the end-state energy difference F_{F-1} - F_0
-    # (which does converge) stays within 1e-6 of the FP64 run's final value.
-    # Default (--ttb-config 2): the mixed-precision workload itself, the 256x256
-    # two-component string (100 steps per reparametrization; about 2.5 minutes),
-    # IEEE FP64 against FP32 then paired-FP64 polish, to the value its long FP64
-    # run converges to.  --ttb-config 1: the small single-component string
-    # (64x64, 16 images, 50 steps per reparametrization; latency-bound, seconds).
+    # ---- time to barrier, plain FP64 against FP32 + FP64 ----------------------
+    # One run (mepgl_gb300.barrier.time_to_barrier): a string phase in the
+    # schedule's precision (mode L, linear reparametrization + `relax` NLCG
+    # steps, until the string's maximum image and estimate plateau), then the
+    # IEEE FP64 refinement of image 0 to its minimum and of that image to the
+    # index-1 saddle.  dF* = F(saddle) - F(minimum) of a first FP64 run
+    # refined to |g| <= 1e-10 (measured here, not hard-coded); each run's time
+    # to barrier is when its trace (the string's estimate, then the refined
+    # barrier) enters and stays within 1e-6 of dF*.  Schedules: "fp64" IEEE
+    # double string, "mixed" FP32 string, "fp64_paired" the string in
+    # float-float FP64 (labelled as such); the refinement is IEEE double in all.
     ttb = None
     if rank == 0 and not args.no_ttb:
         from mepgl_gb300 import barrier as B
-        rmx = r64p = None
-        if args.ttb_config == 2:
-            target = 1.00779044   # F_{F-1} - F_0 after 600 outer iterations of FP64 (IEEE) relaxation
-            r64, _ = B.run(2, 100, 160, "fp64")
-            rmxp, _ = B.run(2, 100, 250, "mixed", -1, fp64_arith="paired")
-            work = "two-component GL 256x256 dx=0.4, 64 images, mode L, 100 NLCG steps per iteration"
-        else:
-            r64, _ = B.run(1, 50, 150, "fp64")
-            target = r64[-1][3]
-            rmx, _ = B.run(1, 50, 150, "mixed", -1)
-            rmxp, _ = B.run(1, 50, 150, "mixed", -1, fp64_arith="paired")
-            r64p, _ = B.run(1, 50, 150, "fp64", fp64_arith="paired")
-            work = "single-component GL 64x64 dx=0.5, 16 images, mode L, 50 NLCG steps per iteration"
+        cfg, relax, reps = args.ttb_config, 10, args.ttb_repeats
+        ref = B.time_to_barrier(cfg, "fp64", relax, g_tol=1e-10)
+        target = ref["barrier"]
+        runs = {"fp64": [ref], "mixed": [], "fp64_paired": []}
+        for _ in range(reps):
+            runs["mixed"].append(B.time_to_barrier(cfg, "mixed", relax))
+            if len(runs["fp64"]) < reps:
+                runs["fp64"].append(B.time_to_barrier(cfg, "fp64", relax))
+        runs["fp64_paired"].append(B.time_to_barrier(cfg, "fp64_paired", relax))
 
-        def t_to(rec):
-            if rec is None:
-                return None
-            return B.time_within([x[0] for x in rec], [x[3] for x in rec], target, 1e-6)
-        ttb = {"quantity": "F_end - F_0 within 1e-6 of the converged FP64 value",
-               "workload": work, "target": target,
-               "fp64_s": t_to(r64),                 # IEEE double throughout
-               "mixed_s": t_to(rmx),                # FP32 until the end states plateau, then IEEE double
-               "mixed_paired_s": t_to(rmxp),        # FP32, then paired (float-float) FP64
-               "fp64_paired_s": t_to(r64p),         # paired FP64 throughout
-               "mixed_fp32_iterations": sum(1 for x in rmxp if x[4] == "fp32"),
-               "ends_fp64": r64[-1][3], "ends_mixed": rmxp[-1][3],
-               "barrier_fp64": r64[-1][1], "barrier_mixed": rmxp[-1][1]}
-        if ttb["fp64_s"] and ttb["mixed_paired_s"]:
-            ttb["speedup_mixed_vs_fp64"] = ttb["fp64_s"] / ttb["mixed_paired_s"]
-        ttb["ends_rel_err_mixed"] = abs(ttb["ends_mixed"] - target) / abs(target)
+        def leg(rs, rtol):
+            ts = [B.time_within([x[0] for x in r["trace"]], [x[1] for x in r["trace"]], target, rtol) for r in rs]
+            return {"times_s": ts, "median_s": statistics.median(ts) if all(t is not None for t in ts) else None,
+                    "string_s": [r["string_s"] for r in rs], "string_iterations": [r["string_iterations"] for r in rs],
+                    "newton": [r["newton"] for r in rs], "total_s": [r["total_s"] for r in rs],
+                    "barrier_rel_err": [abs(r["barrier"] - target) / abs(target) for r in rs],
+                    "is_saddle": [r["is_saddle"] for r in rs], "seed_image": [r["seed_image"] for r in rs]}
+        work = {1: "single-component GL 64x64 dx=0.5, 16 images", 2: WORKLOAD}[cfg]
+        ttb = {"quantity": "dF = F(saddle) - F(minimum), refined stationary points; time until within 1e-6 of dF*",
+               "workload": work, "relax_steps": relax, "target_dF": target,
+               "target_g_norms": ref["g_norms"], "target_min_curvature": ref["min_curvature"],
+               "fp64": leg(runs["fp64"], 1e-6), "mixed": leg(runs["mixed"], 1e-6),
+               "fp64_paired_string": leg(runs["fp64_paired"], 1e-6),
+               "fp64_to_1e-8": leg(runs["fp64"], 1e-8)}
+        if ttb["fp64"]["median_s"] and ttb["mixed"]["median_s"]:
+            ttb["speedup_mixed_vs_fp64"] = ttb["fp64"]["median_s"] / ttb["mixed"]["median_s"]
 
     # ---- CPU baseline (rank 0, N = 1 only) ------------------------------------
     cpu = None
@@ -429,7 +471,7 @@ def run_ours(args):
             "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": bench_config(world),
             "e2e": e2e, "gpu_launches": launches, "roofline": roofline, "kernels": kern, "fp64": fp64,
-            "cpu_baseline": cpu, "clocks": clk.summary(), "time_to_end_state": ttb,
+            "cpu_baseline": cpu, "clocks": clk.summary(), "time_to_barrier": ttb, "reference_cuda": refcuda,
         }
         print(json.dumps(line), flush=True)
     ctx.close()
@@ -445,10 +487,11 @@ def main(argv=None):
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=("ours", "reference"), default="ours")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
-    ap.add_argument("--no-ttb", action="store_true", help="skip the time-to-converged-end-state leg")
+    ap.add_argument("--no-ttb", action="store_true", help="skip the time-to-barrier leg")
+    ap.add_argument("--no-refcuda", action="store_true", help="skip timing the reference's own CUDA build")
     ap.add_argument("--ttb-config", type=int, choices=(1, 2), default=2,
-                    help="workload of that leg: 2 (the 256x256 mixed-precision string, about 2.5 minutes) "
-                         "or 1 (64x64, seconds)")
+                    help="workload of that leg: 2 (the 256x256 mixed-precision string) or 1 (64x64, seconds)")
+    ap.add_argument("--ttb-repeats", type=int, default=3, help="runs per schedule of the time-to-barrier leg")
     args = ap.parse_args(argv)
     if args.impl == "reference":
         return run_reference(args)
