@@ -15,7 +15,9 @@ later build.
     python -m mepgl_gb300.autotune [--workload string|sweep] [--out mepgl_gb300/tuning.json]
 
 Workloads: ``string`` = the 256x256, 64-image two-component string;
-``sweep`` = 16 strings of the parameter sweep (uneven sizes, one component).
+``sweep`` = the 64 strings of the parameter sweep (uneven sizes, one
+component).  ``--keep-selection`` records a workload's results beside the
+others without changing the definitions the build applies.
 """
 from __future__ import annotations
 
@@ -77,7 +79,7 @@ def measure(workload: str, steps: int = 20, warmup: int = 4):
         ctx.set_state(st)
     else:
         from .sweep import build_batch
-        ctx, *_ = build_batch(16, stream=stream.cuda_stream)
+        ctx, *_ = build_batch(64, stream=stream.cuda_stream)
     ctx.nlcg_steps(warmup)
     torch.cuda.synchronize()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -94,6 +96,8 @@ def main(argv=None):
     ap.add_argument("--out", default=TUNING)
     ap.add_argument("--measure", action="store_true", help=argparse.SUPPRESS)
     ap.add_argument("--jobs", type=int, default=min(8, os.cpu_count() or 1))
+    ap.add_argument("--keep-selection", action="store_true",
+                    help="record this workload's results without changing the build's selection")
     a = ap.parse_args(argv)
     if a.measure:
         print(json.dumps({"ms_per_step": measure(a.workload)}))
@@ -128,8 +132,9 @@ def main(argv=None):
         with open(a.out) as f:
             doc = json.load(f)
     doc.setdefault("by_workload", {})[a.workload] = dict(device=device, results=results, best=best["defines"])
-    doc["selected"] = best["defines"]
-    doc["selected_by"] = a.workload
+    if not a.keep_selection or "selected" not in doc:
+        doc["selected"] = best["defines"]
+        doc["selected_by"] = a.workload
     with open(a.out, "w") as f:
         json.dump(doc, f, indent=1)
     print(json.dumps({"selected": best["defines"], "ms_per_step": best["ms_per_step"]}))
