@@ -63,24 +63,48 @@ def variant_dir(n: int, dx: float, comps: int, prec: str) -> str:
     return os.path.join(BASE, f"N{n}_dx{dx!r}_C{comps}_{prec}")
 
 
+def _config_cuh(n: int, dx: float, comps: int, prec: str) -> str:
+    """config.cuh as the reference's header generator writes it
+    (mepgl/mepgl_lib/launcher_utils.py:84-110): 512 threads per block in FP64,
+    1024 in FP32."""
+    lines = ["#ifndef CONFIG_CUH", "#define CONFIG_CUH", '#include <string>', '#include "real.cuh"',
+             "const int devNumber = 0;"]
+    if comps == 2:
+        lines.append("#define MULTICOMPONENT")
+    lines += [f"constexpr int N = {n};", f"constexpr int blockSizeX = {512 if prec == 'f64' else 1024};",
+              "constexpr int gridSizeX = (int)((N*N)/blockSizeX + 1);", f"constexpr real dx = {dx!r};",
+              "constexpr int default_relaxation_step_number = 10;", "#endif"]
+    return "\n".join(lines) + "\n"
+
+
 def compile(n: int, dx: float, comps: int, prec: str) -> str:
-    """Compile one variant (sm_103a) and return the path of its binary."""
-    from oracle.ref_build import _config_cuh, _real_cuh
+    """Compile one variant (sm_103a) and return the path of its binary.
+
+    FP32 variants get -maxrregcount=64: nvcc 13 gives the reference's
+    heaviest kernel 68 registers for sm_103a, and its 1024-thread blocks
+    (above) then need more than the 65,536 registers of an SM, so the launch
+    fails -- silently, since the reference checks no launch (the sm_61 build
+    it was written for fits in 64).  The sources are unchanged."""
+    from oracle.ref_build import _real_cuh
     if not staged():
         raise FileNotFoundError("reference CUDA sources not staged (oracle.ref_cuda_build.stage())")
     d = variant_dir(n, dx, comps, prec)
     exe = os.path.join(d, "ref_nlcg")
     drv = os.path.join(HERE, "ref_cuda_driver.cu")
     srcs = [os.path.join(SRC, "nlcg.cu"), os.path.join(SRC, "parallel_sum.cu"), drv]
-    if os.path.isfile(exe) and os.path.getmtime(exe) >= max(os.path.getmtime(s) for s in srcs):
-        return exe
     os.makedirs(d, exist_ok=True)
-    with open(os.path.join(d, "config.cuh"), "w") as f:
-        f.write(_config_cuh(n, dx, comps, False))
-    with open(os.path.join(d, "real.cuh"), "w") as f:
-        f.write(_real_cuh(prec))
+    for name, text in (("config.cuh", _config_cuh(n, dx, comps, prec)), ("real.cuh", _real_cuh(prec))):
+        path = os.path.join(d, name)
+        if not os.path.isfile(path) or open(path).read() != text:
+            with open(path, "w") as f:
+                f.write(text)
+    deps = srcs + [os.path.join(d, "config.cuh"), os.path.join(d, "real.cuh"), os.path.abspath(__file__)]
+    if os.path.isfile(exe) and os.path.getmtime(exe) >= max(os.path.getmtime(s) for s in deps):
+        return exe
     nvcc = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
     cmd = [nvcc, "-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-w", "-I", d, "-I", SRC, "-o", exe + ".tmp"]
+    if prec != "f64":
+        cmd += ["-maxrregcount=64"]
     r = subprocess.run(cmd + srcs, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"reference CUDA build failed:\n{r.stdout}\n{r.stderr}")
@@ -116,7 +140,10 @@ def run(prob, state, prec: str, steps: int, warmup: int, workdir: str | None = N
     r = subprocess.run([exe, path, str(steps), str(warmup)], capture_output=True, text=True, timeout=timeout)
     if r.returncode != 0:
         raise RuntimeError(f"reference CUDA run failed ({r.returncode}): {r.stderr[-2000:]}")
-    return json.loads(r.stdout.strip().splitlines()[-1])
+    out = json.loads(r.stdout.strip().splitlines()[-1])
+    if out.get("launch_error"):
+        raise RuntimeError(f"reference CUDA kernels failed to launch: {out['launch_error']}")
+    return out
 
 
 if __name__ == "__main__":

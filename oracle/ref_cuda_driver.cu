@@ -150,14 +150,18 @@ int main(int argc, char **argv)
     CK(cudaEventSynchronize(e1));
     float ms = 0.f;
     CK(cudaEventElapsedTime(&ms, e0, e1));
+    // the reference checks none of its launches; a kernel that could not
+    // launch (e.g. too many registers for its block size) is reported here
+    const cudaError_t launch = cudaGetLastError();
     // the per-image energies nlcgSteps reports (the last line polynomial's
     // constant term: F before the last update, mepgl/src/nlcg.cu:1036,1567);
     // computeFreeEnergy is not used: it accumulates into an uninitialised
     // scratch buffer (mepgl/src/nlcg.cu:223-232)
     const real *dev_fe = fenergy;
-    std::printf("{\"n\": %d, \"images\": %d, \"real_bytes\": %d, \"steps\": %d, \"warmup\": %d, \"ms_per_step\": %.6f, "
-                "\"site_images_per_s\": %.6e, \"fenergy\": [",
-                N, F, (int)sizeof(real), steps, warmup, ms / steps, (double)F * M * steps / (ms / 1e3));
+    std::printf("{\"n\": %d, \"images\": %d, \"real_bytes\": %d, \"block\": %d, \"steps\": %d, \"warmup\": %d, "
+                "\"ms_per_step\": %.6f, \"site_images_per_s\": %.6e, \"launch_error\": \"%s\", \"fenergy\": [",
+                N, F, (int)sizeof(real), blockSizeX, steps, warmup, ms / steps, (double)F * M * steps / (ms / 1e3),
+                launch == cudaSuccess ? "" : cudaGetErrorString(launch));
     for (int n = 0; n < F; ++n) std::printf("%s%.17g", n ? ", " : "", (double)dev_fe[n]);
     std::printf("]}\n");
     return 0;
