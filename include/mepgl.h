@@ -399,7 +399,8 @@ typedef struct mepgl_refine_options {
     double mu0;                /* initial Levenberg-Marquardt shift (1e-3)        */
     double cg_eta;             /* CG relative tolerance cap (0.1)                 */
     int32_t max_retries;       /* rejected steps retried per iteration (8)        */
-    int32_t gauge_refresh;     /* iterations a gauge-subspace Hessian is reused (4);
+    int32_t gauge_refresh;     /* iterations a gauge-subspace Hessian is reused; 0 =
+                                  auto: 1 up to 64 gauge functions, else 4 (default);
                                   kept between calls while the state is unchanged */
 } mepgl_refine_options;
 

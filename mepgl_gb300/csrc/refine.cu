@@ -1037,7 +1037,7 @@ void mepgl_default_refine_options(mepgl_refine_options *o)
     o->mu0 = 1e-3;
     o->cg_eta = 0.1;
     o->max_retries = 8;
-    o->gauge_refresh = 4;
+    o->gauge_refresh = 0;
 }
 
 mepgl_status mepgl_refine_stationary(mepgl_ctx *c, const int32_t *kind, const void *mode_a, const void *mode_psi_1,
@@ -1056,7 +1056,7 @@ mepgl_status mepgl_refine_stationary(mepgl_ctx *c, const int32_t *kind, const vo
     if (opt_in) opt = *opt_in;
     if (opt.lanczos_steps < 2 || opt.lanczos_steps > RF_MAX_LZ || opt.gauge_degree < -1 ||
         opt.gauge_degree > RF_MAX_DEG || opt.max_newton < 0 || opt.max_cg < 1 || !(opt.g_tol >= 0) ||
-        !(opt.mu0 > 0) || !(opt.cg_eta > 0 && opt.cg_eta < 1) || opt.max_retries < 0 || opt.gauge_refresh < 1)
+        !(opt.mu0 > 0) || !(opt.cg_eta > 0 && opt.cg_eta < 1) || opt.max_retries < 0 || opt.gauge_refresh < 0)
         return ctx_fail(c, MEPGL_ERR_INVALID_ARG, "mepgl_refine_stationary: option out of range");
     const int F = c->strings[0].F;
     for (int n = 0; n < F; ++n)
@@ -1163,7 +1163,10 @@ mepgl_status mepgl_refine_stationary(mepgl_ctx *c, const int32_t *kind, const vo
         if (B.m > 0) {
             st = set_active(act);
             const auto tg0 = std::chrono::steady_clock::now();
-            if (st == MEPGL_OK) st = gauge_step(R, B, 1e-4, opt.gauge_refresh);
+            // auto: small bases are cheap to rebuild and a fresh Hessian saves
+            // iterations; large ones (2m gradients each) are reused
+            const int refresh = opt.gauge_refresh > 0 ? opt.gauge_refresh : (B.m <= 64 ? 1 : 4);
+            if (st == MEPGL_OK) st = gauge_step(R, B, 1e-4, refresh);
             if (st != MEPGL_OK) return st;
             t_gauge = std::chrono::duration<double>(std::chrono::steady_clock::now() - tg0).count();
         }
