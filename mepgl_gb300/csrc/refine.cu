@@ -108,6 +108,13 @@ struct RefineWork {
     std::vector<int> gauge_age;
     int gauge_m = -1;
     uint64_t state_version = ~0ull;   // the context's state version after the last refinement call
+    // gauge Hessians are built from many perturbed copies of the images at
+    // once: an internal FP64 context holding `wide_images` of them as one
+    // string (chunks of the 2m F perturbations), its gauge partials and sums
+    mepgl_ctx *wide = nullptr;
+    int wide_images = 0, wide_nb = 16;
+    double *wide_part = nullptr, *wide_gd = nullptr;
+    size_t wide_gd_cap = 0;
 };
 
 void refine_free(RefineWork *w)
@@ -122,6 +129,9 @@ void refine_free(RefineWork *w)
     cudaFree(w->coef);
     cudaFree(w->gcoef);
     cudaFree(w->gd);
+    cudaFree(w->wide_part);
+    cudaFree(w->wide_gd);
+    if (w->wide) mepgl_destroy(w->wide);
     delete w;
 }
 
@@ -417,6 +427,34 @@ __global__ void __launch_bounds__(NT) k_gauge_apply(Vec in, Vec out, GaugeBasis 
     }
 }
 
+// Wide copies for the gauge Hessian: image b of `out` is perturbation
+// w = w0 + b of the 2 m F perturbations, U(+-h phi_i) applied to image n of
+// `in`, w = (n m + i) 2 + sign.
+__global__ void __launch_bounds__(NT) k_gauge_perturb(Vec in, Vec out, GaugeBasis B, int F, int w0, int n_out,
+                                                      double h, int nx, int ny, int ncomp, double q1, double q2,
+                                                      double idx)
+{
+    const int b = blockIdx.y, w = w0 + b;
+    if (b >= n_out || w >= 2 * B.m * F) return;
+    const int n = w / (2 * B.m), r = w % (2 * B.m), i = r >> 1;
+    const double mult = (r & 1) ? -h : h;
+    const long M = (long)nx * ny;
+    for (long s = blockIdx.x * (long)NT + threadIdx.x; s < M; s += (long)gridDim.x * NT) {
+        const int ii = (int)(s % nx), jj = (int)(s / nx);
+        const GaugeField G = gauge_field(B, nullptr, i, ii, jj, nx, ny, idx);
+        const long o = 2 * ((long)n * M + s), ob = 2 * ((long)b * M + s);
+        out.p[0][ob] = in.p[0][o] + mult * G.gx;
+        out.p[0][ob + 1] = in.p[0][o + 1] + mult * G.gy;
+        for (int a = 0; a < ncomp; ++a) {
+            double sn, cs;
+            sincos((a ? q2 : q1) * mult * G.chi, &sn, &cs);
+            const double re = in.p[1 + a][o], im = in.p[1 + a][o + 1];
+            out.p[1 + a][ob] = re * cs - im * sn;
+            out.p[1 + a][ob + 1] = re * sn + im * cs;
+        }
+    }
+}
+
 // Partials of dE/dc_m = g . J phi_m = sum_s g_A . grad phi_m + sum_a q_a phi_m (Re psi_a g_Im,a - Im psi_a g_Re,a),
 // for the basis functions [16 z, 16 z + 16) of block row z.
 __global__ void __launch_bounds__(NT) k_gauge_dots(Vec x, Vec g, GaugeBasis B, int nx, int ny, int ncomp, double q1,
@@ -690,6 +728,87 @@ mepgl_status hess_vec(Ctx &R, const Vec &u, const Vec &y, bool with_mu)
     return MEPGL_OK;
 }
 
+// Orbit gradients g . J phi_k at the 2 m F perturbed states U(+-h phi_i) x_n,
+// into out[((n m + i) 2 + sign) m + k].  The perturbed states are images of
+// an internal context (chunks of at most 2^25 sites in all), so each
+// gradient launch covers hundreds of images instead of the F of the
+// refinement.
+mepgl_status wide_gauge_gradients(Ctx &R, const GaugeBasis &B, double h, std::vector<double> &out)
+{
+    RefineWork *w = R.w;
+    mepgl_ctx *c = R.c;
+    const StringHost &s = c->strings[0];
+    const int m = B.m, F = R.F, total = 2 * m * F;
+    const long M = s.M();
+    const int cap = (int)std::max<long>(1, std::min<long>(total, (1L << 25) / M));
+    if (!w->wide || w->wide_images != cap) {
+        if (w->wide) mepgl_destroy(w->wide);
+        w->wide = nullptr;
+        mepgl_problem p;
+        memset(&p, 0, sizeof(p));
+        p.nx = s.nx;
+        p.ny = s.ny;
+        p.n_images = cap;
+        p.multicomponent = c->ncomp == 2;
+        p.thin_film = c->thin_film;
+        p.precision = MEPGL_FP64;
+        p.dx = s.dx;
+        p.q_1 = s.q[0];
+        p.q_2 = s.q[1];
+        p.eta = s.eta;
+        p.gamma = s.gamma;
+        p.delta = s.delta;
+        const double **pp[9] = {&p.a_1, &p.b_1, &p.m_xx_1, &p.m_yy_1, &p.a_2, &p.b_2, &p.m_xx_2, &p.m_yy_2, &p.h};
+        for (int k = 0; k < 9; ++k) *pp[k] = s.params[k].empty() ? nullptr : s.params[k].data();
+        if (c->ncomp == 1)
+            for (int k = 4; k < 8; ++k) *pp[k] = nullptr;
+        p.comp_domain = s.comp.data();
+        p.sc_domain = s.sc.data();
+        mepgl_options o = c->opt;
+        o.fp64_arith = MEPGL_FP64_NATIVE;
+        if (mepgl_create(&p, &o, c->stream, &w->wide) != MEPGL_OK)
+            return ctx_fail(c, MEPGL_ERR_CUDA, std::string("refine: gauge workspace: ") + mepgl_last_error(nullptr));
+        w->wide_images = cap;
+        cudaFree(w->wide_part);
+        w->wide_part = nullptr;
+        RK(cudaMalloc(&w->wide_part, (size_t)cap * m * w->wide_nb * sizeof(double)));
+    }
+    if (w->wide_gd_cap < (size_t)total * m) {
+        cudaFree(w->wide_gd);
+        w->wide_gd = nullptr;
+        RK(cudaMalloc(&w->wide_gd, (size_t)total * m * sizeof(double)));
+        w->wide_gd_cap = (size_t)total * m;
+    }
+    mepgl_ctx *wc = w->wide;
+    const StringHost &ws = wc->strings[0];
+    Vec xw{{(double *)ws.x[0][0], (double *)ws.x[0][1], (double *)ws.x[0][2]}};
+    Vec gw{{(double *)ws.g[0][0], (double *)ws.g[0][1], (double *)ws.g[0][2]}};
+    Launch Lw = ctx_string_launch(wc, 0);
+    Lw.paired = 0;
+    Lw.stream = R.st;
+    const double q1 = s.q[0], q2 = s.q[1], idx = 1.0 / s.dx;
+    const int nc = c->ncomp;
+    for (int w0 = 0; w0 < total; w0 += cap) {
+        const int nW = std::min(cap, total - w0);
+        const dim3 gp((unsigned)std::min<long>((M + NT - 1) / NT, 256), nW);
+        k_gauge_perturb<<<gp, NT, 0, R.st>>>(R.x(), xw, B, F, w0, nW, h, s.nx, s.ny, nc, q1, q2, idx);
+        RK(cudaGetLastError());
+        FieldPtrs fp;
+        for (int f = 0; f < 3; ++f) fp.p[f] = f < w->nf ? gw.p[f] : nullptr;
+        RK(launch_gradient_only(Lw, 0, fp, 0));
+        const dim3 gdg(w->wide_nb, nW, (m + RF_GB_CHUNK - 1) / RF_GB_CHUNK);
+        k_gauge_dots<<<gdg, NT, 0, R.st>>>(xw, gw, B, s.nx, s.ny, nc, q1, q2, idx, w->wide_part, w->wide_nb);
+        k_gauge_sums<<<nW, NT, 0, R.st>>>(w->wide_part, m, w->wide_nb, w->wide_gd + (size_t)w0 * m, m, 0);
+        RK(cudaGetLastError());
+        c->launches += 4;
+        R.grads += (nW + F - 1) / F;      // in units of the refinement's own gradient launches
+    }
+    out.resize((size_t)total * m);
+    RK(cudaMemcpyAsync(out.data(), w->wide_gd, out.size() * 8, cudaMemcpyDeviceToHost, R.st));
+    RK(cudaStreamSynchronize(R.st));
+    return MEPGL_OK;
+}
+
 // Gauge-subspace Newton step on every image with S_ACTIVE != 0.  The m x m
 // Hessian (2m gradient evaluations) is rebuilt when older than `refresh`
 // iterations; in between only the orbit gradient is evaluated.  The step is
@@ -742,16 +861,11 @@ mepgl_status gauge_step(Ctx &R, const GaugeBasis &B, double h, int refresh)
             if (todo[n] && (attempt > 0 || w->gauge_age[n] >= refresh)) rebuild = true;
         }
         if (!any) break;
-        for (int k = 0; k < m && rebuild; ++k)
-            for (int sg = 0; sg < 2; ++sg) {
-                k_gauge_apply<<<gg, NT, 0, R.st>>>(R.x(), R.xt(), B, w->gcoef, RF_MAX_GB, k, sg ? -h : h, s.nx, s.ny,
-                                                  nc, q1, q2, idx, w->sc, -1);
-                R.c->launches += 1;
-                RK(cudaGetLastError());
-                RK(R.grad(xb, w->gp));
-                st = gdots(R.xt(), w->gp, 1 + 2 * k + sg);
-                if (st != MEPGL_OK) return st;
-            }
+        std::vector<double> gw;
+        if (rebuild) {
+            st = wide_gauge_gradients(R, B, h, gw);
+            if (st != MEPGL_OK) return st;
+        }
         RK(cudaMemcpyAsync(gd.data(), w->gd, gd.size() * 8, cudaMemcpyDeviceToHost, R.st));
         RK(cudaStreamSynchronize(R.st));
         std::vector<double> coef((size_t)F * RF_MAX_GB, 0.0);
@@ -761,9 +875,10 @@ mepgl_status gauge_step(Ctx &R, const GaugeBasis &B, double h, int refresh)
             std::vector<double> &H = w->gauge_h[n];
             if (rebuild) {
                 H.assign(m * m, 0.0);
+                const double *Gw = gw.data() + (size_t)n * 2 * m * m;   // [(i, sign)][k]
                 for (int i = 0; i < m; ++i)
                     for (int k = 0; k < m; ++k)
-                        H[k * m + i] = (G[(1 + 2 * i) * m + k] - G[(2 + 2 * i) * m + k]) / (2 * h);
+                        H[k * m + i] = (Gw[(2 * i) * m + k] - Gw[(2 * i + 1) * m + k]) / (2 * h);
                 for (int i = 0; i < m; ++i)
                     for (int k = 0; k < i; ++k) H[i * m + k] = H[k * m + i] = 0.5 * (H[i * m + k] + H[k * m + i]);
                 w->gauge_age[n] = 0;
