@@ -445,6 +445,8 @@ def run_ours(args):
                     "string_s": [r["string_s"] for r in rs], "string_iterations": [r["string_iterations"] for r in rs],
                     "newton": [r["newton"] for r in rs], "total_s": [r["total_s"] for r in rs],
                     "barrier_rel_err": [abs(r["barrier"] - target) / abs(target) for r in rs],
+                    "energy_rel_err": [max(abs(e - e0) / abs(e0) for e, e0 in zip(r["energies"], ref["energies"]))
+                                       for r in rs],
                     "is_saddle": [r["is_saddle"] for r in rs], "seed_image": [r["seed_image"] for r in rs]}
         work = {1: "single-component GL 64x64 dx=0.5, 16 images", 2: WORKLOAD}[cfg]
         ttb = {"quantity": "dF = F(saddle) - F(minimum), refined stationary points; time until within 1e-6 of dF*",
