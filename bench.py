@@ -323,6 +323,17 @@ def run_ours(args):
 
     fp64 = fp64_leg(native.FP64_NATIVE)
     fp64["paired"] = fp64_leg(native.FP64_PAIRED)
+    # FP64 FLOP roofline of the IEEE-double passes: DADD + DMUL + 2 DFMA per
+    # site-image counted by ncu (profiles/fp64_passes_flops_config2.md) over the
+    # event-timed passes; no FP64 peak is measured on this machine, so the
+    # denominator is GB300's nominal FP64 rate
+    fp64_flop = {"k_grad": 480.3, "k_dir_poly": 711.4}
+    nominal_fp64_tflops = 1.25
+    fp64["flop_roofline"] = {
+        k: {"flop_per_site_image": f, "tflops": f * units_per_step / (ms_ / 1e3) / 1e12,
+            "frac_of_nominal": f * units_per_step / (ms_ / 1e3) / 1e12 / nominal_fp64_tflops}
+        for (k, f), ms_ in zip(fp64_flop.items(), (fp64["ms_grad"], fp64["ms_dir_poly"]))}
+    fp64["flop_roofline"]["peak"] = {"tflops": nominal_fp64_tflops, "source": "nominal (not measured)"}
 
     # ---- the reference's own CUDA build on this GPU ---------------------------
     # its unmodified nlcg.cu / parallel_sum.cu compiled for sm_103a (staged from
