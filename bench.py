@@ -440,20 +440,21 @@ def run_ours(args):
     ttb = None
     if rank == 0 and not args.no_ttb:
         from mepgl_gb300 import barrier as B
-        cfg, relax, reps = args.ttb_config, 10, args.ttb_repeats
-        ref = B.time_to_barrier(cfg, "fp64", relax, g_tol=1e-10)
+        cfg, relax, reps, budget = args.ttb_config, 10, args.ttb_repeats, args.ttb_string
+        ref = B.time_to_barrier(cfg, "fp64", relax, max_string=budget, g_tol=1e-10)
         target = ref["barrier"]
         runs = {"fp64": [ref], "mixed": [], "fp64_paired": []}
         for _ in range(reps):
-            runs["mixed"].append(B.time_to_barrier(cfg, "mixed", relax))
+            runs["mixed"].append(B.time_to_barrier(cfg, "mixed", relax, max_string=budget))
             if len(runs["fp64"]) < reps:
-                runs["fp64"].append(B.time_to_barrier(cfg, "fp64", relax))
-        runs["fp64_paired"].append(B.time_to_barrier(cfg, "fp64_paired", relax))
+                runs["fp64"].append(B.time_to_barrier(cfg, "fp64", relax, max_string=budget))
+        runs["fp64_paired"].append(B.time_to_barrier(cfg, "fp64_paired", relax, max_string=budget))
 
         def leg(rs, rtol):
             ts = [B.time_within([x[0] for x in r["trace"]], [x[1] for x in r["trace"]], target, rtol) for r in rs]
             return {"times_s": ts, "median_s": statistics.median(ts) if all(t is not None for t in ts) else None,
                     "string_s": [r["string_s"] for r in rs], "string_iterations": [r["string_iterations"] for r in rs],
+                    "refine_s": [r["total_s"] - r["string_s"] for r in rs],
                     "newton": [r["newton"] for r in rs], "total_s": [r["total_s"] for r in rs],
                     "barrier_rel_err": [abs(r["barrier"] - target) / abs(target) for r in rs],
                     "energy_rel_err": [max(abs(e - e0) / abs(e0) for e, e0 in zip(r["energies"], ref["energies"]))
@@ -461,7 +462,7 @@ def run_ours(args):
                     "is_saddle": [r["is_saddle"] for r in rs], "seed_image": [r["seed_image"] for r in rs]}
         work = {1: "single-component GL 64x64 dx=0.5, 16 images", 2: WORKLOAD}[cfg]
         ttb = {"quantity": "dF = F(saddle) - F(minimum), refined stationary points; time until within 1e-6 of dF*",
-               "workload": work, "relax_steps": relax, "target_dF": target,
+               "workload": work, "relax_steps": relax, "string_budget_iterations": budget, "target_dF": target,
                "target_g_norms": ref["g_norms"], "target_min_curvature": ref["min_curvature"],
                "fp64": leg(runs["fp64"], 1e-6), "mixed": leg(runs["mixed"], 1e-6),
                "fp64_paired_string": leg(runs["fp64_paired"], 1e-6),
@@ -505,6 +506,8 @@ def main(argv=None):
     ap.add_argument("--ttb-config", type=int, choices=(1, 2), default=2,
                     help="workload of that leg: 2 (the 256x256 mixed-precision string) or 1 (64x64, seconds)")
     ap.add_argument("--ttb-repeats", type=int, default=3, help="runs per schedule of the time-to-barrier leg")
+    ap.add_argument("--ttb-string", type=int, default=300,
+                    help="string-phase budget (outer iterations of 10 NLCG steps) of the time-to-barrier leg")
     args = ap.parse_args(argv)
     if args.impl == "reference":
         return run_reference(args)

@@ -51,7 +51,6 @@ namespace mepgl {
 constexpr int RF_MAX_LZ = 32;       // Lanczos vectors
 constexpr int RF_MAX_DEG = 16;      // gauge polynomial degree
 constexpr int RF_MAX_GB = (RF_MAX_DEG + 1) * (RF_MAX_DEG + 2) / 2 - 1;   // 152 basis functions
-constexpr int RF_GB_CHUNK = 16;     // basis functions per block of the gauge-dot kernel
 constexpr int RF_DOTS = 40;         // per-image dot results kept per launch
 constexpr int RF_NB = 256;          // blocks per image of the vector kernels (upper bound)
 
@@ -110,11 +109,16 @@ struct RefineWork {
     uint64_t state_version = ~0ull;   // the context's state version after the last refinement call
     // gauge Hessians are built from many perturbed copies of the images at
     // once: an internal FP64 context holding `wide_images` of them as one
-    // string (chunks of the 2m F perturbations), its gauge partials and sums
+    // string (chunks of the 2m F perturbations), and their orbit gradients
     mepgl_ctx *wide = nullptr;
-    int wide_images = 0, wide_nb = 16;
-    double *wide_part = nullptr, *wide_gd = nullptr;
+    int wide_images = 0;
+    double *wide_gd = nullptr;
     size_t wide_gd_cap = 0;
+    // Legendre tables of the separable orbit gradients and their row sums
+    double *gtab = nullptr;
+    int gtab_deg = -1;
+    double *rows = nullptr;
+    size_t rows_cap = 0;
 };
 
 void refine_free(RefineWork *w)
@@ -129,8 +133,9 @@ void refine_free(RefineWork *w)
     cudaFree(w->coef);
     cudaFree(w->gcoef);
     cudaFree(w->gd);
-    cudaFree(w->wide_part);
     cudaFree(w->wide_gd);
+    cudaFree(w->gtab);
+    cudaFree(w->rows);
     if (w->wide) mepgl_destroy(w->wide);
     delete w;
 }
@@ -455,66 +460,76 @@ __global__ void __launch_bounds__(NT) k_gauge_perturb(Vec in, Vec out, GaugeBasi
     }
 }
 
-// Partials of dE/dc_m = g . J phi_m = sum_s g_A . grad phi_m + sum_a q_a phi_m (Re psi_a g_Im,a - Im psi_a g_Re,a),
-// for the basis functions [16 z, 16 z + 16) of block row z.
-__global__ void __launch_bounds__(NT) k_gauge_dots(Vec x, Vec g, GaugeBasis B, int nx, int ny, int ncomp, double q1,
-                                                   double q2, double idx, double *part, int nb)
+// Separable orbit gradients.  With phi_m = P_a(X_i) P_b(Y_j),
+//   dE/dc_m = sum_j [ Py_j,b Sx_j,a + DPy_j,b Sy_j,a + Py_j,b Sw_j,a ],
+//   Sx_j,a = sum_i gAx DPx_i,a,  Sy_j,a = sum_i gAy Px_i,a,  Sw_j,a = sum_i w Px_i,a,
+// w = sum_c q_c (Re psi_c g_Im,c - Im psi_c g_Re,c); P / DP are the Legendre
+// values and their lattice differences (central, one-sided at the edge, times
+// 1/dx) per column / row, tabulated once.  Per site this is 3 (deg + 1)
+// multiply-adds instead of the polynomial recurrences for every function.
+struct GaugeTables {
+    const double *px, *dpx, *py, *dpy;   // [nx][deg+1], [ny][deg+1]
+};
+
+constexpr int RS_THREADS = 128;
+
+// Row sums: block (j, n) -> rows[(n ny + j) 3 (deg+1) + {x, y, w} (deg+1) + a].
+template <int D1>
+__global__ void __launch_bounds__(RS_THREADS) k_gauge_rows(Vec x, Vec g, GaugeTables T, int nx, int ny, int ncomp,
+                                                           double q1, double q2, double *rows)
 {
-    __shared__ double sh[NT / 32];
-    const int n = blockIdx.y, m0 = blockIdx.z * RF_GB_CHUNK;
-    const int mc = min(RF_GB_CHUNK, B.m - m0);
-    const long M = (long)nx * ny, per = (M + nb - 1) / nb;
-    const long s0 = blockIdx.x * per, s1 = min(M, s0 + per);
-    double acc[RF_GB_CHUNK];
+    __shared__ double sh[RS_THREADS / 32][3 * D1];
+    const int j = blockIdx.x, n = blockIdx.y;
+    const long M = (long)nx * ny;
+    double sx[D1], sy[D1], sw[D1];
 #pragma unroll
-    for (int m = 0; m < RF_GB_CHUNK; ++m) acc[m] = 0.0;
-    for (long s = s0 + threadIdx.x; s < s1; s += NT) {
-        const int i = (int)(s % nx), j = (int)(s / nx);
-        const long o = 2 * ((long)n * M + s);
+    for (int a = 0; a < D1; ++a) sx[a] = sy[a] = sw[a] = 0.0;
+    for (int i = threadIdx.x; i < nx; i += RS_THREADS) {
+        const long o = 2 * ((long)n * M + (long)j * nx + i);
         const double gax = g.p[0][o], gay = g.p[0][o + 1];
         double w = 0.0;
-        for (int a = 0; a < ncomp; ++a)
-            w += (a ? q2 : q1) * (x.p[1 + a][o] * g.p[1 + a][o + 1] - x.p[1 + a][o + 1] * g.p[1 + a][o]);
-        double Px[3][RF_MAX_DEG + 1], Py[3][RF_MAX_DEG + 1];
-        const int il = i > 0 ? i - 1 : i, ir = i < nx - 1 ? i + 1 : i;
-        const int jd = j > 0 ? j - 1 : j, ju = j < ny - 1 ? j + 1 : j;
-        legendre(coord(i, nx), B.deg, Px[0]);
-        legendre(coord(il, nx), B.deg, Px[1]);
-        legendre(coord(ir, nx), B.deg, Px[2]);
-        legendre(coord(j, ny), B.deg, Py[0]);
-        legendre(coord(jd, ny), B.deg, Py[1]);
-        legendre(coord(ju, ny), B.deg, Py[2]);
-        const double sx = idx / (ir - il), sy = idx / (ju - jd);
+        for (int c = 0; c < ncomp; ++c)
+            w += (c ? q2 : q1) * (x.p[1 + c][o] * g.p[1 + c][o + 1] - x.p[1 + c][o + 1] * g.p[1 + c][o]);
+        const double *px = T.px + (long)i * D1, *dpx = T.dpx + (long)i * D1;
 #pragma unroll
-        for (int m = 0; m < RF_GB_CHUNK; ++m) {
-            if (m < mc) {
-                const int pa = B.a[m0 + m], pb = B.b[m0 + m];
-                const double phi = Px[0][pa] * Py[0][pb];
-                const double dxp = (Px[2][pa] - Px[1][pa]) * Py[0][pb] * sx;
-                const double dyp = Px[0][pa] * (Py[2][pb] - Py[1][pb]) * sy;
-                acc[m] += gax * dxp + gay * dyp + w * phi;
-            }
+        for (int a = 0; a < D1; ++a) {
+            const double p = px[a];
+            sx[a] += gax * dpx[a];
+            sy[a] += gay * p;
+            sw[a] += w * p;
         }
     }
+    const int wi = threadIdx.x >> 5, l = threadIdx.x & 31;
 #pragma unroll
-    for (int m = 0; m < RF_GB_CHUNK; ++m) {
-        if (m < mc) {
-            const double t = block_reduce(acc[m], sh);
-            if (threadIdx.x == 0) part[((long)n * B.m + m0 + m) * nb + blockIdx.x] = t;
+    for (int a = 0; a < D1; ++a) {
+        double v[3] = {sx[a], sy[a], sw[a]};
+#pragma unroll
+        for (int t = 0; t < 3; ++t) {
+            for (int o = 16; o > 0; o >>= 1) v[t] += __shfl_down_sync(0xffffffffu, v[t], o);
+            if (l == 0) sh[wi][t * D1 + a] = v[t];
         }
+    }
+    __syncthreads();
+    for (int t = threadIdx.x; t < 3 * D1; t += RS_THREADS) {
+        double v = 0.0;
+        for (int k = 0; k < RS_THREADS / 32; ++k) v += sh[k][t];
+        rows[((long)n * ny + j) * 3 * D1 + t] = v;
     }
 }
 
-// Sums of gauge partials into gd[n][slot * m + k].
-__global__ void __launch_bounds__(NT) k_gauge_sums(const double *part, int m, int nb, double *gd, int gstride, int slot)
+// Combination over rows: block n, thread m -> gd[n gstride + slot m_total + m].
+__global__ void __launch_bounds__(NT) k_gauge_combine(const double *rows, GaugeBasis B, GaugeTables T, int ny,
+                                                      double *gd, int gstride, int slot)
 {
-    __shared__ double sh[NT / 32];
-    const int n = blockIdx.x;
-    for (int k = 0; k < m; ++k) {
+    const int n = blockIdx.x, D1 = B.deg + 1;
+    for (int m = threadIdx.x; m < B.m; m += NT) {
+        const int a = B.a[m], b = B.b[m];
         double v = 0.0;
-        for (int b = threadIdx.x; b < nb; b += NT) v += part[((long)n * m + k) * nb + b];
-        const double t = block_reduce(v, sh);
-        if (threadIdx.x == 0) gd[(long)n * gstride + slot * m + k] = t;
+        for (int j = 0; j < ny; ++j) {
+            const double *r = rows + ((long)n * ny + j) * 3 * D1;
+            v += T.py[(long)j * D1 + b] * (r[a] + r[2 * D1 + a]) + T.dpy[(long)j * D1 + b] * r[D1 + a];
+        }
+        gd[(long)n * gstride + slot * B.m + m] = v;
     }
 }
 
@@ -728,6 +743,81 @@ mepgl_status hess_vec(Ctx &R, const Vec &u, const Vec &y, bool with_mu)
     return MEPGL_OK;
 }
 
+// Legendre tables of the lattice (see k_gauge_rows), uploaded once per degree.
+mepgl_status gauge_tables(Ctx &R, const GaugeBasis &B, GaugeTables &T)
+{
+    RefineWork *w = R.w;
+    const StringHost &s = R.c->strings[0];
+    const int D1 = B.deg + 1, nx = s.nx, ny = s.ny;
+    if (w->gtab_deg != B.deg) {
+        std::vector<double> t((size_t)2 * (nx + ny) * D1);
+        auto fill = [&](int n, double *p, double *dp) {
+            auto leg = [&](int i, double *P) {
+                const double x = n > 1 ? (2.0 * i - (n - 1)) / (n - 1) : 0.0;
+                P[0] = 1.0;
+                if (B.deg >= 1) P[1] = x;
+                for (int k = 1; k < B.deg; ++k) P[k + 1] = ((2 * k + 1) * x * P[k] - k * P[k - 1]) / (k + 1);
+            };
+            std::vector<double> Pl(D1), Pr(D1);
+            for (int i = 0; i < n; ++i) {
+                leg(i, p + (size_t)i * D1);
+                const int il = i > 0 ? i - 1 : i, ir = i < n - 1 ? i + 1 : i;
+                leg(il, Pl.data());
+                leg(ir, Pr.data());
+                for (int a = 0; a < D1; ++a) dp[(size_t)i * D1 + a] = (Pr[a] - Pl[a]) / (s.dx * (ir - il));
+            }
+        };
+        double *px = t.data(), *dpx = px + (size_t)nx * D1, *py = dpx + (size_t)nx * D1, *dpy = py + (size_t)ny * D1;
+        fill(nx, px, dpx);
+        fill(ny, py, dpy);
+        cudaFree(w->gtab);
+        w->gtab = nullptr;
+        RK(cudaMalloc(&w->gtab, t.size() * sizeof(double)));
+        RK(cudaMemcpy(w->gtab, t.data(), t.size() * sizeof(double), cudaMemcpyHostToDevice));
+        w->gtab_deg = B.deg;
+    }
+    T.px = w->gtab;
+    T.dpx = T.px + (size_t)nx * D1;
+    T.py = T.dpx + (size_t)nx * D1;
+    T.dpy = T.py + (size_t)ny * D1;
+    return MEPGL_OK;
+}
+
+// Orbit gradients g . J phi_m of n_img images of (x, g) into
+// gd[n gstride + slot m_total + m].
+mepgl_status orbit_gradients(Ctx &R, const GaugeBasis &B, Vec x, Vec g, int n_img, double *gd, int gstride, int slot)
+{
+    RefineWork *w = R.w;
+    const StringHost &s = R.c->strings[0];
+    const int D1 = B.deg + 1;
+    GaugeTables T;
+    mepgl_status st = gauge_tables(R, B, T);
+    if (st != MEPGL_OK) return st;
+    const size_t need = (size_t)n_img * s.ny * 3 * D1;
+    if (w->rows_cap < need) {
+        cudaFree(w->rows);
+        w->rows = nullptr;
+        RK(cudaMalloc(&w->rows, need * sizeof(double)));
+        w->rows_cap = need;
+    }
+    const dim3 grid(s.ny, n_img);
+    const int nc = R.c->ncomp;
+    const double q1 = s.q[0], q2 = s.q[1];
+    switch (D1) {
+#define ROWS_CASE(d)                                                                                \
+    case d: k_gauge_rows<d><<<grid, RS_THREADS, 0, R.st>>>(x, g, T, s.nx, s.ny, nc, q1, q2, w->rows); break;
+        ROWS_CASE(2) ROWS_CASE(3) ROWS_CASE(4) ROWS_CASE(5) ROWS_CASE(6) ROWS_CASE(7) ROWS_CASE(8) ROWS_CASE(9)
+        ROWS_CASE(10) ROWS_CASE(11) ROWS_CASE(12) ROWS_CASE(13) ROWS_CASE(14) ROWS_CASE(15) ROWS_CASE(16)
+        ROWS_CASE(17)
+#undef ROWS_CASE
+    default: return ctx_fail(R.c, MEPGL_ERR_INVALID_ARG, "refine: gauge degree out of range");
+    }
+    k_gauge_combine<<<n_img, NT, 0, R.st>>>(w->rows, B, T, s.ny, gd, gstride, slot);
+    R.c->launches += 2;
+    RK(cudaGetLastError());
+    return MEPGL_OK;
+}
+
 // Orbit gradients g . J phi_k at the 2 m F perturbed states U(+-h phi_i) x_n,
 // into out[((n m + i) 2 + sign) m + k].  The perturbed states are images of
 // an internal context (chunks of at most 2^25 sites in all), so each
@@ -769,9 +859,6 @@ mepgl_status wide_gauge_gradients(Ctx &R, const GaugeBasis &B, double h, std::ve
         if (mepgl_create(&p, &o, c->stream, &w->wide) != MEPGL_OK)
             return ctx_fail(c, MEPGL_ERR_CUDA, std::string("refine: gauge workspace: ") + mepgl_last_error(nullptr));
         w->wide_images = cap;
-        cudaFree(w->wide_part);
-        w->wide_part = nullptr;
-        RK(cudaMalloc(&w->wide_part, (size_t)cap * m * w->wide_nb * sizeof(double)));
     }
     if (w->wide_gd_cap < (size_t)total * m) {
         cudaFree(w->wide_gd);
@@ -796,11 +883,9 @@ mepgl_status wide_gauge_gradients(Ctx &R, const GaugeBasis &B, double h, std::ve
         FieldPtrs fp;
         for (int f = 0; f < 3; ++f) fp.p[f] = f < w->nf ? gw.p[f] : nullptr;
         RK(launch_gradient_only(Lw, 0, fp, 0));
-        const dim3 gdg(w->wide_nb, nW, (m + RF_GB_CHUNK - 1) / RF_GB_CHUNK);
-        k_gauge_dots<<<gdg, NT, 0, R.st>>>(xw, gw, B, s.nx, s.ny, nc, q1, q2, idx, w->wide_part, w->wide_nb);
-        k_gauge_sums<<<nW, NT, 0, R.st>>>(w->wide_part, m, w->wide_nb, w->wide_gd + (size_t)w0 * m, m, 0);
-        RK(cudaGetLastError());
-        c->launches += 4;
+        mepgl_status st = orbit_gradients(R, B, xw, gw, nW, w->wide_gd + (size_t)w0 * m, m, 0);
+        if (st != MEPGL_OK) return st;
+        c->launches += 2;
         R.grads += (nW + F - 1) / F;      // in units of the refinement's own gradient launches
     }
     out.resize((size_t)total * m);
@@ -823,13 +908,8 @@ mepgl_status gauge_step(Ctx &R, const GaugeBasis &B, double h, int refresh)
     const double q1 = s.q[0], q2 = s.q[1], idx = 1.0 / s.dx;
     const int nc = R.c->ncomp, xb = R.c->xi ^ 1;
     const dim3 gg((unsigned)std::min<long>((s.M() + NT - 1) / NT, 1024), F);
-    const dim3 gdg(w->nb, F, (m + RF_GB_CHUNK - 1) / RF_GB_CHUNK);
     auto gdots = [&](Vec xx, Vec gv, int slot) -> mepgl_status {
-        k_gauge_dots<<<gdg, NT, 0, R.st>>>(xx, gv, B, s.nx, s.ny, nc, q1, q2, idx, w->part, w->nb);
-        k_gauge_sums<<<F, NT, 0, R.st>>>(w->part, m, w->nb, w->gd, gstride, slot);
-        R.c->launches += 2;
-        RK(cudaGetLastError());
-        return MEPGL_OK;
+        return orbit_gradients(R, B, xx, gv, F, w->gd, gstride, slot);
     };
     auto energies = [&](int xbuf, std::vector<double> &e) -> mepgl_status {
         RK(launch_energy(R.L, R.c->sc, xbuf, R.c->dscratch));
