@@ -397,11 +397,19 @@ typedef struct mepgl_refine_options {
     int32_t gauge_degree;      /* gauge polynomial degree <= 16, 0 = off,
                                   -1 = auto: max(nx, ny) / 8 within 4..16 (default) */
     double mu0;                /* initial Levenberg-Marquardt shift (1e-3)        */
-    double cg_eta;             /* CG relative tolerance cap (0.1)                 */
+    double cg_eta;             /* CG relative tolerance (0.1), see `forcing`      */
     int32_t max_retries;       /* rejected steps retried per iteration (8)        */
     int32_t gauge_refresh;     /* iterations a gauge-subspace Hessian is reused; 0 =
                                   auto: 1 up to 64 gauge functions, else 4 (default);
                                   kept between calls while the state is unchanged */
+    int32_t precondition;      /* 1: CG preconditioned by the cosine-basis inverse of a
+                                  constant-coefficient model of the Hessian (needs
+                                  cuFFT at run time; without it the CG runs
+                                  unpreconditioned), 0: plain CG (default 1) */
+    int32_t forcing;           /* CG tolerance per Newton step: 0 = cg_eta (default;
+                                  linear convergence at about that rate), 1 =
+                                  sqrt|g| capped at cg_eta (superlinear, tighter
+                                  solves); never tighter than g_tol needs      */
 } mepgl_refine_options;
 
 typedef struct mepgl_refine_report {
@@ -410,6 +418,7 @@ typedef struct mepgl_refine_report {
     double min_curvature;      /* saddles: the lowest Hessian eigenvalue          */
     double mu;                 /* Levenberg-Marquardt shift reached               */
     int32_t newton_iterations, cg_iterations, gradient_evaluations, converged;
+    int32_t preconditioned;    /* the CG of this call was preconditioned          */
 } mepgl_refine_report;
 
 void mepgl_default_refine_options(mepgl_refine_options *opt);

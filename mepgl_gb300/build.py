@@ -82,7 +82,7 @@ def build(force: bool = False, verbose: bool = False, ptxas_info: bool = False) 
                 sys.stdout.write(out)
     if jobs or _stale(LIB, objs):
         tmp = LIB + f".{os.getpid()}.tmp"
-        _run([nvcc()] + ARCH + ["-shared", "-o", tmp] + objs)
+        _run([nvcc()] + ARCH + ["-shared", "-o", tmp] + objs + ["-ldl"])
         os.replace(tmp, LIB)
     cli_src = os.path.join(CSRC, "cli.cpp")
     npy_src = os.path.join(CSRC, "npy.cpp")

@@ -28,6 +28,16 @@
 //    gradients.  Minima use plain shifted CG.  Hessian-vector products are
 //    central differences of the gradient kernel, H u = (g(x + h u) -
 //    g(x - h u)) / 2h, with |h u| = 1e-6 sqrt(dof).
+//  * Preconditioner.  The CG runs preconditioned by the inverse of a
+//    constant-coefficient model of the Hessian, one per field component and
+//    image: M = sigma - c_x d_xx - c_y d_yy (5-point differences, Neumann
+//    boundary), with c_x, c_y and the mass sigma averaged from Hessian
+//    columns probed at a comb of bulk sites, applied on the degrees of freedom
+//    the energy depends on (mask from one Hessian probe).  M^-1 is exact in
+//    the cosine basis: the masked field is mirrored to a 2 nx x 2 ny lattice,
+//    transformed by cuFFT (loaded at run time), divided by the model's
+//    eigenvalues and transformed back.  It removes the stiff kinetic part of
+//    the spectrum (about 3x fewer CG iterations on the 64x64 string).
 //  * Globalisation.  The step is kept when it lowers |g|^2 (for an index-1
 //    saddle the modified force -g + 2 (g.v_1) v_1 is a descent direction of
 //    |g|^2); then mu /= 4, else mu *= 4 and the solve is repeated
@@ -44,6 +54,8 @@
 #include <cstring>
 #include <vector>
 
+#include <dlfcn.h>
+
 #include "context.h"
 
 namespace mepgl {
@@ -57,7 +69,44 @@ constexpr int RF_NB = 256;          // blocks per image of the vector kernels (u
 // per-image device scalars (sc[n * NSC + k])
 enum { S_ACTIVE, S_RR, S_R0, S_ETA, S_ALPHA, S_BETA, S_H, S_INV2H, S_MU, S_V1Y, S_G1, S_P1, S_DELTA, S_IT, S_NEG,
        S_ACCEPT, S_INVB, S_ONE, NSC };
-enum { OP_NONE, OP_FDSTEP, OP_STORE_V1Y, OP_ALPHA, OP_BETA, OP_CGINIT, OP_STORE_G1, OP_UNIT };
+enum { OP_NONE, OP_FDSTEP, OP_STORE_V1Y, OP_ALPHA, OP_BETA, OP_CGINIT, OP_STORE_G1, OP_UNIT, OP_PCGINIT, OP_PBETA };
+
+// cuFFT, resolved at run time (the preconditioner is optional: without the
+// library the CG runs unpreconditioned).  Handles are ints; the two
+// transform types and the success code are cuFFT's public enum values.
+using fft_handle = int;
+constexpr int FFT_R2C = 0x2a, FFT_C2R = 0x2c, FFT_SUCCESS = 0;
+
+struct FftApi {
+    bool tried = false, ok = false;
+    int (*plan_many)(fft_handle *, int, int *, int *, int, int, int *, int, int, int, int) = nullptr;
+    int (*exec_r2c)(fft_handle, float *, float2 *) = nullptr;
+    int (*exec_c2r)(fft_handle, float2 *, float *) = nullptr;
+    int (*set_stream)(fft_handle, cudaStream_t) = nullptr;
+    int (*destroy)(fft_handle) = nullptr;
+};
+
+FftApi &fft_api()
+{
+    static FftApi api;
+    if (api.tried) return api;
+    api.tried = true;
+    std::vector<std::string> names = {"libcufft.so.12", "libcufft.so"};
+    for (const char *env : {"CUDA_HOME", "CUDA_PATH"})
+        if (const char *h = std::getenv(env)) names.push_back(std::string(h) + "/lib64/libcufft.so.12");
+    names.push_back("/usr/local/cuda/lib64/libcufft.so.12");
+    void *lib = nullptr;
+    for (const auto &n : names)
+        if ((lib = dlopen(n.c_str(), RTLD_NOW | RTLD_LOCAL))) break;
+    if (!lib) return api;
+    api.plan_many = (decltype(api.plan_many))dlsym(lib, "cufftPlanMany");
+    api.exec_r2c = (decltype(api.exec_r2c))dlsym(lib, "cufftExecR2C");
+    api.exec_c2r = (decltype(api.exec_c2r))dlsym(lib, "cufftExecC2R");
+    api.set_stream = (decltype(api.set_stream))dlsym(lib, "cufftSetStream");
+    api.destroy = (decltype(api.destroy))dlsym(lib, "cufftDestroy");
+    api.ok = api.plan_many && api.exec_r2c && api.exec_c2r && api.set_stream && api.destroy;
+    return api;
+}
 
 // One vector of the context's shape: nf arrays of F*M (x, y) / (Re, Im) double pairs.
 struct Vec {
@@ -88,7 +137,7 @@ struct RefineWork {
     int nb = 1;                       // blocks per image in the vector kernels
     double *block = nullptr;          // all workspace vectors
     size_t vs = 0;                    // doubles per vector
-    Vec g, v1, p, r, y, s, gp, gm;
+    Vec g, v1, p, r, y, s, gp, gm, z[2], pmask;   // z: this and the previous preconditioned residual
     Vec lz[RF_MAX_LZ + 1];
     double *part = nullptr;           // partial sums [F][K][nb]
     double *dots = nullptr;           // [F][RF_DOTS]
@@ -99,8 +148,24 @@ struct RefineWork {
     std::vector<double> lam1, mu;
     std::vector<int> has_mode;        // a saddle image has a direction to start its Lanczos from
     std::vector<int> fresh;           // that direction is the caller's (longer first Lanczos)
-    cudaGraphExec_t cg_graph[2] = {nullptr, nullptr};   // CG iterations, per current x buffer
-    int64_t graph_launches = 0, graph_grads = 0;        // kernels and gradients per replay
+    // CG iterations, per preconditioning (off / on) and current x buffer
+    cudaGraphExec_t cg_graph[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};
+    int64_t graph_launches[2] = {0, 0}, graph_grads[2] = {0, 0};   // kernels and gradients per replay
+    bool pc_capture_failed = false;   // the preconditioned iterations then run without a graph
+    // preconditioner: planes (n, f, c) mirrored to 2 ny x 2 nx, their spectra
+    // (FP32: a preconditioner needs no more, and GB300's FP64 rate would make
+    // the transforms cost more than a Hessian product), the model
+    // (sigma, c_x, c_y) per plane and the eigenvalue factors 2 - 2 cos(pi k / n)
+    // of the two directions
+    int planes = 0;
+    float *pc_ext = nullptr;
+    float2 *pc_spec = nullptr;
+    double *pc_coef = nullptr;
+    double *pc_eig = nullptr;          // [nx + 1] x-factors, then [2 ny] y-factors
+    double *pc_probe = nullptr;        // comb gathers
+    size_t pc_probe_cap = 0;
+    fft_handle fft_fwd = 0, fft_inv = 0;
+    bool fft_plans = false;
     // gauge-subspace Hessians kept between Newton iterations (and calls on
     // the same state): per image m x m, its age in iterations
     std::vector<std::vector<double>> gauge_h;
@@ -124,8 +189,18 @@ struct RefineWork {
 void refine_free(RefineWork *w)
 {
     if (!w) return;
-    for (auto &g : w->cg_graph)
-        if (g) cudaGraphExecDestroy(g);
+    for (auto &row : w->cg_graph)
+        for (auto &g : row)
+            if (g) cudaGraphExecDestroy(g);
+    if (w->fft_plans) {
+        fft_api().destroy(w->fft_fwd);
+        fft_api().destroy(w->fft_inv);
+    }
+    cudaFree(w->pc_ext);
+    cudaFree(w->pc_spec);
+    cudaFree(w->pc_coef);
+    cudaFree(w->pc_eig);
+    cudaFree(w->pc_probe);
     cudaFree(w->block);
     cudaFree(w->part);
     cudaFree(w->dots);
@@ -360,6 +435,23 @@ __global__ void __launch_bounds__(NT) k_dot_sums(const double *part, int K, int 
     case OP_UNIT:     // s[0] = |w|^2: 1/|w| for normalisation
         q[S_INVB] = s[0] > 0 ? 1.0 / sqrt(s[0]) : 0.0;
         break;
+    case OP_PCGINIT:  // s[0] = r_0 . z_0, s[1] = |r_0|^2 (z = M^-1 r)
+        q[S_RR] = s[0];
+        q[S_R0] = sqrt(s[1]);
+        q[S_IT] = 0.0;
+        q[S_NEG] = 0.0;
+        if (!(s[1] > 0) || !(s[0] > 0)) q[S_ACTIVE] = 0.0;
+        break;
+    case OP_PBETA:    // s[0] = r_new . z_new, s[1] = |r_new|^2, s[2] = r_new . z_old
+        if (act) {
+            q[S_BETA] = q[S_RR] > 0 ? (s[0] - s[2]) / q[S_RR] : 0.0;
+            q[S_RR] = s[0];
+            q[S_IT] += 1.0;
+            if (!(sqrt(s[1]) > q[S_ETA] * q[S_R0]) || !(s[0] > 0)) q[S_ACTIVE] = 0.0;
+        } else {
+            q[S_BETA] = 0.0;
+        }
+        break;
     default: break;
     }
 }
@@ -432,34 +524,6 @@ __global__ void __launch_bounds__(NT) k_gauge_apply(Vec in, Vec out, GaugeBasis 
     }
 }
 
-// Wide copies for the gauge Hessian: image b of `out` is perturbation
-// w = w0 + b of the 2 m F perturbations, U(+-h phi_i) applied to image n of
-// `in`, w = (n m + i) 2 + sign.
-__global__ void __launch_bounds__(NT) k_gauge_perturb(Vec in, Vec out, GaugeBasis B, int F, int w0, int n_out,
-                                                      double h, int nx, int ny, int ncomp, double q1, double q2,
-                                                      double idx)
-{
-    const int b = blockIdx.y, w = w0 + b;
-    if (b >= n_out || w >= 2 * B.m * F) return;
-    const int n = w / (2 * B.m), r = w % (2 * B.m), i = r >> 1;
-    const double mult = (r & 1) ? -h : h;
-    const long M = (long)nx * ny;
-    for (long s = blockIdx.x * (long)NT + threadIdx.x; s < M; s += (long)gridDim.x * NT) {
-        const int ii = (int)(s % nx), jj = (int)(s / nx);
-        const GaugeField G = gauge_field(B, nullptr, i, ii, jj, nx, ny, idx);
-        const long o = 2 * ((long)n * M + s), ob = 2 * ((long)b * M + s);
-        out.p[0][ob] = in.p[0][o] + mult * G.gx;
-        out.p[0][ob + 1] = in.p[0][o + 1] + mult * G.gy;
-        for (int a = 0; a < ncomp; ++a) {
-            double sn, cs;
-            sincos((a ? q2 : q1) * mult * G.chi, &sn, &cs);
-            const double re = in.p[1 + a][o], im = in.p[1 + a][o + 1];
-            out.p[1 + a][ob] = re * cs - im * sn;
-            out.p[1 + a][ob + 1] = re * sn + im * cs;
-        }
-    }
-}
-
 // Separable orbit gradients.  With phi_m = P_a(X_i) P_b(Y_j),
 //   dE/dc_m = sum_j [ Py_j,b Sx_j,a + DPy_j,b Sy_j,a + Py_j,b Sw_j,a ],
 //   Sx_j,a = sum_i gAx DPx_i,a,  Sy_j,a = sum_i gAy Px_i,a,  Sw_j,a = sum_i w Px_i,a,
@@ -470,6 +534,40 @@ __global__ void __launch_bounds__(NT) k_gauge_perturb(Vec in, Vec out, GaugeBasi
 struct GaugeTables {
     const double *px, *dpx, *py, *dpy;   // [nx][deg+1], [ny][deg+1]
 };
+
+// Wide copies for the gauge Hessian: image b of `out` is perturbation
+// w = w0 + b of the 2 m F perturbations, U(+-h phi_k) applied to image n of
+// `in`, w = (n m + k) 2 + sign, with phi_k = P_a(X_i) P_b(Y_j) and its lattice
+// gradient read from the Legendre tables.  Grid (row blocks, n_out).
+__global__ void __launch_bounds__(NT) k_gauge_perturb(Vec in, Vec out, GaugeBasis B, GaugeTables T, int F, int w0,
+                                                      int n_out, double h, int nx, int ny, int ncomp, double q1,
+                                                      double q2)
+{
+    const int b = blockIdx.y, w = w0 + b;
+    if (b >= n_out || w >= 2 * B.m * F) return;
+    const int n = w / (2 * B.m), r = w % (2 * B.m), k = r >> 1;
+    const double mult = (r & 1) ? -h : h;
+    const int D1 = B.deg + 1, ea = B.a[k], eb = B.b[k];
+    const long M = (long)nx * ny;
+    for (int j = blockIdx.x; j < ny; j += gridDim.x) {
+        const double py = T.py[(long)j * D1 + eb], dpy = T.dpy[(long)j * D1 + eb];
+        for (int i = threadIdx.x; i < nx; i += NT) {
+            const double px = T.px[(long)i * D1 + ea], dpx = T.dpx[(long)i * D1 + ea];
+            const double chi = px * py;
+            const long s = (long)j * nx + i;
+            const long o = 2 * ((long)n * M + s), ob = 2 * ((long)b * M + s);
+            out.p[0][ob] = in.p[0][o] + mult * (dpx * py);
+            out.p[0][ob + 1] = in.p[0][o + 1] + mult * (px * dpy);
+            for (int a = 0; a < ncomp; ++a) {
+                double sn, cs;
+                sincos((a ? q2 : q1) * mult * chi, &sn, &cs);
+                const double re = in.p[1 + a][o], im = in.p[1 + a][o + 1];
+                out.p[1 + a][ob] = re * cs - im * sn;
+                out.p[1 + a][ob + 1] = re * sn + im * cs;
+            }
+        }
+    }
+}
 
 constexpr int RS_THREADS = 128;
 
@@ -531,6 +629,121 @@ __global__ void __launch_bounds__(NT) k_gauge_combine(const double *rows, GaugeB
         }
         gd[(long)n * gstride + slot * B.m + m] = v;
     }
+}
+
+// ------------------------------------------------------ preconditioner kernels
+__device__ __forceinline__ const double *field_ptr(const Vec &v, int f)
+{
+    return f == 0 ? v.p[0] : (f == 1 ? v.p[1] : v.p[2]);
+}
+
+__device__ __forceinline__ double *field_ptr_w(const Vec &v, int f)
+{
+    return f == 0 ? v.p[0] : (f == 1 ? v.p[1] : v.p[2]);
+}
+
+// Mirror the masked field (n, f) = blockIdx.z to its two planes (Re / x, Im / y)
+// of 2 ny x 2 nx: plane row J < ny is lattice row J, row J >= ny is row
+// 2 ny - 1 - J (columns alike).  Grid (ceil(2 nx / NT), 2 ny, F nf).
+__global__ void __launch_bounds__(NT) k_pc_extend(Vec r, Vec mask, float *ext, int nx, int ny, int nf)
+{
+    const int I = blockIdx.x * NT + threadIdx.x, J = blockIdx.y, nfz = blockIdx.z;
+    const int W = 2 * nx;
+    if (I >= W) return;
+    const int n = nfz / nf, f = nfz % nf;
+    const int i = I < nx ? I : W - 1 - I, j = J < ny ? J : 2 * ny - 1 - J;
+    const long o = 2 * ((long)n * nx * ny + (long)j * nx + i);
+    const double2 v = *reinterpret_cast<const double2 *>(field_ptr(r, f) + o);
+    const double2 m = *reinterpret_cast<const double2 *>(field_ptr(mask, f) + o);
+    const long E = 4L * nx * ny, e = (long)J * W + I;
+    ext[(2L * nfz) * E + e] = (float)(v.x * m.x);
+    ext[(2L * nfz + 1) * E + e] = (float)(v.y * m.y);
+}
+
+// Spectrum of plane q = blockIdx.z (2 ny rows of nx + 1 frequencies) divided by
+// the model's eigenvalue sigma + c_x ex[kx] + c_y ey[ky], and by the 4 nx ny of
+// the unnormalised transform pair.
+__global__ void __launch_bounds__(NT) k_pc_scale(float2 *spec, const double *coef, const double *eig, int nx, int ny)
+{
+    const int kx = blockIdx.x * NT + threadIdx.x, ky = blockIdx.y, q = blockIdx.z;
+    if (kx > nx) return;
+    const double sg = coef[3 * q], cx = coef[3 * q + 1], cy = coef[3 * q + 2];
+    const double lam = (sg + cx * eig[kx] + cy * eig[nx + 1 + ky]) * (4.0 * nx * ny);
+    const long o = (long)q * 2 * ny * (nx + 1) + (long)ky * (nx + 1) + kx;
+    const float il = (float)(1.0 / lam);
+    float2 v = spec[o];
+    v.x *= il;
+    v.y *= il;
+    spec[o] = v;
+}
+
+// z = mask * (top-left ny x nx block of the two planes).  Grid (ceil(nx / NT), ny, F nf).
+__global__ void __launch_bounds__(NT) k_pc_extract(const float *ext, Vec z, Vec mask, int nx, int ny, int nf)
+{
+    const int i = blockIdx.x * NT + threadIdx.x, j = blockIdx.y, nfz = blockIdx.z;
+    if (i >= nx) return;
+    const int n = nfz / nf, f = nfz % nf;
+    const long o = 2 * ((long)n * nx * ny + (long)j * nx + i);
+    const long E = 4L * nx * ny, e = (long)j * 2 * nx + i;
+    const double2 m = *reinterpret_cast<const double2 *>(field_ptr(mask, f) + o);
+    *reinterpret_cast<double2 *>(field_ptr_w(z, f) + o) =
+        make_double2((double)ext[(2L * nfz) * E + e] * m.x, (double)ext[(2L * nfz + 1) * E + e] * m.y);
+}
+
+// A probe vector with entries in [0.5, 1.5) from a hash of the index.
+__global__ void __launch_bounds__(NT) k_pc_hash(Vec u, long n_per_field, int nf)
+{
+    for (long k = blockIdx.x * (long)NT + threadIdx.x; k < n_per_field; k += (long)gridDim.x * NT) {
+        for (int f = 0; f < nf; ++f) {
+            uint64_t h = (uint64_t)k * 0x9E3779B97F4A7C15ull + (uint64_t)(f + 1) * 0xD1B54A32D192ED03ull;
+            h ^= h >> 31;
+            h *= 0xBF58476D1CE4E5B9ull;
+            h ^= h >> 29;
+            field_ptr_w(u, f)[k] = 0.5 + (double)(h >> 11) * (1.0 / 9007199254740992.0);
+        }
+    }
+}
+
+// mask = 1 where (H u) != 0 (the energy depends on that degree of freedom), else 0.
+__global__ void __launch_bounds__(NT) k_pc_mask(Vec y, Vec mask, long n_per_field, int nf)
+{
+    for (long k = blockIdx.x * (long)NT + threadIdx.x; k < n_per_field; k += (long)gridDim.x * NT)
+        for (int f = 0; f < nf; ++f) field_ptr_w(mask, f)[k] = field_ptr(y, f)[k] != 0.0 ? 1.0 : 0.0;
+}
+
+// Comb of probe sites: site k = (2 + (k % kx) sp, 2 + (k / kx) sp).
+struct Comb {
+    int kx, ky, sp;
+};
+
+// u: 1 at the comb sites of component c of field f in every image (u zero elsewhere).
+__global__ void __launch_bounds__(NT) k_pc_comb(Vec u, Comb cb, int f, int c, int nx, int ny)
+{
+    const int k = blockIdx.x * NT + threadIdx.x, n = blockIdx.y;
+    if (k >= cb.kx * cb.ky) return;
+    const int i = 2 + (k % cb.kx) * cb.sp, j = 2 + (k / cb.kx) * cb.sp;
+    field_ptr_w(u, f)[2 * ((long)n * nx * ny + (long)j * nx + i) + c] = 1.0;
+}
+
+// Column of H at each comb site: out[(n K + k) 6 + t] = diagonal, +x, -x, +y,
+// -y neighbours (same component), and 1 when all five are live dofs.
+__global__ void __launch_bounds__(NT) k_pc_gather(Vec y, Vec mask, Comb cb, int f, int c, int nx, int ny, double *out)
+{
+    const int k = blockIdx.x * NT + threadIdx.x, n = blockIdx.y;
+    const int K = cb.kx * cb.ky;
+    if (k >= K) return;
+    const int i = 2 + (k % cb.kx) * cb.sp, j = 2 + (k / cb.kx) * cb.sp;
+    const double *yp = field_ptr(y, f), *mp = field_ptr(mask, f);
+    const long base = (long)n * nx * ny;
+    const long s[5] = {(long)j * nx + i, (long)j * nx + i + 1, (long)j * nx + i - 1, (long)(j + 1) * nx + i,
+                       (long)(j - 1) * nx + i};
+    double live = 1.0;
+    double *o = out + ((long)n * K + k) * 6;
+    for (int t = 0; t < 5; ++t) {
+        o[t] = yp[2 * (base + s[t]) + c];
+        live *= mp[2 * (base + s[t]) + c];
+    }
+    o[5] = live;
 }
 
 // ------------------------------------------------------------ host helpers
@@ -743,6 +956,172 @@ mepgl_status hess_vec(Ctx &R, const Vec &u, const Vec &y, bool with_mu)
     return MEPGL_OK;
 }
 
+// ------------------------------------------------------------ preconditioner
+// Buffers and cuFFT plans (kept with the workspace); false when cuFFT is
+// unavailable or the plans cannot be made.
+bool pc_alloc(Ctx &R)
+{
+    RefineWork *w = R.w;
+    if (w->fft_plans) return true;
+    FftApi &api = fft_api();
+    if (!api.ok) return false;
+    const int nx = w->nx, ny = w->ny;
+    w->planes = R.F * w->nf * 2;
+    const size_t E = 4ull * nx * ny, S = 2ull * ny * (nx + 1);
+    cudaError_t e = cudaMalloc(&w->pc_ext, w->planes * E * sizeof(float));
+    if (e == cudaSuccess) e = cudaMalloc(&w->pc_spec, w->planes * S * sizeof(float2));
+    if (e == cudaSuccess) e = cudaMalloc(&w->pc_coef, w->planes * 3 * sizeof(double));
+    if (e == cudaSuccess) e = cudaMalloc(&w->pc_eig, (nx + 1 + 2 * ny) * sizeof(double));
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    std::vector<double> eig(nx + 1 + 2 * ny);
+    const double pi = 3.14159265358979323846;
+    for (int k = 0; k <= nx; ++k) eig[k] = 2.0 - 2.0 * std::cos(pi * k / nx);
+    for (int k = 0; k < 2 * ny; ++k) eig[nx + 1 + k] = 2.0 - 2.0 * std::cos(pi * k / ny);
+    if (cudaMemcpy(w->pc_eig, eig.data(), eig.size() * sizeof(double), cudaMemcpyHostToDevice) != cudaSuccess)
+        return false;
+    int dims[2] = {2 * ny, 2 * nx};
+    if (api.plan_many(&w->fft_fwd, 2, dims, nullptr, 1, 0, nullptr, 1, 0, FFT_R2C, w->planes) != FFT_SUCCESS)
+        return false;
+    if (api.plan_many(&w->fft_inv, 2, dims, nullptr, 1, 0, nullptr, 1, 0, FFT_C2R, w->planes) != FFT_SUCCESS) {
+        api.destroy(w->fft_fwd);
+        return false;
+    }
+    w->fft_plans = true;
+    return true;
+}
+
+// z = P M^-1 r (P: projection off v1; the images' planes all transformed).
+mepgl_status pc_apply(Ctx &R, const Vec &r, const Vec &z)
+{
+    RefineWork *w = R.w;
+    FftApi &api = fft_api();
+    const int nx = w->nx, ny = w->ny;
+    k_pc_extend<<<dim3((2 * nx + NT - 1) / NT, 2 * ny, R.F * w->nf), NT, 0, R.st>>>(r, w->pmask, w->pc_ext, nx, ny,
+                                                                                 w->nf);
+    RK(cudaGetLastError());
+    if (api.set_stream(w->fft_fwd, R.st) != FFT_SUCCESS || api.exec_r2c(w->fft_fwd, w->pc_ext, w->pc_spec) != FFT_SUCCESS)
+        return ctx_fail(R.c, MEPGL_ERR_CUDA, "refine: preconditioner forward transform failed");
+    k_pc_scale<<<dim3((nx + 1 + NT - 1) / NT, 2 * ny, w->planes), NT, 0, R.st>>>(w->pc_spec, w->pc_coef, w->pc_eig,
+                                                                              nx, ny);
+    RK(cudaGetLastError());
+    if (api.set_stream(w->fft_inv, R.st) != FFT_SUCCESS || api.exec_c2r(w->fft_inv, w->pc_spec, w->pc_ext) != FFT_SUCCESS)
+        return ctx_fail(R.c, MEPGL_ERR_CUDA, "refine: preconditioner inverse transform failed");
+    k_pc_extract<<<dim3((nx + NT - 1) / NT, ny, R.F * w->nf), NT, 0, R.st>>>(w->pc_ext, z, w->pmask, nx, ny, w->nf);
+    R.c->launches += 3;
+    RK(cudaGetLastError());
+    RK(R.dots({{w->v1, z}}, OP_STORE_V1Y));
+    LinArgs a = lin_args(z, S_ACTIVE);
+    add_term(a, z, 1.0);
+    add_term(a, w->v1, -1.0, S_V1Y);
+    RK(R.lin(a));
+    return MEPGL_OK;
+}
+
+// The model of each image's planes at the current x: the live-dof mask from
+// one probe H u (u positive, hashed), then per field component a comb probe
+// whose Hessian columns give c_x, c_y and the mass averaged over live bulk
+// sites.  Images with S_ACTIVE == 0 keep M = I.  Returns false (no
+// preconditioning) when the lattice has no comb site.
+mepgl_status pc_setup(Ctx &R, bool &usable)
+{
+    RefineWork *w = R.w;
+    usable = false;
+    const int nx = w->nx, ny = w->ny, F = R.F, nf = w->nf;
+    if (nx < 5 || ny < 5) return MEPGL_OK;
+    if (!pc_alloc(R)) return MEPGL_OK;
+    const long nper = (long)F * 2 * w->M;
+    const int grid = (int)std::min<long>((nper + NT - 1) / NT, 4096);
+    // 1. mask
+    k_pc_hash<<<grid, NT, 0, R.st>>>(w->p, nper, nf);
+    R.c->launches += 1;
+    RK(cudaGetLastError());
+    mepgl_status st = hess_vec(R, w->p, w->y, false);
+    if (st != MEPGL_OK) return st;
+    k_pc_mask<<<grid, NT, 0, R.st>>>(w->y, w->pmask, nper, nf);
+    R.c->launches += 1;
+    RK(cudaGetLastError());
+    // 2. comb probes: about 1024 sites, spacing >= 4 (the Hessian couples sites
+    // at most 2 apart, so the probed columns do not overlap where they are read)
+    Comb cb;
+    cb.sp = std::max(4, (int)std::ceil(std::sqrt((double)(nx - 4) * (ny - 4) / 1024.0)));
+    cb.kx = (nx - 5) / cb.sp + 1;
+    cb.ky = (ny - 5) / cb.sp + 1;
+    const int K = cb.kx * cb.ky;
+    const size_t need = (size_t)2 * nf * F * K * 6;
+    if (w->pc_probe_cap < need) {
+        cudaFree(w->pc_probe);
+        w->pc_probe = nullptr;
+        w->pc_probe_cap = 0;
+        RK(cudaMalloc(&w->pc_probe, need * sizeof(double)));
+        w->pc_probe_cap = need;
+    }
+    for (int f = 0; f < nf; ++f)
+        for (int c = 0; c < 2; ++c) {
+            for (int ff = 0; ff < nf; ++ff) RK(cudaMemsetAsync(w->p.p[ff], 0, nper * sizeof(double), R.st));
+            k_pc_comb<<<dim3((K + NT - 1) / NT, F), NT, 0, R.st>>>(w->p, cb, f, c, nx, ny);
+            R.c->launches += 1;
+            RK(cudaGetLastError());
+            st = hess_vec(R, w->p, w->y, false);
+            if (st != MEPGL_OK) return st;
+            k_pc_gather<<<dim3((K + NT - 1) / NT, F), NT, 0, R.st>>>(w->y, w->pmask, cb, f, c, nx, ny,
+                                                                  w->pc_probe + (size_t)(f * 2 + c) * F * K * 6);
+            R.c->launches += 1;
+            RK(cudaGetLastError());
+        }
+    std::vector<double> h(need);
+    RK(cudaMemcpyAsync(h.data(), w->pc_probe, need * sizeof(double), cudaMemcpyDeviceToHost, R.st));
+    RK(R.read_scalars());
+    // 3. per image and field: c_x, c_y per component, one mass for both
+    std::vector<double> coef((size_t)w->planes * 3);
+    bool any = false;
+    for (int n = 0; n < F; ++n)
+        for (int f = 0; f < nf; ++f) {
+            double cx[2] = {0, 0}, cy[2] = {0, 0}, mass = 0.0;
+            long cnt[2] = {0, 0};
+            for (int c = 0; c < 2; ++c) {
+                const double *o = h.data() + ((size_t)(f * 2 + c) * F + n) * K * 6;
+                for (int k = 0; k < K; ++k, o += 6) {
+                    if (o[5] == 0.0) continue;
+                    const double sx = -0.5 * (o[1] + o[2]), sy = -0.5 * (o[3] + o[4]);
+                    cx[c] += sx;
+                    cy[c] += sy;
+                    mass += o[0] - 2.0 * sx - 2.0 * sy;
+                    ++cnt[c];
+                }
+            }
+            const bool ok = R.S(n, S_ACTIVE) != 0.0 && cnt[0] > 0 && cnt[1] > 0;
+            mass = ok ? mass / (double)(cnt[0] + cnt[1]) : 0.0;
+            double top = 0.0;
+            for (int c = 0; c < 2; ++c) {
+                cx[c] = ok ? std::max(0.0, cx[c] / cnt[c]) : 0.0;
+                cy[c] = ok ? std::max(0.0, cy[c] / cnt[c]) : 0.0;
+                top = std::max(top, cx[c] + cy[c]);
+            }
+            const double sigma = ok ? std::max(mass, 1e-3 * top) : 1.0;
+            for (int c = 0; c < 2; ++c) {
+                double *q = coef.data() + 3 * ((size_t)(n * nf + f) * 2 + c);
+                q[0] = sigma > 0 ? sigma : 1.0;
+                q[1] = sigma > 0 ? cx[c] : 0.0;
+                q[2] = sigma > 0 ? cy[c] : 0.0;
+            }
+            any |= ok;
+        }
+    RK(cudaMemcpyAsync(w->pc_coef, coef.data(), coef.size() * sizeof(double), cudaMemcpyHostToDevice, R.st));
+    RK(cudaStreamSynchronize(R.st));
+    if (std::getenv("MEPGL_REFINE_LOG") && std::getenv("MEPGL_REFINE_LOG")[0] == '1')
+        for (int n = 0; n < F; ++n)
+            for (int f = 0; f < nf; ++f) {
+                const double *q = coef.data() + 3 * ((size_t)(n * nf + f) * 2);
+                std::fprintf(stderr, "precondition image %d field %d: sigma %.4g  c_x %.4g %.4g  c_y %.4g %.4g\n", n, f,
+                             q[0], q[1], q[4], q[2], q[5]);
+            }
+    usable = any;
+    return MEPGL_OK;
+}
+
 // Legendre tables of the lattice (see k_gauge_rows), uploaded once per degree.
 mepgl_status gauge_tables(Ctx &R, const GaugeBasis &B, GaugeTables &T)
 {
@@ -873,12 +1252,15 @@ mepgl_status wide_gauge_gradients(Ctx &R, const GaugeBasis &B, double h, std::ve
     Launch Lw = ctx_string_launch(wc, 0);
     Lw.paired = 0;
     Lw.stream = R.st;
-    const double q1 = s.q[0], q2 = s.q[1], idx = 1.0 / s.dx;
+    const double q1 = s.q[0], q2 = s.q[1];
     const int nc = c->ncomp;
+    GaugeTables T;
+    mepgl_status tst = gauge_tables(R, B, T);
+    if (tst != MEPGL_OK) return tst;
     for (int w0 = 0; w0 < total; w0 += cap) {
         const int nW = std::min(cap, total - w0);
-        const dim3 gp((unsigned)std::min<long>((M + NT - 1) / NT, 256), nW);
-        k_gauge_perturb<<<gp, NT, 0, R.st>>>(R.x(), xw, B, F, w0, nW, h, s.nx, s.ny, nc, q1, q2, idx);
+        const dim3 gp((unsigned)std::min(s.ny, 1024), nW);
+        k_gauge_perturb<<<gp, NT, 0, R.st>>>(R.x(), xw, B, T, F, w0, nW, h, s.nx, s.ny, nc, q1, q2);
         RK(cudaGetLastError());
         FieldPtrs fp;
         for (int f = 0; f < 3; ++f) fp.p[f] = f < w->nf ? gw.p[f] : nullptr;
@@ -1076,8 +1458,11 @@ mepgl_status lanczos(Ctx &R, int steps, std::vector<double> &lam)
 }
 
 // One CG iteration on the images with S_ACTIVE != 0 (device scalars only,
-// so that a run of iterations can be captured as one CUDA graph).
-mepgl_status cg_iteration(Ctx &R)
+// so that a run of iterations can be captured as one CUDA graph).  With
+// `pc` the iteration is preconditioned (z = P M^-1 r; S_RR holds r . z) and
+// beta is the flexible form r_new . (z_new - z_old) / (r_old . z_old), which
+// tolerates the FP32 rounding of M^-1; iteration k writes z[k & 1].
+mepgl_status cg_iteration(Ctx &R, bool pc, int k)
 {
     RefineWork *w = R.w;
     mepgl_status st = hess_vec(R, w->p, w->y, true);
@@ -1099,62 +1484,102 @@ mepgl_status cg_iteration(Ctx &R)
     a = lin_args(w->r, S_ACTIVE);
     add_term(a, w->r, 1.0);
     add_term(a, w->y, -1.0, S_ALPHA);
-    a.dw = w->r;
-    a.dot_k = 1;
-    a.dot_slot = 0;
-    RK(R.lin(a));
-    RK(R.sums(1, OP_BETA));
+    if (pc) {
+        RK(R.lin(a));
+        st = pc_apply(R, w->r, w->z[k & 1]);
+        if (st != MEPGL_OK) return st;
+        RK(R.dots({{w->r, w->z[k & 1]}, {w->r, w->r}, {w->r, w->z[(k & 1) ^ 1]}}, OP_PBETA));
+    } else {
+        a.dw = w->r;
+        a.dot_k = 1;
+        a.dot_slot = 0;
+        RK(R.lin(a));
+        RK(R.sums(1, OP_BETA));
+    }
     a = lin_args(w->p, S_ACTIVE);
-    add_term(a, w->r, 1.0);
+    add_term(a, pc ? w->z[k & 1] : w->r, 1.0);
     add_term(a, w->p, 1.0, S_BETA);
     RK(R.lin(a));
     return MEPGL_OK;
 }
 
 constexpr int CG_GRAPH_ITERS = 8;     // CG iterations per graph replay
+static_assert(CG_GRAPH_ITERS % 2 == 0, "the preconditioned iterations alternate two z buffers");
 
 // Projected shifted CG for the images with S_ACTIVE != 0 at entry:
-// (H + mu) s = -(g - g1 v1), s orthogonal to v1 (v1 = 0 for minima).
-// The iterations run as replays of a captured graph of CG_GRAPH_ITERS
-// iterations (images that converge inside a replay stop updating).
-mepgl_status cg_solve(Ctx &R, int max_it)
+// (H + mu) s = -(g - g1 v1), s orthogonal to v1 (v1 = 0 for minima),
+// preconditioned when `pc`.  The iterations run as replays of a captured
+// graph of CG_GRAPH_ITERS iterations (images that converge inside a replay
+// stop updating); if the preconditioned iterations cannot be captured they
+// are launched directly, the same kernels in the same order.
+mepgl_status cg_solve(Ctx &R, int max_it, bool pc)
 {
     RefineWork *w = R.w;
     LinArgs a = lin_args(w->r, S_ACTIVE);
     add_term(a, w->g, -1.0);
     add_term(a, w->v1, 1.0, S_G1);
-    a.dw = w->r;   // |r|^2
-    a.dot_k = 1;
-    a.dot_slot = 0;
-    RK(R.lin(a));
-    RK(R.sums(1, OP_CGINIT));
+    if (pc) {
+        RK(R.lin(a));
+        mepgl_status st = pc_apply(R, w->r, w->z[1]);   // the "previous" z of iteration 0
+        if (st != MEPGL_OK) return st;
+        RK(R.dots({{w->r, w->z[1]}, {w->r, w->r}}, OP_PCGINIT));
+    } else {
+        a.dw = w->r;   // |r|^2
+        a.dot_k = 1;
+        a.dot_slot = 0;
+        RK(R.lin(a));
+        RK(R.sums(1, OP_CGINIT));
+    }
     a = lin_args(w->p, S_ACTIVE);
-    add_term(a, w->r, 1.0);
+    add_term(a, pc ? w->z[1] : w->r, 1.0);
     RK(R.lin(a));
     a = lin_args(w->s, S_ACTIVE);
     add_term(a, w->s, 0.0);
     RK(R.lin(a));
-    cudaGraphExec_t &ex = w->cg_graph[R.c->xi & 1];
-    const int64_t l0 = R.c->launches, g0 = R.grads;
-    if (!ex) {
+    const int gi = pc ? 1 : 0;
+    cudaGraphExec_t &ex = w->cg_graph[gi][R.c->xi & 1];
+    const bool direct = pc && w->pc_capture_failed;
+    if (!ex && !direct) {
+        const int64_t l0 = R.c->launches, g0 = R.grads;
         RK(cudaStreamBeginCapture(R.st, cudaStreamCaptureModeThreadLocal));
         mepgl_status st = MEPGL_OK;
-        for (int k = 0; k < CG_GRAPH_ITERS && st == MEPGL_OK; ++k) st = cg_iteration(R);
+        for (int k = 0; k < CG_GRAPH_ITERS && st == MEPGL_OK; ++k) st = cg_iteration(R, pc, k);
         cudaGraph_t g = nullptr;
         const cudaError_t e = cudaStreamEndCapture(R.st, &g);
-        if (st != MEPGL_OK) return st;
-        RK(e);
-        RK(cudaGraphInstantiate(&ex, g, 0));
-        cudaGraphDestroy(g);
-        w->graph_launches = R.c->launches - l0;
-        w->graph_grads = R.grads - g0;
+        cudaGraphExec_t made = nullptr;
+        cudaError_t ei = e;
+        if (st == MEPGL_OK && e == cudaSuccess) ei = cudaGraphInstantiate(&made, g, 0);
+        if (g) cudaGraphDestroy(g);
         R.c->launches = l0;
         R.grads = g0;
+        if (st != MEPGL_OK || e != cudaSuccess || ei != cudaSuccess) {
+            if (!pc) {
+                if (st != MEPGL_OK) return st;
+                RK(e);
+                RK(ei);
+            }
+            // the transforms did not capture: clear the error state, launch directly
+            cudaGetLastError();
+            R.c->err.clear();
+            w->pc_capture_failed = true;
+        } else {
+            ex = made;
+            w->graph_launches[gi] = R.c->launches - l0;
+            w->graph_grads[gi] = R.grads - g0;
+        }
     }
+    if (!ex && !w->pc_capture_failed) return ctx_fail(R.c, MEPGL_ERR_CUDA, "refine: CG graph missing");
     for (int it = 0; it < max_it; it += CG_GRAPH_ITERS) {
-        RK(cudaGraphLaunch(ex, R.st));
-        R.c->launches += w->graph_launches;
-        R.grads += w->graph_grads;
+        if (ex) {
+            RK(cudaGraphLaunch(ex, R.st));
+            R.c->launches += w->graph_launches[gi];
+            R.grads += w->graph_grads[gi];
+        } else {
+            for (int k = 0; k < CG_GRAPH_ITERS; ++k) {
+                mepgl_status st = cg_iteration(R, pc, k);
+                if (st != MEPGL_OK) return st;
+            }
+        }
         if ((it / CG_GRAPH_ITERS) % 2 == 1 || it + CG_GRAPH_ITERS >= max_it) {
             RK(R.read_scalars());
             bool any = false;
@@ -1180,7 +1605,7 @@ mepgl_status alloc_work(mepgl_ctx *c)
     // about four 16-byte pairs per thread and array
     w->nb = (int)std::max<long>(1, std::min<long>(RF_NB, (2 * w->M + 8L * NT - 1) / (8L * NT)));
     w->vs = (size_t)w->nf * w->F * 2 * w->M;
-    const int nvec = 8 + RF_MAX_LZ + 1;
+    const int nvec = 11 + RF_MAX_LZ + 1;
     cudaError_t e = cudaMalloc(&w->block, nvec * w->vs * sizeof(double));
     if (e == cudaSuccess) e = cudaMemsetAsync(w->block, 0, nvec * w->vs * sizeof(double), c->stream);
     if (e != cudaSuccess) return ctx_fail(c, MEPGL_ERR_CUDA, std::string("refine workspace: ") + cudaGetErrorString(e));
@@ -1193,7 +1618,8 @@ mepgl_status alloc_work(mepgl_ctx *c)
     // lz vectors first and contiguous (the multi-dot kernels index them by stride)
     for (int k = 0; k <= RF_MAX_LZ; ++k) w->lz[k] = vec(k);
     int k = RF_MAX_LZ + 1;
-    for (Vec *v : {&w->g, &w->v1, &w->p, &w->r, &w->y, &w->s, &w->gp, &w->gm}) *v = vec(k++);
+    for (Vec *v : {&w->g, &w->v1, &w->p, &w->r, &w->y, &w->s, &w->gp, &w->gm, &w->z[0], &w->z[1], &w->pmask})
+        *v = vec(k++);
     const size_t parts = (size_t)w->F * std::max(RF_DOTS, RF_MAX_GB) * w->nb;
     e = cudaMalloc(&w->part, parts * sizeof(double));
     if (e == cudaSuccess) e = cudaMalloc(&w->dots, (size_t)w->F * RF_DOTS * sizeof(double));
@@ -1233,6 +1659,8 @@ void mepgl_default_refine_options(mepgl_refine_options *o)
     o->cg_eta = 0.1;
     o->max_retries = 8;
     o->gauge_refresh = 0;
+    o->precondition = 1;
+    o->forcing = 0;
 }
 
 mepgl_status mepgl_refine_stationary(mepgl_ctx *c, const int32_t *kind, const void *mode_a, const void *mode_psi_1,
@@ -1251,7 +1679,8 @@ mepgl_status mepgl_refine_stationary(mepgl_ctx *c, const int32_t *kind, const vo
     if (opt_in) opt = *opt_in;
     if (opt.lanczos_steps < 2 || opt.lanczos_steps > RF_MAX_LZ || opt.gauge_degree < -1 ||
         opt.gauge_degree > RF_MAX_DEG || opt.max_newton < 0 || opt.max_cg < 1 || !(opt.g_tol >= 0) ||
-        !(opt.mu0 > 0) || !(opt.cg_eta > 0 && opt.cg_eta < 1) || opt.max_retries < 0 || opt.gauge_refresh < 0)
+        !(opt.mu0 > 0) || !(opt.cg_eta > 0 && opt.cg_eta < 1) || opt.max_retries < 0 || opt.gauge_refresh < 0 ||
+        opt.precondition < 0 || opt.precondition > 1 || opt.forcing < 0 || opt.forcing > 1)
         return ctx_fail(c, MEPGL_ERR_INVALID_ARG, "mepgl_refine_stationary: option out of range");
     const int F = c->strings[0].F;
     for (int n = 0; n < F; ++n)
@@ -1341,6 +1770,21 @@ mepgl_status mepgl_refine_stationary(mepgl_ctx *c, const int32_t *kind, const vo
     };
     st = measure();
     if (st != MEPGL_OK) return st;
+    // preconditioner model at the starting point (images still to refine)
+    bool pc = false;
+    if (opt.precondition) {
+        std::vector<int> todo(F);
+        bool any = false;
+        for (int n = 0; n < F; ++n) {
+            todo[n] = !done[n] && gnorm[n] > opt.g_tol;
+            any |= todo[n] != 0;
+        }
+        if (any && opt.max_newton > 0) {
+            st = set_active(todo);
+            if (st == MEPGL_OK) st = pc_setup(R, pc);
+            if (st != MEPGL_OK) return st;
+        }
+    }
     // MEPGL_REFINE_LOG=1: one line per image and Newton iteration on stderr
     const char *env = std::getenv("MEPGL_REFINE_LOG");
     const bool log = env && env[0] == '1';
@@ -1419,14 +1863,18 @@ mepgl_status mepgl_refine_stationary(mepgl_ctx *c, const int32_t *kind, const vo
             st = set_active(pending);
             if (st != MEPGL_OK) return st;
             RK(R.read_scalars());
-            // forcing term: sqrt|g| (superlinear), but no tighter than the target needs
+            // forcing term: cg_eta (linear convergence at about that rate per
+            // Newton step), or sqrt|g| capped at cg_eta (superlinear, tighter
+            // solves); never tighter than reaching g_tol needs
             for (int n = 0; n < F; ++n) {
                 const double gn = std::sqrt(g2[n]);
-                R.S(n, S_ETA) = std::min(opt.cg_eta, std::max(std::sqrt(gn), gn > 0 ? 0.5 * opt.g_tol / gn : 0.0));
+                const double need = gn > 0 ? 0.5 * opt.g_tol / gn : 0.0;
+                R.S(n, S_ETA) = opt.forcing == 1 ? std::min(opt.cg_eta, std::max(std::sqrt(gn), need))
+                                                 : std::min(0.5, std::max(opt.cg_eta, need));
             }
             RK(R.write_scalars());
             const auto tc0 = std::chrono::steady_clock::now();
-            st = cg_solve(R, opt.max_cg);
+            st = cg_solve(R, opt.max_cg, pc);
             if (st != MEPGL_OK) return st;
             RK(R.read_scalars());
             cg_seconds += std::chrono::duration<double>(std::chrono::steady_clock::now() - tc0).count();
@@ -1477,12 +1925,13 @@ mepgl_status mepgl_refine_stationary(mepgl_ctx *c, const int32_t *kind, const vo
                     std::fprintf(stderr,
                                  "refine image %d (%s): |g| %.3e -> %.3e  E %.13f  mu %.2e  tries %d  cg %d  "
                                  "lambda1 %.5f  grads %lld  newton-step %.3f s of which CG %.3f s  gauge %.3f s  "
-                                 "lanczos %.3f s  cg-negative %d\n",
+                                 "lanczos %.3f s  cg-negative %d  pc %d%s\n",
                                  n, kind[n] == MEPGL_STATIONARY_SADDLE ? "saddle" : "minimum", std::sqrt(g2[n]),
                                  gnorm[n], energy[n], w->mu[n], tries_used[n], cg_it[n] - cg_before[n], w->lam1[n],
                                  (long long)R.grads,
                                  std::chrono::duration<double>(std::chrono::steady_clock::now() - tn0).count(),
-                                 cg_seconds, t_gauge, t_lanczos, neg_hits[n]);
+                                 cg_seconds, t_gauge, t_lanczos, neg_hits[n], pc ? 1 : 0,
+                                 pc && w->pc_capture_failed ? " (direct launches)" : "");
     }
     w->state_version = c->state_version;
     if (report)
@@ -1496,6 +1945,7 @@ mepgl_status mepgl_refine_stationary(mepgl_ctx *c, const int32_t *kind, const vo
             r.cg_iterations = cg_it[n];
             r.gradient_evaluations = (int32_t)std::min<int64_t>(R.grads, INT32_MAX);
             r.converged = kind[n] == MEPGL_STATIONARY_SKIP || gnorm[n] <= opt.g_tol;
+            r.preconditioned = pc ? 1 : 0;
         }
     return ctx_check_device_status(c);
 }

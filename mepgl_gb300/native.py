@@ -64,13 +64,14 @@ class MepglVortex(C.Structure):
 class MepglRefineOptions(C.Structure):
     _fields_ = [("g_tol", C.c_double), ("max_newton", C.c_int32), ("max_cg", C.c_int32),
                 ("lanczos_steps", C.c_int32), ("gauge_degree", C.c_int32), ("mu0", C.c_double),
-                ("cg_eta", C.c_double), ("max_retries", C.c_int32), ("gauge_refresh", C.c_int32)]
+                ("cg_eta", C.c_double), ("max_retries", C.c_int32), ("gauge_refresh", C.c_int32),
+                ("precondition", C.c_int32), ("forcing", C.c_int32)]
 
 
 class MepglRefineReport(C.Structure):
     _fields_ = [("energy", C.c_double), ("g_norm", C.c_double), ("min_curvature", C.c_double), ("mu", C.c_double),
                 ("newton_iterations", C.c_int32), ("cg_iterations", C.c_int32),
-                ("gradient_evaluations", C.c_int32), ("converged", C.c_int32)]
+                ("gradient_evaluations", C.c_int32), ("converged", C.c_int32), ("preconditioned", C.c_int32)]
 
 
 STATIONARY_MINIMUM, STATIONARY_SADDLE, STATIONARY_SKIP = 0, 1, 2

@@ -38,6 +38,7 @@ class BarrierResult:
     trace: list = field(default_factory=list)   # (seconds, barrier, |g| min, |g| saddle) per Newton iteration
     state: StringState | None = None     # refined [minimum, saddle] fields
     dbarrier_dH: float | None = None     # envelope theorem: dF/dH(saddle) - dF/dH(minimum)
+    cg_iterations: tuple = (0, 0)        # CG iterations over all calls (minimum, saddle)
 
     @property
     def converged(self) -> bool:
@@ -89,15 +90,18 @@ def refine_barrier(prob, state: StringState, fenergy, g_tol: float = 1e-8, max_n
         reps = ctx.refine_stationary(kinds, mode, max_newton=0, g_tol=g_tol, **options)
         trace = [(time.perf_counter() - t0, reps[1]["energy"] - reps[0]["energy"], reps[0]["g_norm"],
                   reps[1]["g_norm"])]
+        cg = [0, 0]
         for _ in range(max_newton):
             if all(r["converged"] for r in reps):
                 break
             reps = ctx.refine_stationary(kinds, None, max_newton=1, g_tol=g_tol, **options)
+            cg = [c + r["cg_iterations"] for c, r in zip(cg, reps)]
             trace.append((time.perf_counter() - t0, reps[1]["energy"] - reps[0]["energy"], reps[0]["g_norm"],
                           reps[1]["g_norm"]))
         res = BarrierResult(barrier=reps[1]["energy"] - reps[0]["energy"],
                             energies=(reps[0]["energy"], reps[1]["energy"]), seed_image=k,
-                            string_barrier=float(fe.max() - fe[0]), reports=reps, trace=trace)
+                            string_barrier=float(fe.max() - fe[0]), reports=reps, trace=trace,
+                            cg_iterations=tuple(cg))
         if adjoint:
             adj = ctx.param_adjoint()
             res.dbarrier_dH = float(adj[1, 0] - adj[0, 0])

@@ -13,7 +13,10 @@ index-1 saddle.  Checks:
   an oracle-side Lanczos (exactly one negative curvature);
 * dF/dH by the envelope theorem at the refined points against a central
   difference of the re-converged barrier at H +- h;
-* minima of a two-component string against the oracle refiner.
+* minima of a two-component string against the oracle refiner;
+* the preconditioned and the plain conjugate gradients (and the two forcing
+  terms) reach the same stationary points, the preconditioned one in fewer
+  CG iterations.
 """
 import json
 import os
@@ -121,6 +124,22 @@ def test_minima_of_a_two_component_string_match_the_oracle_refiner(native):
         np.testing.assert_allclose(rep[k]["energy"], ref["energy"], rtol=ENERGY_RTOL)
 
 
+def test_preconditioned_and_plain_cg_reach_the_same_stationary_points(config1_barrier):
+    from mepgl_gb300 import saddle
+    prob, st, fe, r = config1_barrier
+    runs = {}
+    for pc, forcing in ((1, 0), (0, 0), (1, 1)):
+        runs[pc, forcing] = saddle.refine_barrier(prob, st, fe, g_tol=1e-9, max_newton=40, adjoint=False,
+                                                  precondition=pc, forcing=forcing)
+    for key, q in runs.items():
+        assert q.converged and q.is_saddle, (key, q.reports)
+        assert all(rep["preconditioned"] == key[0] for rep in q.reports), (key, q.reports)
+        np.testing.assert_allclose(q.barrier, r.barrier, rtol=1e-10)
+        np.testing.assert_allclose(q.energies, r.energies, rtol=1e-12)
+    cg = {k: sum(q.cg_iterations) for k, q in runs.items()}
+    assert cg[1, 0] < cg[0, 0], cg
+
+
 def test_refinement_arguments_are_checked(native):
     prob, st = W.config1(n=16, images=3)
     with native.StringContext(prob, 3, "fp32") as c:
@@ -136,6 +155,10 @@ def test_refinement_arguments_are_checked(native):
         with pytest.raises(native.MepglError) as e:
             c.refine_stationary([0, 7, 0])
         assert e.value.status == 1
+        for bad in (dict(precondition=2), dict(forcing=-1)):
+            with pytest.raises(native.MepglError) as e:
+                c.refine_stationary([0, 0, 0], **bad)
+            assert e.value.status == 1
         rep = c.refine_stationary([2, 2, 2])   # all skipped: nothing changes
         assert all(x["converged"] for x in rep)
         np.testing.assert_array_equal(c.get_state().psi_1, st.psi_1)
