@@ -429,9 +429,9 @@ def run_ours(args):
     # ---- time to barrier, plain FP64 against FP32 + FP64 ----------------------
     # One run (mepgl_gb300.barrier.time_to_barrier): a string phase in the
     # schedule's precision (mode L, linear reparametrization + `relax` NLCG
-    # steps, until the string's maximum image and estimate plateau), then the
-    # IEEE FP64 refinement of image 0 to its minimum and of that image to the
-    # index-1 saddle.  dF* = F(saddle) - F(minimum) of a first FP64 run
+    # steps, a fixed budget of outer iterations), then the IEEE FP64
+    # refinement of image 0 to its minimum and of the string's energy maximum
+    # to the index-1 saddle (preconditioned CG, forcing term 0.1).  dF* = F(saddle) - F(minimum) of a first FP64 run
     # refined to |g| <= 1e-10 (measured here, not hard-coded); each run's time
     # to barrier is when its trace (the string's estimate, then the refined
     # barrier) enters and stays within 1e-6 of dF*.  Schedules: "fp64" IEEE
@@ -463,6 +463,8 @@ def run_ours(args):
         work = {1: "single-component GL 64x64 dx=0.5, 16 images", 2: WORKLOAD}[cfg]
         ttb = {"quantity": "dF = F(saddle) - F(minimum), refined stationary points; time until within 1e-6 of dF*",
                "workload": work, "relax_steps": relax, "string_budget_iterations": budget, "target_dF": target,
+               "refinement": "IEEE FP64 Newton with gauge-subspace steps; CG preconditioned by the cosine-basis "
+                             "inverse of a constant-coefficient Hessian model, relative tolerance 0.1 per step",
                "target_g_norms": ref["g_norms"], "target_min_curvature": ref["min_curvature"],
                "fp64": leg(runs["fp64"], 1e-6), "mixed": leg(runs["mixed"], 1e-6),
                "fp64_paired_string": leg(runs["fp64_paired"], 1e-6),

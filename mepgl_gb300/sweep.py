@@ -16,8 +16,10 @@ energy maximum are refined to a minimum and an index-1 saddle in IEEE FP64
 (mepgl_gb300.saddle), once from the mixed schedule's string and once from the
 same string relaxed in FP64 throughout (B + P iterations); the barrier error
 of the mixed schedule is the relative difference of the two refined
-barriers.  Strings whose energy profile has no interior saddle near the seed
-are reported as such.
+barriers.  Each row carries both refinements' final |g| (minimum, saddle)
+and Newton counts: a barrier difference means something only where both
+converged.  Strings whose energy profile has no interior saddle near the
+seed are reported as such.
 
     python -m mepgl_gb300.sweep [--strings 64] [--steps 20] [--warmup 3] [--bulk 50]
                                 [--polish 5] [--refine 8]
@@ -125,6 +127,9 @@ def main(argv=None):
                            string_barrier_mixed=r_mixed.string_barrier, string_barrier_fp64=r_64.string_barrier,
                            saddle=bool(r_mixed.is_saddle and r_64.is_saddle),
                            converged=bool(r_mixed.converged and r_64.converged),
+                           g_mixed=[x["g_norm"] for x in r_mixed.reports],
+                           g_fp64=[x["g_norm"] for x in r_64.reports],
+                           newton=[len(r_mixed.trace) - 1, len(r_64.trace) - 1],
                            refine_s=r_mixed.trace[-1][0])
                 if row["saddle"]:
                     row["rel_err"] = abs(r_mixed.barrier - r_64.barrier) / abs(r_64.barrier)
@@ -133,9 +138,12 @@ def main(argv=None):
             rows.append(row)
             print(json.dumps(row), flush=True)
         errs = [r["rel_err"] for r in rows if "rel_err" in r]
+        conv = [r["rel_err"] for r in rows if "rel_err" in r and r["converged"]]
         out["per_string_barrier"] = dict(strings=len(rows), with_saddle=len(errs),
                                          max_rel_err=max(errs) if errs else None,
-                                         median_rel_err=float(np.median(errs)) if errs else None, rows=rows)
+                                         median_rel_err=float(np.median(errs)) if errs else None,
+                                         converged=len(conv), max_rel_err_converged=max(conv) if conv else None,
+                                         rows=rows)
     print(json.dumps(out))
 
 
