@@ -1025,14 +1025,16 @@ mepgl_status pc_apply(Ctx &R, const Vec &r, const Vec &z)
 // The model of each image's planes at the current x: the live-dof mask from
 // one probe H u (u positive, hashed), then per field component a comb probe
 // whose Hessian columns give c_x, c_y and the mass averaged over live bulk
-// sites.  Images with S_ACTIVE == 0 keep M = I.  Returns false (no
-// preconditioning) when the lattice has no comb site.
+// sites.  Images with S_ACTIVE == 0 keep M = I.  `usable` is false (no
+// preconditioning) when the lattice has no comb site, is taller than the
+// transform kernels' grid allows, or cuFFT or its buffers are unavailable.
 mepgl_status pc_setup(Ctx &R, bool &usable)
 {
     RefineWork *w = R.w;
     usable = false;
     const int nx = w->nx, ny = w->ny, F = R.F, nf = w->nf;
-    if (nx < 5 || ny < 5) return MEPGL_OK;
+    // (the transform kernels put the 2 ny mirrored rows on the grid's y dimension)
+    if (nx < 5 || ny < 5 || 2L * ny > 65535) return MEPGL_OK;
     if (!pc_alloc(R)) return MEPGL_OK;
     const long nper = (long)F * 2 * w->M;
     const int grid = (int)std::min<long>((nper + NT - 1) / NT, 4096);
