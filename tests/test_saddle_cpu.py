@@ -10,6 +10,11 @@ and the committed barrier golden, without a GPU.
 * tests/golden/saddle_cfg1.json is self-consistent: the barrier is the
   difference of its energies, the saddle has exactly one negative curvature,
   and it lies above the string's own estimate.
+* The CG preconditioner's solve (mepgl_gb300/csrc/refine.cu, k_pc_extend /
+  k_pc_scale / k_pc_extract): mirroring a field to 2 ny x 2 nx, a real FFT,
+  division by sigma + c_x (2 - 2 cos(pi kx / nx)) + c_y (2 - 2 cos(pi ky / ny))
+  and the inverse FFT is the exact inverse of sigma - c_x d_xx - c_y d_yy with
+  Neumann (mirror) boundaries, on odd and even lattices.
 """
 import json
 import os
@@ -75,3 +80,29 @@ def test_saddle_golden_is_consistent():
     assert z["g_min"] <= 1e-9 and z["g_saddle"] <= 1e-9
     assert z["string_barrier"] < z["barrier"]
     assert z["dbarrier_dH"] == pytest.approx(z["dF_dH_saddle"] - z["dF_dH_min"], rel=1e-12)
+
+
+def _neumann_second_difference(n):
+    """-d_xx on n sites with mirror boundaries: tridiag(-1, 2, -1), corners 1."""
+    L = 2 * np.eye(n) - np.eye(n, k=1) - np.eye(n, k=-1)
+    L[0, 0] = L[-1, -1] = 1.0
+    return L
+
+
+@pytest.mark.parametrize("nx,ny,sigma,cx,cy", [(6, 5, 0.3, 1.0, 0.5), (7, 8, 0.05, 0.0, 1.0), (9, 9, 1.0, 2.0, 2.0)])
+def test_mirrored_fft_solve_inverts_the_neumann_model(nx, ny, sigma, cx, cy):
+    rng = np.random.default_rng(nx * 100 + ny)
+    r = rng.standard_normal((ny, nx))
+    M = sigma * np.eye(nx * ny) + cx * np.kron(np.eye(ny), _neumann_second_difference(nx)) + \
+        cy * np.kron(_neumann_second_difference(ny), np.eye(nx))
+    z_ref = np.linalg.solve(M, r.ravel()).reshape(ny, nx)
+    # the device path: mirror, R2C, divide, C2R, top-left block
+    e = np.zeros((2 * ny, 2 * nx))
+    e[:ny, :nx] = r
+    e[:ny, nx:] = r[:, ::-1]
+    e[ny:, :] = e[:ny, :][::-1, :]
+    ex = 2 - 2 * np.cos(np.pi * np.arange(nx + 1) / nx)
+    ey = 2 - 2 * np.cos(np.pi * np.arange(2 * ny) / ny)
+    spec = np.fft.rfft2(e) / (sigma + cx * ex[None, :] + cy * ey[:, None])
+    z = np.fft.irfft2(spec, s=e.shape)[:ny, :nx]
+    np.testing.assert_allclose(z, z_ref, rtol=1e-10, atol=1e-12)
