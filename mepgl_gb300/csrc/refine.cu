@@ -80,7 +80,7 @@ using fft_handle = int;
 constexpr int FFT_R2C = 0x2a, FFT_C2R = 0x2c, FFT_SUCCESS = 0;
 
 struct FftApi {
-    bool tried = false, ok = false;
+    bool ok = false;
     int (*plan_many)(fft_handle *, int, int *, int *, int, int, int *, int, int, int, int) = nullptr;
     int (*exec_r2c)(fft_handle, float *, float2 *) = nullptr;
     int (*exec_c2r)(fft_handle, float2 *, float *) = nullptr;
@@ -88,11 +88,9 @@ struct FftApi {
     int (*destroy)(fft_handle) = nullptr;
 };
 
-FftApi &fft_api()
+FftApi fft_load()
 {
-    static FftApi api;
-    if (api.tried) return api;
-    api.tried = true;
+    FftApi api;
     std::vector<std::string> names = {"libcufft.so.12", "libcufft.so"};
     for (const char *env : {"CUDA_HOME", "CUDA_PATH"})
         if (const char *h = std::getenv(env)) names.push_back(std::string(h) + "/lib64/libcufft.so.12");
@@ -107,6 +105,13 @@ FftApi &fft_api()
     api.set_stream = (decltype(api.set_stream))dlsym(lib, "cufftSetStream");
     api.destroy = (decltype(api.destroy))dlsym(lib, "cufftDestroy");
     api.ok = api.plan_many && api.exec_r2c && api.exec_c2r && api.set_stream && api.destroy;
+    return api;
+}
+
+// Loaded once per process (a function-local static: thread-safe initialisation).
+FftApi &fft_api()
+{
+    static FftApi api = fft_load();
     return api;
 }
 
