@@ -173,6 +173,7 @@ struct RefineWork {
     size_t pc_probe_cap = 0;
     fft_handle fft_fwd = 0, fft_inv = 0;
     bool fft_plans = false;
+    bool pc_failed = false;            // buffers or plans could not be made: no preconditioning
     // gauge-subspace Hessians kept between Newton iterations (and calls on
     // the same state): per image m x m, its age in iterations
     std::vector<std::vector<double>> gauge_h;
@@ -971,7 +972,8 @@ bool pc_alloc(Ctx &R)
     RefineWork *w = R.w;
     if (w->fft_plans) return true;
     FftApi &api = fft_api();
-    if (!api.ok) return false;
+    if (!api.ok || w->pc_failed) return false;
+    w->pc_failed = true;   // until the plans exist
     const int nx = w->nx, ny = w->ny;
     w->planes = R.F * w->nf * 2;
     const size_t E = 4ull * nx * ny, S = 2ull * ny * (nx + 1);
@@ -997,6 +999,7 @@ bool pc_alloc(Ctx &R)
         return false;
     }
     w->fft_plans = true;
+    w->pc_failed = false;
     return true;
 }
 
