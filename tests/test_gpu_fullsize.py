@@ -111,3 +111,25 @@ def test_config4_full_size_strings_against_the_oracle(native):
         sv.nlcg_steps(2)
         np.testing.assert_allclose(b.string_scalars(k)["fenergy"], sv.get()["fenergy"], rtol=FP32_RTOL)
     b.close()
+
+
+def test_large_string_barrier_leg_extracts_the_seed_images(native):
+    """mepgl_gb300.large's time-to-barrier leg on a small disk string: the
+    four images copied out of the FP32 device string reach the FP64
+    refinement intact (its first barrier, before any Newton step, is the FP32
+    string's F_k - F_0 re-evaluated in FP64), and the leg reports a finite
+    refinement."""
+    import argparse
+
+    import torch
+    from mepgl_gb300 import large
+    a = argparse.Namespace(n=128, images=8, barrier=4, relax=2, g_tol=1e-8, max_newton=2)
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    r = large.barrier_leg(a, stream)
+    assert 1 <= r["seed_image"] <= a.images - 2
+    assert [p for _, _, p in r["trace"]].count("string") == 1
+    first = [b for _, b, p in r["trace"] if p == "refine"][0]
+    e0 = abs(r["energies"][0])
+    assert abs(first - r["string_barrier"]) <= 1e-3 * abs(r["string_barrier"]) + 1e-5 * e0, (first, r)
+    assert r["newton"] <= a.max_newton and np.all(np.isfinite(r["g_norms"])) and np.isfinite(r["barrier"])
