@@ -38,12 +38,10 @@
 //    transformed by cuFFT (loaded at run time), divided by the model's
 //    eigenvalues and transformed back.  It removes the stiff kinetic part of
 //    the spectrum (about 3x fewer CG iterations on the 64x64 string).
-//  * Globalisation.  The merit is |g|^2 (for an index-1 saddle the modified
-//    force -g + 2 (g.v_1) v_1 is a descent direction of it).  The step is kept
-//    when |g|^2 falls by at least a tenth of the fall the linear model
-//    predicts (|r + mu s|^2 + (g.v_1 + p_1 lambda_1)^2, r the CG residual);
-//    then mu /= 4 if it fell by a quarter of that or more, else mu stays.  A
-//    rejected step sets mu *= 4 and the solve is repeated (Levenberg-Marquardt).
+//  * Globalisation.  The step is kept when it lowers |g|^2 (for an index-1
+//    saddle the modified force -g + 2 (g.v_1) v_1 is a descent direction of
+//    |g|^2); then mu /= 4, else mu *= 4 (at most 1e8) and the solve is
+//    repeated (Levenberg-Marquardt).
 //
 // Everything runs in IEEE double on the context's FP64 buffers; the CG
 // scalars live on the device, so its iterations run as replays of a captured
@@ -67,6 +65,7 @@ constexpr int RF_MAX_DEG = 16;      // gauge polynomial degree
 constexpr int RF_MAX_GB = (RF_MAX_DEG + 1) * (RF_MAX_DEG + 2) / 2 - 1;   // 152 basis functions
 constexpr int RF_DOTS = 40;         // per-image dot results kept per launch
 constexpr int RF_NB = 256;          // blocks per image of the vector kernels (upper bound)
+constexpr double RF_MU_MAX = 1e8;   // Levenberg-Marquardt shift bound
 
 // per-image device scalars (sc[n * NSC + k])
 enum { S_ACTIVE, S_RR, S_R0, S_ETA, S_ALPHA, S_BETA, S_H, S_INV2H, S_MU, S_V1Y, S_G1, S_P1, S_DELTA, S_IT, S_NEG,
@@ -1895,27 +1894,6 @@ mepgl_status mepgl_refine_stationary(mepgl_ctx *c, const int32_t *kind, const vo
                     cg_it[n] += (int)R.S(n, S_IT);
                     neg_hits[n] += R.S(n, S_NEG) != 0.0;
                 }
-            // |g|^2 the linear model predicts after the step: |P(g + H s)|^2 =
-            // |r + mu s|^2 in the complement (r the CG residual), and
-            // (g1 + p1 lambda1)^2 along v1
-            std::vector<double> pred(F, 0.0);
-            {
-                LinArgs b = lin_args(w->y);
-                add_term(b, w->r, 1.0);
-                add_term(b, w->s, 1.0, S_MU);
-                b.dw = w->y;
-                b.dot_k = 1;
-                b.dot_slot = 0;
-                RK(R.lin(b));
-                RK(R.sums(1, OP_NONE));
-                RK(cudaMemcpyAsync(hd.data(), w->dots, hd.size() * 8, cudaMemcpyDeviceToHost, R.st));
-                RK(cudaStreamSynchronize(R.st));
-                for (int n = 0; n < F; ++n) {
-                    const double along =
-                        kind[n] == MEPGL_STATIONARY_SADDLE ? R.S(n, S_G1) + R.S(n, S_P1) * w->lam1[n] : 0.0;
-                    pred[n] = hd[(size_t)n * RF_DOTS] + along * along;
-                }
-            }
             // trial x + s + p1 v1 (pending images), merit |g(trial)|^2
             for (int n = 0; n < F; ++n) R.S(n, S_ACTIVE) = pending[n] ? 1.0 : 0.0;
             RK(R.write_scalars());
@@ -1932,17 +1910,15 @@ mepgl_status mepgl_refine_stationary(mepgl_ctx *c, const int32_t *kind, const vo
             for (int n = 0; n < F; ++n) {
                 R.S(n, S_ACCEPT) = 0.0;
                 if (!pending[n]) continue;
-                // kept when |g|^2 falls by at least a tenth of the predicted
-                // fall (any fall where the model predicts none); a small step
-                // of a large shift then still counts, so mu cannot run away
                 const double gt2 = hd[(size_t)n * RF_DOTS];
-                const double dact = g2[n] - gt2, dpred = g2[n] - pred[n];
-                if (std::isfinite(gt2) && dact > 0 && (dpred <= 0 || dact >= 0.1 * dpred)) {
+                if (std::isfinite(gt2) && gt2 < g2[n] * (1 - 1e-4)) {
                     R.S(n, S_ACCEPT) = 1.0;
-                    if (dpred <= 0 || dact >= 0.25 * dpred) w->mu[n] = std::max(w->mu[n] / 4, 1e-12);
+                    w->mu[n] = std::max(w->mu[n] / 4, 1e-12);
                     pending[n] = 0;
                 } else {
-                    w->mu[n] *= 4;
+                    // bounded: from a seed where no step lowers |g|^2 (far from any
+                    // stationary point) the shift would otherwise grow without end
+                    w->mu[n] = std::min(w->mu[n] * 4, RF_MU_MAX);
                     again = true;
                 }
             }
