@@ -37,15 +37,20 @@
 //    the cosine basis: the masked field is mirrored to a 2 nx x 2 ny lattice,
 //    transformed by cuFFT (loaded at run time), divided by the model's
 //    eigenvalues and transformed back.  It removes the stiff kinetic part of
-//    the spectrum (about 3x fewer CG iterations on the 64x64 string).
+//    the spectrum (about 3x fewer CG iterations on the 64x64 string, 5x on the
+//    256x256 two-component string).  Each solve stops at a relative residual
+//    of cg_eta (0.1): linear convergence at about that rate per Newton step
+//    costs fewer CG iterations than tighter, superlinear solves.
 //  * Globalisation.  The step is kept when it lowers |g|^2 (for an index-1
 //    saddle the modified force -g + 2 (g.v_1) v_1 is a descent direction of
 //    |g|^2); then mu /= 4, else mu *= 4 (at most 1e8) and the solve is
 //    repeated (Levenberg-Marquardt).
 //
-// Everything runs in IEEE double on the context's FP64 buffers; the CG
-// scalars live on the device, so its iterations run as replays of a captured
-// CUDA graph with no host round trip inside.
+// Everything runs in IEEE double on the context's FP64 buffers, except the
+// preconditioner's transforms (FP32: they only shape the Krylov space; the
+// residuals, iterates and steps stay IEEE double).  The CG scalars live on
+// the device, so its iterations run as replays of a captured CUDA graph with
+// no host round trip inside.
 #include <algorithm>
 #include <chrono>
 #include <cmath>
