@@ -189,6 +189,10 @@ struct RefineWork {
     // string (chunks of the 2m F perturbations), and their orbit gradients
     mepgl_ctx *wide = nullptr;
     int wide_images = 0;
+    // Hessian products: an internal FP64 context of 2F images holding x + h u
+    // (images 0..F-1) and x - h u (F..2F-1), so that both gradients of the
+    // central difference run as one launch
+    mepgl_ctx *hvc = nullptr;
     double *wide_gd = nullptr;
     size_t wide_gd_cap = 0;
     // Legendre tables of the separable orbit gradients and their row sums
@@ -224,6 +228,7 @@ void refine_free(RefineWork *w)
     cudaFree(w->gtab);
     cudaFree(w->rows);
     if (w->wide) mepgl_destroy(w->wide);
+    if (w->hvc) mepgl_destroy(w->hvc);
     delete w;
 }
 
@@ -674,15 +679,17 @@ __global__ void __launch_bounds__(NT) k_pc_extend(Vec r, Vec mask, float *ext, i
 
 // Spectrum of plane q = blockIdx.z (2 ny rows of nx + 1 frequencies) divided by
 // the model's eigenvalue sigma + c_x ex[kx] + c_y ey[ky], and by the 4 nx ny of
-// the unnormalised transform pair.
+// the unnormalised transform pair.  FP32 like the spectrum (an FP64 division
+// per element made this kernel cost more than both transforms).
 __global__ void __launch_bounds__(NT) k_pc_scale(float2 *spec, const double *coef, const double *eig, int nx, int ny)
 {
     const int kx = blockIdx.x * NT + threadIdx.x, ky = blockIdx.y, q = blockIdx.z;
     if (kx > nx) return;
-    const double sg = coef[3 * q], cx = coef[3 * q + 1], cy = coef[3 * q + 2];
-    const double lam = (sg + cx * eig[kx] + cy * eig[nx + 1 + ky]) * (4.0 * nx * ny);
+    const float norm = 4.0f * (float)nx * (float)ny;
+    const float sg = (float)coef[3 * q] * norm, cx = (float)coef[3 * q + 1] * norm, cy = (float)coef[3 * q + 2] * norm;
+    const float lam = sg + cx * (float)eig[kx] + cy * (float)eig[nx + 1 + ky];
     const long o = (long)q * 2 * ny * (nx + 1) + (long)ky * (nx + 1) + kx;
-    const float il = (float)(1.0 / lam);
+    const float il = 1.0f / lam;
     float2 v = spec[o];
     v.x *= il;
     v.y *= il;
@@ -944,25 +951,77 @@ void add_term(LinArgs &a, Vec v, double mult, int s1 = -1, int s2 = -1, int cidx
             return ctx_fail(R.c, MEPGL_ERR_CUDA, std::string("refine: ") + #call + ": " + cudaGetErrorString(e_)); \
     } while (0)
 
+// An internal FP64 context with the refined context's problem and options
+// and `images` images (IEEE double arithmetic), on the same stream.
+mepgl_status twin_ctx(Ctx &R, int images, mepgl_ctx **out)
+{
+    mepgl_ctx *c = R.c;
+    const StringHost &s = c->strings[0];
+    mepgl_problem p;
+    memset(&p, 0, sizeof(p));
+    p.nx = s.nx;
+    p.ny = s.ny;
+    p.n_images = images;
+    p.multicomponent = c->ncomp == 2;
+    p.thin_film = c->thin_film;
+    p.precision = MEPGL_FP64;
+    p.dx = s.dx;
+    p.q_1 = s.q[0];
+    p.q_2 = s.q[1];
+    p.eta = s.eta;
+    p.gamma = s.gamma;
+    p.delta = s.delta;
+    const double **pp[9] = {&p.a_1, &p.b_1, &p.m_xx_1, &p.m_yy_1, &p.a_2, &p.b_2, &p.m_xx_2, &p.m_yy_2, &p.h};
+    for (int k = 0; k < 9; ++k) *pp[k] = s.params[k].empty() ? nullptr : s.params[k].data();
+    if (c->ncomp == 1)
+        for (int k = 4; k < 8; ++k) *pp[k] = nullptr;
+    p.comp_domain = s.comp.data();
+    p.sc_domain = s.sc.data();
+    mepgl_options o = c->opt;
+    o.fp64_arith = MEPGL_FP64_NATIVE;
+    if (mepgl_create(&p, &o, c->stream, out) != MEPGL_OK)
+        return ctx_fail(c, MEPGL_ERR_CUDA, std::string("refine: internal context: ") + mepgl_last_error(nullptr));
+    return MEPGL_OK;
+}
+
 // y = (H + mu) u by central differences (u's step from S_DELTA / |u|); images gated by S_ACTIVE.
+// x + h u and x - h u go to the two halves of the Hessian-product context,
+// whose gradient then runs as one launch over its 2F images.
 mepgl_status hess_vec(Ctx &R, const Vec &u, const Vec &y, bool with_mu)
 {
     RefineWork *w = R.w;
-    const int xb = R.c->xi ^ 1;
+    if (!w->hvc) return ctx_fail(R.c, MEPGL_ERR_CUDA, "refine: Hessian-product context missing");
+    const StringHost &hs = w->hvc->strings[0];
+    const size_t half = (size_t)R.F * R.M2;   // doubles of F images in one field array
+    Vec xp, xm, gp, gm;
+    for (int f = 0; f < 3; ++f) {
+        double *xb = f < w->nf ? (double *)hs.x[0][f] : nullptr;
+        double *gb = f < w->nf ? (double *)hs.g[0][f] : nullptr;
+        xp.p[f] = xb;
+        xm.p[f] = xb ? xb + half : nullptr;
+        gp.p[f] = gb;
+        gm.p[f] = gb ? gb + half : nullptr;
+    }
     RK(R.dots({{u, u}}, OP_FDSTEP));
-    LinArgs a = lin_args(R.xt());
+    LinArgs a = lin_args(xp);
     add_term(a, R.x(), 1.0);
     add_term(a, u, 1.0, S_H);
     RK(R.lin(a));
-    RK(R.grad(xb, w->gp));
-    a = lin_args(R.xt());
+    a = lin_args(xm);
     add_term(a, R.x(), 1.0);
     add_term(a, u, -1.0, S_H);
     RK(R.lin(a));
-    RK(R.grad(xb, w->gm));
+    FieldPtrs fp;
+    for (int f = 0; f < 3; ++f) fp.p[f] = gp.p[f];
+    Launch Lh = ctx_string_launch(w->hvc, 0);
+    Lh.paired = 0;
+    Lh.stream = R.st;
+    R.grads += 2;
+    R.c->launches += 1;
+    RK(launch_gradient_only(Lh, 0, fp, 0));
     a = lin_args(y);
-    add_term(a, w->gp, 1.0, S_INV2H);
-    add_term(a, w->gm, -1.0, S_INV2H);
+    add_term(a, gp, 1.0, S_INV2H);
+    add_term(a, gm, -1.0, S_INV2H);
     if (with_mu) add_term(a, u, 1.0, S_MU);
     RK(R.lin(a));
     return MEPGL_OK;
@@ -1229,30 +1288,8 @@ mepgl_status wide_gauge_gradients(Ctx &R, const GaugeBasis &B, double h, std::ve
     if (!w->wide || w->wide_images != cap) {
         if (w->wide) mepgl_destroy(w->wide);
         w->wide = nullptr;
-        mepgl_problem p;
-        memset(&p, 0, sizeof(p));
-        p.nx = s.nx;
-        p.ny = s.ny;
-        p.n_images = cap;
-        p.multicomponent = c->ncomp == 2;
-        p.thin_film = c->thin_film;
-        p.precision = MEPGL_FP64;
-        p.dx = s.dx;
-        p.q_1 = s.q[0];
-        p.q_2 = s.q[1];
-        p.eta = s.eta;
-        p.gamma = s.gamma;
-        p.delta = s.delta;
-        const double **pp[9] = {&p.a_1, &p.b_1, &p.m_xx_1, &p.m_yy_1, &p.a_2, &p.b_2, &p.m_xx_2, &p.m_yy_2, &p.h};
-        for (int k = 0; k < 9; ++k) *pp[k] = s.params[k].empty() ? nullptr : s.params[k].data();
-        if (c->ncomp == 1)
-            for (int k = 4; k < 8; ++k) *pp[k] = nullptr;
-        p.comp_domain = s.comp.data();
-        p.sc_domain = s.sc.data();
-        mepgl_options o = c->opt;
-        o.fp64_arith = MEPGL_FP64_NATIVE;
-        if (mepgl_create(&p, &o, c->stream, &w->wide) != MEPGL_OK)
-            return ctx_fail(c, MEPGL_ERR_CUDA, std::string("refine: gauge workspace: ") + mepgl_last_error(nullptr));
+        mepgl_status st = twin_ctx(R, cap, &w->wide);
+        if (st != MEPGL_OK) return st;
         w->wide_images = cap;
     }
     if (w->wide_gd_cap < (size_t)total * m) {
@@ -1716,6 +1753,10 @@ mepgl_status mepgl_refine_stationary(mepgl_ctx *c, const int32_t *kind, const vo
         for (auto &a : w->gauge_age) a = 1 << 30;
     Ctx R{c, w, ctx_string_launch(c, 0), F, 2 * w->M, c->stream};
     R.L.paired = 0;     // IEEE double gradients
+    if (!w->hvc) {      // before any capture: creating it allocates
+        st = twin_ctx(R, 2 * F, &w->hvc);
+        if (st != MEPGL_OK) return st;
+    }
     const StringHost &s = c->strings[0];
     // initial min modes: the caller's directions (then the history restarts)
     if (new_modes) {
