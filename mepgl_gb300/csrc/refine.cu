@@ -140,6 +140,7 @@ struct LinArgs {
     Vec dw;              // partial dot of out with dw (dw.p[0] == null: none)
     int dot_slot;        // K index of that partial
     int dot_k;           // K of the partial buffer layout
+    int op;              // with a dot: the per-image scalar step the last block runs (OP_*)
 };
 
 struct RefineWork {
@@ -151,6 +152,7 @@ struct RefineWork {
     Vec g, v1, p, r, y, s, gp, gm, z[2], pmask;   // z: this and the previous preconditioned residual
     Vec lz[RF_MAX_LZ + 1];
     double *part = nullptr;           // partial sums [F][K][nb]
+    unsigned *ticket = nullptr;       // per image: blocks that wrote their partials (last one finishes)
     double *dots = nullptr;           // [F][RF_DOTS]
     double *sc = nullptr;             // [F][NSC]
     double *coef = nullptr;           // [F][RF_MAX_LZ + 1] host-given coefficients
@@ -219,6 +221,7 @@ void refine_free(RefineWork *w)
     cudaFree(w->pc_probe);
     cudaFree(w->block);
     cudaFree(w->part);
+    cudaFree(w->ticket);
     cudaFree(w->dots);
     cudaFree(w->sc);
     cudaFree(w->coef);
@@ -259,156 +262,21 @@ __device__ __forceinline__ void vrange(long M2, int nb, long &r0, long &r1)
     r1 = min(M2, r0 + per);
 }
 
-// out = sum_t c_t in_t, per image; optional partial dot of out with dw.
-template <int NTT>
-__global__ void __launch_bounds__(NT) k_lincomb(LinArgs a, long M2, int nf, const double *sc, const double *coef,
-                                                int ccols, double *part, int nb)
+// Per-image sums of the partials of image n, then the scalar step `op`
+// (thread 0).  Run by a whole block: the last one of a dot kernel's blocks
+// for the image (ticket), or a k_dot_sums block.  The partials come through
+// L2 (other blocks wrote them).
+__device__ void dot_finish(const double *part, int K, int nb, double *dots, double *sc, int op, int n,
+                           unsigned *ticket, double *sh)
 {
-    __shared__ double sh[NT / 32];
-    const int n = blockIdx.y;
-    const bool on = a.gate < 0 || sc[n * NSC + a.gate] != 0.0;
-    double c[NTT];
-#pragma unroll
-    for (int k = 0; k < NTT; ++k) {
-        double v = a.t[k].mult;
-        if (a.t[k].s1 >= 0) v *= sc[n * NSC + a.t[k].s1];
-        if (a.t[k].s2 >= 0) v *= sc[n * NSC + a.t[k].s2];
-        if (a.t[k].cidx >= 0) v *= coef[n * ccols + a.t[k].cidx];
-        c[k] = v;
-    }
-    long r0, r1;
-    vrange(M2, nb, r0, r1);
-    const long off = (long)n * M2;
-    const bool dot = a.dw.p[0] != nullptr;
-    double acc = 0.0;
-    if (on)
-#pragma unroll
-        for (int f = 0; f < 3; ++f) {
-            if (f >= nf) break;
-            double2 *o = reinterpret_cast<double2 *>(a.out.p[f] + off);
-            const double2 *dw = dot ? reinterpret_cast<const double2 *>(a.dw.p[f] + off) : nullptr;
-            for (long r = r0 / 2 + threadIdx.x; r < r1 / 2; r += NT) {
-                double2 v = make_double2(0.0, 0.0);
-#pragma unroll
-                for (int k = 0; k < NTT; ++k) {
-                    const double2 x = reinterpret_cast<const double2 *>(a.in[k].p[f] + off)[r];
-                    v.x += c[k] * x.x;
-                    v.y += c[k] * x.y;
-                }
-                o[r] = v;
-                if (dot) {
-                    const double2 d = dw[r];
-                    acc += v.x * d.x + v.y * d.y;
-                }
-            }
-        }
-    if (dot) {
-        const double t = block_reduce(acc, sh);
-        if (threadIdx.x == 0) part[((long)n * a.dot_k + a.dot_slot) * nb + blockIdx.x] = t;
-    }
-}
-
-// Partial dots of up to 4 pairs (u_k, w_k) per image.
-struct DotArgs {
-    Vec u[4], w[4];
-    int k;
-};
-
-template <int K>
-__global__ void __launch_bounds__(NT) k_dots(DotArgs a, long M2, int nf, double *part, int nb)
-{
-    __shared__ double sh[NT / 32];
-    const int n = blockIdx.y;
-    long r0, r1;
-    vrange(M2, nb, r0, r1);
-    const long off = (long)n * M2;
-    double acc[K];
-#pragma unroll
-    for (int k = 0; k < K; ++k) acc[k] = 0.0;
-#pragma unroll
-    for (int f = 0; f < 3; ++f) {
-        if (f >= nf) break;
-        for (long r = r0 / 2 + threadIdx.x; r < r1 / 2; r += NT) {
-#pragma unroll
-            for (int k = 0; k < K; ++k) {
-                const double2 u = reinterpret_cast<const double2 *>(a.u[k].p[f] + off)[r];
-                const double2 w = reinterpret_cast<const double2 *>(a.w[k].p[f] + off)[r];
-                acc[k] += u.x * w.x + u.y * w.y;
-            }
-        }
-    }
-#pragma unroll
-    for (int k = 0; k < K; ++k) {
-        const double t = block_reduce(acc[k], sh);
-        if (threadIdx.x == 0) part[((long)n * K + k) * nb + blockIdx.x] = t;
-    }
-}
-
-// Partial dots of w with Lanczos vectors lz_0 .. lz_{K-1} (contiguous, stride vs;
-// array f of a vector at offset f * FM2).
-__global__ void __launch_bounds__(NT) k_dots_lz(Vec w, const double *lz0, size_t vs, int K, long M2, int nf,
-                                                long FM2, double *part, int nb)
-{
-    __shared__ double sh[NT / 32];
-    const int n = blockIdx.y;
-    long r0, r1;
-    vrange(M2, nb, r0, r1);
-    const long off = (long)n * M2;
-    for (int k = 0; k < K; ++k) {
-        double acc = 0.0;
-        for (int f = 0; f < nf; ++f) {
-            const double2 *b = reinterpret_cast<const double2 *>(lz0 + k * vs + f * FM2 + off);
-            const double2 *x = reinterpret_cast<const double2 *>(w.p[f] + off);
-            for (long r = r0 / 2 + threadIdx.x; r < r1 / 2; r += NT) {
-                const double2 u = b[r], v = x[r];
-                acc += u.x * v.x + u.y * v.y;
-            }
-        }
-        const double t = block_reduce(acc, sh);
-        if (threadIdx.x == 0) part[((long)n * K + k) * nb + blockIdx.x] = t;
-    }
-}
-
-// w = c0 w - sum_k d_k lz_k, d_k = d[n * dstride + k].
-__global__ void __launch_bounds__(NT) k_sub_lz(Vec w, double c0, const double *lz0, size_t vs, int K, long M2, int nf,
-                                               long FM2, const double *d, int dstride, const double *sc, int gate,
-                                               int nb)
-{
-    const int n = blockIdx.y;
-    if (gate >= 0 && sc[n * NSC + gate] == 0.0) return;
-    double dk[RF_MAX_LZ + 1];
-    for (int k = 0; k < K; ++k) dk[k] = d[n * dstride + k];
-    long r0, r1;
-    vrange(M2, nb, r0, r1);
-    const long off = (long)n * M2;
-    for (int f = 0; f < nf; ++f) {
-        double2 *x = reinterpret_cast<double2 *>(w.p[f] + off);
-        for (long r = r0 / 2 + threadIdx.x; r < r1 / 2; r += NT) {
-            double2 v = x[r];
-            v.x *= c0;
-            v.y *= c0;
-            for (int k = 0; k < K; ++k) {
-                const double2 b = reinterpret_cast<const double2 *>(lz0 + k * vs + f * FM2 + off)[r];
-                v.x -= dk[k] * b.x;
-                v.y -= dk[k] * b.y;
-            }
-            x[r] = v;
-        }
-    }
-}
-
-// Per-image sums of the partials, then the scalar step `op` (thread 0).
-__global__ void __launch_bounds__(NT) k_dot_sums(const double *part, int K, int nb, double *dots, double *sc, int op)
-{
-    __shared__ double sh[NT / 32];
-    const int n = blockIdx.x;
     double s[RF_DOTS];
     for (int k = 0; k < K; ++k) {
         double v = 0.0;
-        for (int b = threadIdx.x; b < nb; b += NT) v += part[((long)n * K + k) * nb + b];
+        for (int b = threadIdx.x; b < nb; b += NT) v += __ldcg(part + ((long)n * K + k) * nb + b);
         s[k] = block_reduce(v, sh);
     }
     if (threadIdx.x != 0) return;
+    if (ticket) ticket[n] = 0;   // ready for the next launch
     for (int k = 0; k < K; ++k) dots[n * RF_DOTS + k] = s[k];
     double *q = sc + n * NSC;
     const bool act = q[S_ACTIVE] != 0.0;
@@ -470,6 +338,170 @@ __global__ void __launch_bounds__(NT) k_dot_sums(const double *part, int K, int 
         }
         break;
     default: break;
+    }
+}
+
+// True in every thread of the last block of image n to have written its
+// partials (the partial writes are fenced before the ticket is taken).
+__device__ __forceinline__ bool last_block(unsigned *ticket, int n, int nb)
+{
+    __shared__ int is_last;
+    if (threadIdx.x == 0) {
+        __threadfence();
+        is_last = atomicAdd(ticket + n, 1u) == (unsigned)(nb - 1);
+    }
+    __syncthreads();
+    const bool last = is_last != 0;
+    if (last) __threadfence();
+    return last;
+}
+
+// Per-image sums of the partials, then the scalar step `op` (a separate launch,
+// for partials written by kernels without a ticket).
+__global__ void __launch_bounds__(NT) k_dot_sums(const double *part, int K, int nb, double *dots, double *sc, int op)
+{
+    __shared__ double sh[NT / 32];
+    dot_finish(part, K, nb, dots, sc, op, blockIdx.x, nullptr, sh);
+}
+
+// out = sum_t c_t in_t, per image; optional partial dot of out with dw.
+template <int NTT>
+__global__ void __launch_bounds__(NT) k_lincomb(LinArgs a, long M2, int nf, double *sc, const double *coef,
+                                                int ccols, double *part, int nb, unsigned *ticket, double *dots)
+{
+    __shared__ double sh[NT / 32];
+    const int n = blockIdx.y;
+    const bool on = a.gate < 0 || sc[n * NSC + a.gate] != 0.0;
+    double c[NTT];
+#pragma unroll
+    for (int k = 0; k < NTT; ++k) {
+        double v = a.t[k].mult;
+        if (a.t[k].s1 >= 0) v *= sc[n * NSC + a.t[k].s1];
+        if (a.t[k].s2 >= 0) v *= sc[n * NSC + a.t[k].s2];
+        if (a.t[k].cidx >= 0) v *= coef[n * ccols + a.t[k].cidx];
+        c[k] = v;
+    }
+    long r0, r1;
+    vrange(M2, nb, r0, r1);
+    const long off = (long)n * M2;
+    const bool dot = a.dw.p[0] != nullptr;
+    double acc = 0.0;
+    if (on)
+#pragma unroll
+        for (int f = 0; f < 3; ++f) {
+            if (f >= nf) break;
+            double2 *o = reinterpret_cast<double2 *>(a.out.p[f] + off);
+            const double2 *dw = dot ? reinterpret_cast<const double2 *>(a.dw.p[f] + off) : nullptr;
+            for (long r = r0 / 2 + threadIdx.x; r < r1 / 2; r += NT) {
+                double2 v = make_double2(0.0, 0.0);
+#pragma unroll
+                for (int k = 0; k < NTT; ++k) {
+                    const double2 x = reinterpret_cast<const double2 *>(a.in[k].p[f] + off)[r];
+                    v.x += c[k] * x.x;
+                    v.y += c[k] * x.y;
+                }
+                o[r] = v;
+                if (dot) {
+                    const double2 d = dw[r];
+                    acc += v.x * d.x + v.y * d.y;
+                }
+            }
+        }
+    if (dot) {
+        const double t = block_reduce(acc, sh);
+        if (threadIdx.x == 0) part[((long)n * a.dot_k + a.dot_slot) * nb + blockIdx.x] = t;
+        if (last_block(ticket, n, nb)) dot_finish(part, a.dot_k, nb, dots, sc, a.op, n, ticket, sh);
+    }
+}
+
+// Partial dots of up to 4 pairs (u_k, w_k) per image.
+struct DotArgs {
+    Vec u[4], w[4];
+    int k;
+};
+
+template <int K>
+__global__ void __launch_bounds__(NT) k_dots(DotArgs a, long M2, int nf, double *part, int nb, int op,
+                                             unsigned *ticket, double *dots, double *sc)
+{
+    __shared__ double sh[NT / 32];
+    const int n = blockIdx.y;
+    long r0, r1;
+    vrange(M2, nb, r0, r1);
+    const long off = (long)n * M2;
+    double acc[K];
+#pragma unroll
+    for (int k = 0; k < K; ++k) acc[k] = 0.0;
+#pragma unroll
+    for (int f = 0; f < 3; ++f) {
+        if (f >= nf) break;
+        for (long r = r0 / 2 + threadIdx.x; r < r1 / 2; r += NT) {
+#pragma unroll
+            for (int k = 0; k < K; ++k) {
+                const double2 u = reinterpret_cast<const double2 *>(a.u[k].p[f] + off)[r];
+                const double2 w = reinterpret_cast<const double2 *>(a.w[k].p[f] + off)[r];
+                acc[k] += u.x * w.x + u.y * w.y;
+            }
+        }
+    }
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+        const double t = block_reduce(acc[k], sh);
+        if (threadIdx.x == 0) part[((long)n * K + k) * nb + blockIdx.x] = t;
+    }
+    if (last_block(ticket, n, nb)) dot_finish(part, K, nb, dots, sc, op, n, ticket, sh);
+}
+
+// Partial dots of w with Lanczos vectors lz_0 .. lz_{K-1} (contiguous, stride vs;
+// array f of a vector at offset f * FM2).
+__global__ void __launch_bounds__(NT) k_dots_lz(Vec w, const double *lz0, size_t vs, int K, long M2, int nf,
+                                                long FM2, double *part, int nb)
+{
+    __shared__ double sh[NT / 32];
+    const int n = blockIdx.y;
+    long r0, r1;
+    vrange(M2, nb, r0, r1);
+    const long off = (long)n * M2;
+    for (int k = 0; k < K; ++k) {
+        double acc = 0.0;
+        for (int f = 0; f < nf; ++f) {
+            const double2 *b = reinterpret_cast<const double2 *>(lz0 + k * vs + f * FM2 + off);
+            const double2 *x = reinterpret_cast<const double2 *>(w.p[f] + off);
+            for (long r = r0 / 2 + threadIdx.x; r < r1 / 2; r += NT) {
+                const double2 u = b[r], v = x[r];
+                acc += u.x * v.x + u.y * v.y;
+            }
+        }
+        const double t = block_reduce(acc, sh);
+        if (threadIdx.x == 0) part[((long)n * K + k) * nb + blockIdx.x] = t;
+    }
+}
+
+// w = c0 w - sum_k d_k lz_k, d_k = d[n * dstride + k].
+__global__ void __launch_bounds__(NT) k_sub_lz(Vec w, double c0, const double *lz0, size_t vs, int K, long M2, int nf,
+                                               long FM2, const double *d, int dstride, const double *sc, int gate,
+                                               int nb)
+{
+    const int n = blockIdx.y;
+    if (gate >= 0 && sc[n * NSC + gate] == 0.0) return;
+    double dk[RF_MAX_LZ + 1];
+    for (int k = 0; k < K; ++k) dk[k] = d[n * dstride + k];
+    long r0, r1;
+    vrange(M2, nb, r0, r1);
+    const long off = (long)n * M2;
+    for (int f = 0; f < nf; ++f) {
+        double2 *x = reinterpret_cast<double2 *>(w.p[f] + off);
+        for (long r = r0 / 2 + threadIdx.x; r < r1 / 2; r += NT) {
+            double2 v = x[r];
+            v.x *= c0;
+            v.y *= c0;
+            for (int k = 0; k < K; ++k) {
+                const double2 b = reinterpret_cast<const double2 *>(lz0 + k * vs + f * FM2 + off)[r];
+                v.x -= dk[k] * b.x;
+                v.y -= dk[k] * b.y;
+            }
+            x[r] = v;
+        }
     }
 }
 
@@ -879,11 +911,13 @@ struct Ctx {
     {
         const double *cf = w->coef;
         const int cc = RF_MAX_LZ + 1;
+        unsigned *tk = w->ticket;
+        double *ds = w->dots;
         switch (a.nt) {
-        case 1: k_lincomb<1><<<vgrid(), NT, 0, st>>>(a, M2, w->nf, w->sc, cf, cc, w->part, w->nb); break;
-        case 2: k_lincomb<2><<<vgrid(), NT, 0, st>>>(a, M2, w->nf, w->sc, cf, cc, w->part, w->nb); break;
-        case 3: k_lincomb<3><<<vgrid(), NT, 0, st>>>(a, M2, w->nf, w->sc, cf, cc, w->part, w->nb); break;
-        default: k_lincomb<4><<<vgrid(), NT, 0, st>>>(a, M2, w->nf, w->sc, cf, cc, w->part, w->nb); break;
+        case 1: k_lincomb<1><<<vgrid(), NT, 0, st>>>(a, M2, w->nf, w->sc, cf, cc, w->part, w->nb, tk, ds); break;
+        case 2: k_lincomb<2><<<vgrid(), NT, 0, st>>>(a, M2, w->nf, w->sc, cf, cc, w->part, w->nb, tk, ds); break;
+        case 3: k_lincomb<3><<<vgrid(), NT, 0, st>>>(a, M2, w->nf, w->sc, cf, cc, w->part, w->nb, tk, ds); break;
+        default: k_lincomb<4><<<vgrid(), NT, 0, st>>>(a, M2, w->nf, w->sc, cf, cc, w->part, w->nb, tk, ds); break;
         }
         c->launches += 1;
         return cudaGetLastError();
@@ -903,16 +937,16 @@ struct Ctx {
             a.w[a.k] = pr.second;
             ++a.k;
         }
+        unsigned *tk = w->ticket;
+        double *ds = w->dots, *scw = w->sc;
         switch (a.k) {
-        case 1: k_dots<1><<<vgrid(), NT, 0, st>>>(a, M2, w->nf, w->part, w->nb); break;
-        case 2: k_dots<2><<<vgrid(), NT, 0, st>>>(a, M2, w->nf, w->part, w->nb); break;
-        case 3: k_dots<3><<<vgrid(), NT, 0, st>>>(a, M2, w->nf, w->part, w->nb); break;
-        default: k_dots<4><<<vgrid(), NT, 0, st>>>(a, M2, w->nf, w->part, w->nb); break;
+        case 1: k_dots<1><<<vgrid(), NT, 0, st>>>(a, M2, w->nf, w->part, w->nb, op, tk, ds, scw); break;
+        case 2: k_dots<2><<<vgrid(), NT, 0, st>>>(a, M2, w->nf, w->part, w->nb, op, tk, ds, scw); break;
+        case 3: k_dots<3><<<vgrid(), NT, 0, st>>>(a, M2, w->nf, w->part, w->nb, op, tk, ds, scw); break;
+        default: k_dots<4><<<vgrid(), NT, 0, st>>>(a, M2, w->nf, w->part, w->nb, op, tk, ds, scw); break;
         }
         c->launches += 1;
-        cudaError_t e = cudaGetLastError();
-        if (e != cudaSuccess) return e;
-        return sums(a.k, op);
+        return cudaGetLastError();   // the last block of each image sums and runs `op`
     }
     cudaError_t read_scalars()
     {
@@ -1528,8 +1562,8 @@ mepgl_status cg_iteration(Ctx &R, bool pc, int k)
     a.dw = w->p;
     a.dot_k = 1;
     a.dot_slot = 0;
+    a.op = OP_ALPHA;
     RK(R.lin(a));
-    RK(R.sums(1, OP_ALPHA));
     a = lin_args(w->s, S_ACTIVE);
     add_term(a, w->s, 1.0);
     add_term(a, w->p, 1.0, S_ALPHA);
@@ -1546,8 +1580,8 @@ mepgl_status cg_iteration(Ctx &R, bool pc, int k)
         a.dw = w->r;
         a.dot_k = 1;
         a.dot_slot = 0;
+        a.op = OP_BETA;
         RK(R.lin(a));
-        RK(R.sums(1, OP_BETA));
     }
     a = lin_args(w->p, S_ACTIVE);
     add_term(a, pc ? w->z[k & 1] : w->r, 1.0);
@@ -1580,8 +1614,8 @@ mepgl_status cg_solve(Ctx &R, int max_it, bool pc)
         a.dw = w->r;   // |r|^2
         a.dot_k = 1;
         a.dot_slot = 0;
+        a.op = OP_CGINIT;
         RK(R.lin(a));
-        RK(R.sums(1, OP_CGINIT));
     }
     a = lin_args(w->p, S_ACTIVE);
     add_term(a, pc ? w->z[1] : w->r, 1.0);
@@ -1675,6 +1709,8 @@ mepgl_status alloc_work(mepgl_ctx *c)
         *v = vec(k++);
     const size_t parts = (size_t)w->F * std::max(RF_DOTS, RF_MAX_GB) * w->nb;
     e = cudaMalloc(&w->part, parts * sizeof(double));
+    if (e == cudaSuccess) e = cudaMalloc(&w->ticket, (size_t)w->F * sizeof(unsigned));
+    if (e == cudaSuccess) e = cudaMemsetAsync(w->ticket, 0, (size_t)w->F * sizeof(unsigned), c->stream);
     if (e == cudaSuccess) e = cudaMalloc(&w->dots, (size_t)w->F * RF_DOTS * sizeof(double));
     if (e == cudaSuccess) e = cudaMalloc(&w->sc, (size_t)w->F * NSC * sizeof(double));
     if (e == cudaSuccess) e = cudaMalloc(&w->coef, (size_t)w->F * (RF_MAX_LZ + 1) * sizeof(double));
