@@ -1102,7 +1102,9 @@ mepgl_status mepgl_energy_grad(mepgl_ctx *c, double *fenergy, void *g_a, void *g
         out.p[1] = g_psi_1;
         out.p[2] = c->ncomp == 2 ? g_psi_2 : nullptr;
     }
-    CK(c, launch_gradient_only(string_launch(c, 0), c->xi, out, 0));
+    Launch L = string_launch(c, 0);
+    L.paired = 0;   // the gradient a caller asks for is IEEE double in every FP64 mode
+    CK(c, launch_gradient_only(L, c->xi, out, 0));
     c->launches += 1;
     if (direct) {
         CK(c, cudaStreamSynchronize(c->stream));

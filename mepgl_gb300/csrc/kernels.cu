@@ -898,7 +898,9 @@ __global__ void __launch_bounds__(NT) k_gradient_only(const __grid_constant__ Ba
                     hd = h_site(S, p, gj > 0 ? s - S.nx : s);
                 }
                 T g[2 + 2 * NC];
-                if (S.disc) {
+                if constexpr (std::is_same<T, ff>::value) {   // float-float: the reference form only
+                    site_gradient<T, NC, TYT>(t, lx + 1, ly + 1, p, w, hr, hl, hu, hd, maxwell, S.thin_film, g);
+                } else if (S.disc) {
                     T hmx_l[2] = {p.hmx[0], p.hmx[1]}, hmy_d[2] = {p.hmy[0], p.hmy[1]};
                     if (S.per_site)
                         for (int c = 0; c < NC; ++c) {
@@ -915,7 +917,7 @@ __global__ void __launch_bounds__(NT) k_gradient_only(const __grid_constant__ Ba
                     V gv;
                     gv.x = g[2 * c];
                     gv.y = g[2 * c + 1];
-                    (static_cast<V *>(out.p[c]) + off)[s] = gv;
+                    store2<T>(static_cast<vec2_t<store_t<T>> *>(out.p[c]) + off + s, gv);
                 }
             }
         }
@@ -1809,9 +1811,17 @@ cudaError_t launch_energy(const Launch &L, const Scalars &sc, int xbuf, double *
     return cudaGetLastError();
 }
 
+// FP64 launches with L.paired compute in float-float on the double fields
+// (about 48 bits) and store double gradients; the link discretisation has
+// no float-float form and stays IEEE double.
 cudaError_t launch_gradient_only(const Launch &L, int xbuf, FieldPtrs out, int maxwell)
 {
-    DISPATCH(L, k_gradient_only, *L.batch, L.tiles, L.n_tiles, xbuf, out, maxwell);
+    if (L.paired && L.precision == 1 && !L.batch->s[0].disc) {
+        if (L.ncomp == 2) k_gradient_only<ff, 2><<<L.grid, NT, 0, L.stream>>>(*L.batch, L.tiles, L.n_tiles, xbuf, out, maxwell);
+        else k_gradient_only<ff, 1><<<L.grid, NT, 0, L.stream>>>(*L.batch, L.tiles, L.n_tiles, xbuf, out, maxwell);
+    } else {
+        DISPATCH(L, k_gradient_only, *L.batch, L.tiles, L.n_tiles, xbuf, out, maxwell);
+    }
     return cudaGetLastError();
 }
 

@@ -69,6 +69,7 @@ cudaError_t launch_energy(const Launch &L, const Scalars &sc, int xbuf, double *
 cudaError_t launch_param_adjoint(const Launch &L, const Scalars &sc, int xbuf, double *out);
 // Gradient of x[xbuf] into the three arrays of `out` (single string).
 struct FieldPtrs { void *p[3]; };
+// Gradient of every image into `out` (FP64 launches with L.paired: float-float arithmetic).
 cudaError_t launch_gradient_only(const Launch &L, int xbuf, FieldPtrs out, int maxwell);
 // B, J of x[xbuf] written to per-string arrays (b: F*M reals, j: F*M pairs).
 cudaError_t launch_jb(const Launch &L, const Scalars &sc, int xbuf, void *const *b, void *const (*j)[2]);
