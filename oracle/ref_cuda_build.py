@@ -1,4 +1,4 @@
-"""Build and time the reference's own CUDA NLCG on this GPU (BASELINE ONLY).
+"""Build and time the reference's own CUDA NLCG on this GPU (a timing baseline only).
 
 The reference compiles its kernels for sm_61 with N, dx, the component count
 and the precision fixed at compile time (mepgl/src/CMakeLists.txt:5-13,

@@ -1,4 +1,4 @@
-// ref_cuda_driver.cu -- times the reference's own CUDA NLCG (BASELINE ONLY).
+// ref_cuda_driver.cu -- times the reference's own CUDA NLCG (a timing baseline only).
 //
 // Links against the reference's unmodified nlcg.cu and parallel_sum.cu,
 // compiled for this GPU by oracle/ref_cuda_build.py with a generated
