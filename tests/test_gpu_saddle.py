@@ -124,6 +124,32 @@ def test_minima_of_a_two_component_string_match_the_oracle_refiner(native):
         np.testing.assert_allclose(rep[k]["energy"], ref["energy"], rtol=ENERGY_RTOL)
 
 
+@pytest.mark.parametrize("case", ["thin_film", "tiny"])
+def test_minimum_refinement_edge_cases_match_the_oracle_refiner(native, case):
+    """A thin film (A fixed: no gauge basis, the A dofs masked out of the
+    preconditioner) and a 4 x 4 lattice (too small for the preconditioner's
+    probe comb: plain CG) refine image 0 to the oracle refiner's minimum.  On
+    16 sites the automatic gauge basis (14 functions) is degenerate, so the
+    4 x 4 case runs both refiners without gauge steps."""
+    deg = -1
+    if case == "thin_film":
+        prob, st = W.config1(n=16, images=3)
+        prob = prob.with_(thin_film=True)
+    else:
+        prob, st = W.config1(n=4, images=3, margin=0)
+        deg = 0
+    sub = StringState(a=st.a[0:1], psi_1=st.psi_1[0:1])
+    with native.StringContext(prob, 1, "fp64") as c:
+        c.set_state(sub)
+        rep = c.refine_stationary([native.STATIONARY_MINIMUM], g_tol=1e-9, max_newton=40, gauge_degree=deg)
+    assert rep[0]["converged"], rep
+    assert rep[0]["preconditioned"] == (1 if case == "thin_film" else 0), rep
+    o = cref.Oracle(prob)
+    R = SR.Refiner(o, deg=None if deg < 0 else deg)
+    _, ref = R.refine(R.pack(sub.a, sub.psi_1), SR.MINIMUM, g_tol=1e-9)
+    np.testing.assert_allclose(rep[0]["energy"], ref["energy"], rtol=ENERGY_RTOL, atol=1e-12)
+
+
 def test_preconditioned_and_plain_cg_reach_the_same_stationary_points(config1_barrier):
     from mepgl_gb300 import saddle
     prob, st, fe, r = config1_barrier
