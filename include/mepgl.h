@@ -395,7 +395,8 @@ typedef struct mepgl_refine_options {
     int32_t max_cg;            /* CG iterations per linear solve (default 3000)   */
     int32_t lanczos_steps;     /* per min-mode update (default 12, 30 at start)   */
     int32_t gauge_degree;      /* gauge polynomial degree <= 16, 0 = off,
-                                  -1 = auto: max(nx, ny) / 8 within 4..16 (default) */
+                                  -1 = auto: max(nx, ny) / 8 within 4..16, at most
+                                  min(nx, ny) / 2 (default)                        */
     double mu0;                /* initial Levenberg-Marquardt shift (1e-3)        */
     double cg_eta;             /* CG relative tolerance (0.1), see `forcing`      */
     int32_t max_retries;       /* rejected steps retried per iteration (8)        */

@@ -1830,7 +1830,11 @@ mepgl_status mepgl_refine_stationary(mepgl_ctx *c, const int32_t *kind, const vo
     memset(&B, 0, sizeof(B));
     // auto: one degree per 8 lattice sites of the longer side, 4 to 16
     const int nmax = std::max(s.nx, s.ny);
-    B.deg = opt.gauge_degree >= 0 ? opt.gauge_degree : std::min(RF_MAX_DEG, std::max(4, nmax / 8));
+    // (and at most half the shorter side, where a higher degree has too few
+    // rows or columns to be a well-posed basis)
+    const int nmin = std::min(s.nx, s.ny);
+    B.deg = opt.gauge_degree >= 0 ? opt.gauge_degree
+                                  : std::min(std::min(RF_MAX_DEG, std::max(4, nmax / 8)), std::max(1, nmin / 2));
     if (c->thin_film) B.deg = 0;
     for (int d = 1; d <= B.deg; ++d)
         for (int k = 0; k <= d; ++k) {

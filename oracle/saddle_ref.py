@@ -9,7 +9,7 @@ The algorithm is the same in outline, written in numpy:
 
 * gauge step: minimise F(U_chi x) over chi = sum_m c_m P_a(X) P_b(Y)
   (Legendre products, 1 <= a + b <= degree, by default max(nx, ny) / 8
-  within 4..16) by Newton on the coefficients, with U_chi: A -> A + grad chi
+  within 4..16 and at most min(nx, ny) / 2) by Newton on the coefficients, with U_chi: A -> A + grad chi
   (central differences, one-sided at the lattice edge),
   psi_a -> psi_a exp(i q_a chi);
 * saddles: lowest Hessian mode by Lanczos (full reorthogonalisation),
@@ -36,7 +36,7 @@ class Refiner:
         self.nc = self.p.ncomp
         ny, nx = self.p.ny, self.p.nx
         if deg is None:     # the library's automatic degree
-            deg = min(16, max(4, max(nx, ny) // 8))
+            deg = min(16, max(4, max(nx, ny) // 8), max(1, min(nx, ny) // 2))
         J, I = np.meshgrid(np.arange(ny), np.arange(nx), indexing="ij")
         X = (2.0 * I - (nx - 1)) / (nx - 1)
         Y = (2.0 * J - (ny - 1)) / (ny - 1)
