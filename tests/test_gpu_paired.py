@@ -94,3 +94,21 @@ def test_paired_loop_and_batches(native):
         out.append([b.string_free_energy(k) for k in range(2)])
     for a, d in zip(*out):
         np.testing.assert_allclose(a, d, rtol=1e-9)
+
+
+@pytest.mark.parametrize("mc", [True, False])
+def test_energy_grad_of_a_paired_context_is_ieee_double(native, mc):
+    """mepgl_energy_grad returns the IEEE double gradient in every FP64 mode:
+    a paired context's gradient equals a native context's bit for bit (the
+    float-float gradient-only form serves the refinement's internal gauge
+    Hessian only)."""
+    prob, st = _case(21 + int(mc), mc=mc)
+    out = []
+    for paired in (False, True):
+        with _ctx(native, prob, st, paired) as c:
+            out.append(c.energy_grad())
+    (e0, g0), (e1, g1) = out
+    np.testing.assert_array_equal(e0, e1)
+    for a, b in zip(g0, g1):
+        if a is not None:
+            np.testing.assert_array_equal(a, b)
