@@ -440,7 +440,11 @@ def run_ours(args):
     ttb = None
     if rank == 0 and not args.no_ttb:
         from mepgl_gb300 import barrier as B
-        cfg, relax, reps, budget = args.ttb_config, 10, args.ttb_repeats, args.ttb_string
+        # the 64x64 string seeds its saddle at one NLCG step per reparametrization
+        # (600 iterations, the oracle golden's protocol); the 256x256 one at 10 (300)
+        cfg, reps = args.ttb_config, args.ttb_repeats
+        relax = 1 if cfg == 1 else 10
+        budget = args.ttb_string if args.ttb_string is not None else (600 if cfg == 1 else 300)
         ref = B.time_to_barrier(cfg, "fp64", relax, max_string=budget, g_tol=1e-10)
         target = ref["barrier"]
         runs = {"fp64": [ref], "mixed": [], "fp64_paired": []}
@@ -508,8 +512,9 @@ def main(argv=None):
     ap.add_argument("--ttb-config", type=int, choices=(1, 2), default=2,
                     help="workload of that leg: 2 (the 256x256 mixed-precision string) or 1 (64x64, seconds)")
     ap.add_argument("--ttb-repeats", type=int, default=3, help="runs per schedule of the time-to-barrier leg")
-    ap.add_argument("--ttb-string", type=int, default=300,
-                    help="string-phase budget (outer iterations of 10 NLCG steps) of the time-to-barrier leg")
+    ap.add_argument("--ttb-string", type=int, default=None,
+                    help="string-phase budget of the time-to-barrier leg in outer iterations (default 300 of 10 "
+                         "NLCG steps on the 256x256 string, 600 of 1 step on the 64x64 one)")
     args = ap.parse_args(argv)
     if args.impl == "reference":
         return run_reference(args)
